@@ -1,0 +1,69 @@
+/*
+ * engine.h -- internal contract between the host layer (world, objects,
+ * sources, phasers, observers: files in this directory) and a stepping
+ * backend.
+ *
+ * The host layer owns the ALiS data model exactly as the public structs
+ * describe it (geometry, 1-D coefficient tables, material maps, source
+ * descriptors, phaser descriptors) and keeps host mirrors of every field.
+ * A backend owns the time stepping: updateE, updateH, updatePhaser and the
+ * near-to-far sums.  The product backend (../gpu) keeps the live state in
+ * HBM and runs CUDA kernels; the hooks below tell it when host-side setup
+ * changed and when host mirrors must be refreshed.
+ */
+#ifndef ALIS_ENGINE_H
+#define ALIS_ENGINE_H
+
+#include "alis_c.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- hooks the host layer calls; every backend implements them ---- */
+
+/* W (a user world or a TFSF auxiliary world) was created; host arrays exist. */
+void alis_be_world_created(world W);
+/* W is about to be freed. */
+void alis_be_world_deleted(world W);
+/* Materials, ADE maps/coefficients or the eps^-1 maps of W changed. */
+void alis_be_objects_changed(world W);
+/* Sources or TFSF boxes of W changed (also scalars such as coskx). */
+void alis_be_sources_changed(world W);
+/* rebootWorld: fields, psi, J/K and time were reset on the host. */
+void alis_be_world_reset(world W);
+/* Bring host mirrors of W's fields (and J/K) up to date. */
+void alis_be_sync_world(world W);
+/* A phaser set (array ending with f == 0) was created / is deleted. */
+void alis_be_phaser_created(phaser P);
+void alis_be_phaser_deleted(phaser P);
+/* Bring host mirrors of a phaser set's accumulators up to date.
+ * P may point at any element of the set. */
+void alis_be_sync_phaser(phaser P);
+/* Flush and sync everything the backend holds (end of a timed loop). */
+void alis_be_sync_all(void);
+
+/*
+ * Near-to-far-field face sums for one phaser and a batch of nA directions.
+ * T[a] are the test fields (host, indexed [kMIN..kMax+1]); kx[a], ky[a] the
+ * lateral wave numbers.  out[a] receives the sum over all PML-side faces of
+ * the farFieldX/Y/Z bilinear forms (reference src/farfld.c:248-459,
+ * 488-493), before the lattice factor and normalisation.
+ */
+void alis_be_farfield_sums(phaser P, int nA, const tfield *T, const float *kx,
+                           const float *ky, double complex *out);
+
+/* ---- helpers the host layer provides to backends ---- */
+
+/* Per-source value for the current half step, following the reference
+ * updateS (src/update.c:161-179): f = waveForm(t, phase) unless the source
+ * carries a Phase map.  Returns 0 if the source is inactive this step. */
+int alis_source_active(world W, source S);
+
+/* Index helpers for the lazy-sync check used by field functions. */
+#define ALIS_SYNC(W) alis_be_sync_world(W)
+
+#ifdef __cplusplus
+}
+#endif
+#endif

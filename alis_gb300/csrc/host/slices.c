@@ -1,0 +1,422 @@
+/*
+ * slices.c -- 1-D / 2-D cuts of a field function: snapshots, time
+ * averages and single-frequency DFTs written as text or PNG images.
+ *
+ * Visualisation side of the reference src/slices.c.  PNG files are
+ * produced by a small encoder in this file (uncompressed deflate blocks),
+ * so no libpng is needed; HDF5 output is not built.  Graded grids are
+ * resampled to the uniform base spacing before writing, as in the
+ * reference's bilinear interpolation.
+ */
+#include <sys/stat.h>
+#include <string.h>
+#include <limits.h>
+#include <stdint.h>
+#include "engine.h"
+
+/* --- graded-grid resampling (reference src/slices.c:25-64) --- */
+
+static float ***resample(world W, slice S, float ***F)
+{
+	float ***T, ***G = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
+	if (S->iMin != S->iMIN || S->iMax != S->iMAX) {
+		T = F, F = G, G = T;
+		for (int i = S->iMin; i < S->iMax; i++) {
+			float x0 = W->itox(W, i), x1 = W->itox(W, i+1);
+			int n0 = x0/W->dx+(i>0?1:0), n1 = x1/W->dx-(i<0?1:0);
+			for (int j = S->jMin; j <= S->jMax; j++) for (int n = n0; n <= n1; n++) for (int k = S->kMin; k <= S->kMax; k++)
+				F[n][j][k] = (G[i][j][k] * (x1 - n*W->dx) + G[i+1][j][k] * (n*W->dx - x0)) / (x1 - x0);
+		}
+	}
+	if (S->jMin != S->jMIN || S->jMax != S->jMAX) {
+		T = F, F = G, G = T;
+		for (int j = S->jMin; j < S->jMax; j++) {
+			float y0 = W->jtoy(W, j), y1 = W->jtoy(W, j+1);
+			int n0 = y0/W->dy+(j>0?1:0), n1 = y1/W->dy-(j<0?1:0);
+			for (int i = S->iMIN; i <= S->iMAX; i++) for (int n = n0; n <= n1; n++) for (int k = S->kMin; k <= S->kMax; k++)
+				F[i][n][k] = (G[i][j][k] * (y1 - n*W->dy) + G[i][j+1][k] * (n*W->dy - y0)) / (y1 - y0);
+		}
+	}
+	if (S->kMin != S->kMIN || S->kMax != S->kMAX) {
+		T = F, F = G, G = T;
+		for (int k = S->kMin; k < S->kMax; k++) {
+			float z0 = W->ktoz(W, k), z1 = W->ktoz(W, k+1);
+			int n0 = z0/W->dz+(k>0?1:0), n1 = z1/W->dz-(k<0?1:0);
+			for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int n = n0; n <= n1; n++)
+				F[i][j][n] = (G[i][j][k] * (z1 - n*W->dz) + G[i][j][k+1] * (n*W->dz - z0)) / (z1 - z0);
+		}
+	}
+	removeField(G, S->iMIN, S->jMIN, S->kMIN);
+	return F;
+}
+
+/* slice through the given box, clipped to the grid; 2-D slices of a
+ * world with objects also carry a normalised index-contour overlay
+ * (reference src/slices.c:67-117) */
+slice createSlice(world W, float xMin, float xMax, float yMin, float yMax, float zMin, float zMax)
+{
+	slice S;
+	MALLOC(S, 0, 1);
+	*S = (struct slice) { W->xtoi(W, xMin), W->xtoi(W, xMax), W->ytoj(W, yMin), W->ytoj(W, yMax), W->ztok(W, zMin), W->ztok(W, zMax) };
+	if (W->Res.nug.x.m>1 || W->Res.nug.y.m>1 || W->Res.nug.z.m>1) S->interpolate = resample;
+	if (S->iMax > W->iMAX) S->iMax = W->iMAX;
+	if (S->jMax > W->jMAX) S->jMax = W->jMAX;
+	if (S->kMax > W->kMAX) S->kMax = W->kMAX;
+	if (S->iMin < W->iMIN && W->xMinSur!=SYM) S->iMin = W->iMIN;
+	if (S->jMin < W->jMIN && W->yMinSur!=SYM) S->jMin = W->jMIN;
+	if (S->kMin < W->kMIN && W->zMinSur!=SYM) S->kMin = W->kMIN;
+	if (S->iMin <-W->iMAX && W->xMinSur==SYM) S->iMin =-W->iMAX;
+	if (S->jMin <-W->jMAX && W->yMinSur==SYM) S->jMin =-W->jMAX;
+	if (S->kMin <-W->kMAX && W->zMinSur==SYM) S->kMin =-W->kMAX;
+	S->iMIN = (S->iMin==S->iMax || !S->interpolate) ? S->iMin : MIN(S->iMin, W->itox(W, S->iMin)/W->dx);
+	S->jMIN = (S->jMin==S->jMax || !S->interpolate) ? S->jMin : MIN(S->jMin, W->jtoy(W, S->jMin)/W->dy);
+	S->kMIN = (S->kMin==S->kMax || !S->interpolate) ? S->kMin : MIN(S->kMin, W->ktoz(W, S->kMin)/W->dz);
+	S->iMAX = (S->iMin==S->iMax || !S->interpolate) ? S->iMax : MAX(S->iMax, W->itox(W, S->iMax)/W->dx);
+	S->jMAX = (S->jMin==S->jMax || !S->interpolate) ? S->jMax : MAX(S->jMax, W->jtoy(W, S->jMax)/W->dy);
+	S->kMAX = (S->kMin==S->kMax || !S->interpolate) ? S->kMax : MAX(S->kMax, W->ktoz(W, S->kMax)/W->dz);
+	S->iNUM = 1-S->iMIN+S->iMAX;
+	S->jNUM = 1-S->jMIN+S->jMAX;
+	S->kNUM = 1-S->kMIN+S->kMAX;
+	S->F = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
+	if (!W->CE->x || !W->CE->y || !W->CE->z || (S->iMin!=S->iMax && S->jMin!=S->jMax && S->kMin!=S->kMax)) return S;
+	float Max = 0;
+	S->C = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
+	for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++)
+		if (Max < (S->C[i][j][k] = ContourRI(W, i, j, k))) Max = S->C[i][j][k];
+	if (Max) for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++)
+		S->C[i][j][k] = 0.5*S->C[i][j][k]/Max;
+	return S;
+}
+
+void deleteSlice(slice S)
+{
+	if (S->F) removeField(S->F, S->iMIN, S->jMIN, S->kMIN);
+	if (S->C) removeField(S->C, S->iMIN, S->jMIN, S->kMIN);
+	free(S);
+}
+
+
+/* --- writers (reference src/slices.c:128-211) --- */
+
+void (h5)(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
+{
+	(void)W; (void)S; (void)Max; (void)F; (void)filename; (void)cmap;
+	fprintf(stderr, "alis: h5 slice output is unavailable (built without HDF5)\n");
+	exit(1);
+}
+
+void (txt)(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
+{
+	(void)Max; (void)F; (void)cmap;
+	int d = 0, dim[3] = {0};
+	FILE *File = fopen(strcat(filename, ".txt"), "w");
+	if (!File) return;
+	if (S->iMin != S->iMax) dim[d++] = S->iNUM;
+	if (S->jMin != S->jMax) dim[d++] = S->jNUM;
+	if (S->kMin != S->kMax) dim[d++] = S->kNUM;
+	if (d == 3) printf("Can't write 3D slice to txt file.\n"), exit(0);
+	if (d == 1) {
+		if (S->iMin != S->iMax) for (int i = S->iMin; i <= S->iMax; i++) fprintf(File, "%f\t%e\n", W->itox(W, i), S->F[i][S->jMin][S->kMin]);
+		if (S->jMin != S->jMax) for (int j = S->jMin; j <= S->jMax; j++) fprintf(File, "%f\t%e\n", W->jtoy(W, j), S->F[S->iMin][j][S->kMin]);
+		if (S->kMin != S->kMax) for (int k = S->kMin; k <= S->kMax; k++) fprintf(File, "%f\t%e\n", W->ktoz(W, k), S->F[S->iMin][S->jMin][k]);
+	} else {
+		if (S->interpolate) S->F = S->interpolate(W, S, S->F);
+		float *base = &S->F[S->iMIN][S->jMIN][S->kMIN];
+		for (int j = dim[1]-1; j >= 0; j--) {
+			fprintf(File, "%e", base[j]);
+			for (int i = 1; i < dim[0]; i++) fprintf(File, "\t%e", base[dim[1]*i+j]);
+			fprintf(File, "\n");
+		}
+	}
+	fclose(File);
+}
+
+/* minimal PNG: RGB8, one IDAT of stored (uncompressed) deflate blocks */
+static uint32_t crcTable[256];
+static void crcInit(void)
+{
+	for (uint32_t n = 0; n < 256; n++) {
+		uint32_t c = n;
+		for (int k = 0; k < 8; k++) c = c & 1 ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+		crcTable[n] = c;
+	}
+}
+static uint32_t crc(uint32_t c, const unsigned char *b, size_t n)
+{
+	for (size_t q = 0; q < n; q++) c = crcTable[(c ^ b[q]) & 0xFF] ^ (c >> 8);
+	return c;
+}
+static void put32(unsigned char *p, uint32_t v) { p[0] = v>>24, p[1] = v>>16, p[2] = v>>8, p[3] = v; }
+static void chunk(FILE *f, const char *type, const unsigned char *data, size_t n)
+{
+	unsigned char h[8];
+	put32(h, n);
+	memcpy(h+4, type, 4);
+	fwrite(h, 1, 8, f);
+	if (n) fwrite(data, 1, n, f);
+	uint32_t c = crc(0xFFFFFFFFu, (const unsigned char*)type, 4);
+	c = crc(c, data, n) ^ 0xFFFFFFFFu;
+	put32(h, c);
+	fwrite(h, 1, 4, f);
+}
+static void writePNG(FILE *f, int w, int h, const unsigned char *rgb)
+{
+	static int init;
+	if (!init) crcInit(), init = 1;
+	size_t raw = (size_t)h*(1+3*w), blocks = (raw+65534)/65535;
+	unsigned char *z = malloc(2 + raw + 5*blocks + 4), *p = z;
+	uint32_t a = 1, b = 0;
+	*p++ = 0x78, *p++ = 0x01;
+	size_t left = raw, row = 0, col = 0;
+	while (left) {
+		size_t n = left < 65535 ? left : 65535;
+		*p++ = left == n;
+		*p++ = n & 0xFF, *p++ = n >> 8, *p++ = ~n & 0xFF, *p++ = (~n >> 8) & 0xFF;
+		for (size_t q = 0; q < n; q++) {
+			unsigned char v = col == 0 ? 0 : rgb[row*3*w + col-1];
+			*p++ = v;
+			a = (a + v) % 65521, b = (b + a) % 65521;
+			if (++col == (size_t)(1+3*w)) col = 0, row++;
+		}
+		left -= n;
+	}
+	put32(p, (b << 16) | a), p += 4;
+	unsigned char ihdr[13];
+	put32(ihdr, w), put32(ihdr+4, h);
+	ihdr[8] = 8, ihdr[9] = 2, ihdr[10] = ihdr[11] = ihdr[12] = 0;
+	fwrite("\x89PNG\r\n\x1a\n", 1, 8, f);
+	chunk(f, "IHDR", ihdr, 13);
+	chunk(f, "IDAT", z, p - z);
+	chunk(f, "IEND", 0, 0);
+	free(z);
+}
+
+/* colour-mapped image of a 1-D (64 rows high) or 2-D slice with the index
+ * contour overlay for field quantities (reference src/slices.c:167-211) */
+void (png)(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
+{
+	int d = 0, dim[3] = {1, 1, 1};
+	float Min = 0;
+	if (cmap[0] > LONG_MAX) Min = -Max;
+	if (F[0]=='L' && F[1]=='o' && F[2]=='g' && F[3]!='R' && F[4]!='I') Min = Max-3;
+	if (S->iMin != S->iMax) dim[d++] = S->iNUM;
+	if (S->jMin != S->jMax) dim[d++] = S->jNUM;
+	if (S->kMin != S->kMax) dim[d++] = S->kNUM;
+	if (d == 1) dim[2] = 64;
+	if (d == 3) printf("Can't write 3D slice to png file.\n"), exit(0);
+	FILE *File = fopen(strcat(filename, ".png"), "wb");
+	if (!File) return;
+	if (S->interpolate) S->F = S->interpolate(W, S, S->F);
+	int stops = labs((long)cmap[0]);
+	unsigned char *img = malloc((size_t)3*dim[0]*dim[1]*dim[2]);
+	float *base = &S->F[S->iMIN][S->jMIN][S->kMIN];
+	float *cb = S->C ? &S->C[S->iMIN][S->jMIN][S->kMIN] : 0;
+	int plain = F[0]!='E' && F[0]!='H' && F[0]!='J' && F[0]!='U' && F[0]!='S' && F[0]!='i';
+	for (int r = 0, j = dim[1]-1; j >= 0; j--) {
+		unsigned char *row = img + (size_t)3*dim[0]*r;
+		for (int i = 0; i < dim[0]; i++) {
+			float C = !cb ? 1 : 1-cb[dim[1]*i+j];
+			float f = (Max-Min) ? MAX(0, MIN(stops-1, (stops-1)*(base[dim[1]*i+j]-Min)/(Max-Min))) : 0;
+			int n = f;
+			if (plain) C = 1;
+			if (n > stops-2) n = stops-2;
+			for (int c = 0; c < 3; c++) {
+				int sh = 16 - 8*c;
+				row[3*i+c] = C * ((1-f+n) * (cmap[n+1]>>sh&0xFF) + (f-n) * (cmap[n+2]>>sh&0xFF));
+			}
+		}
+		for (int q = 1; q < dim[2]; q++) memcpy(img + (size_t)3*dim[0]*(r+q), row, 3*dim[0]);
+		r += dim[2];
+	}
+	writePNG(File, dim[0], dim[1]*dim[2], img);
+	free(img);
+	fclose(File);
+}
+
+
+/* --- per-call-site state (reference src/slices.c:214-239) --- */
+
+typedef struct sliceq {
+	world W;
+	method M;
+	char *name;
+	float max, Max, ***F, ***G;
+	long N;
+	struct sliceq *next;
+} sliceq;
+
+static sliceq *track(world W, char *ID, method M, sliceq **head)
+{
+	sliceq *q;
+	for (q = *head; q; q = q->next) if (q->W == W && q->M == M && !strcmp(q->name, ID)) break;
+	if (!q) {
+		q = calloc(1, sizeof *q);
+		q->W = W, q->M = M, q->name = strdup(ID);
+		q->next = *head, *head = q;
+		strcat(strcpy(ID, W->ID), q->name);
+		if (q->name[0]=='/') mkdir(W->ID, 0755);
+		if (ID[0] && ID[strlen(ID)-1]=='/') mkdir(ID, 0755);
+	} else strcat(strcpy(ID, W->ID), q->name);
+	q->N++;
+	return q;
+}
+
+static int staticField(field F)
+{
+	return F==RI || F==LogRI || F==ContourRI || F==Contour || F==raweEffx || F==raweEffy || F==raweEffz || F==eEff;
+}
+
+/* replace the first '%' of a file name by "<field>-<slice>" */
+static void expandName(char *filename, const char *f, const char *s)
+{
+	char rest[1024], *pct = strchr(filename, '%');
+	if (!pct) return;
+	strcpy(rest, pct+1);
+	sprintf(pct, "%s-%s%s", f, s, rest);
+}
+
+void (sliceSnap)(world W, field F, slice S, char *f, char *s, ...)
+{
+	static sliceq *head;
+	char *format, string[64], filename[1024];
+	va_list ap;
+	va_start(ap, s);
+	int N = staticField(F) ? 0 : va_arg(ap, int);
+	method M = va_arg(ap, method);
+	unsigned long int *cmap = (M == png) ? va_arg(ap, unsigned long int *) : 0;
+	float Max = (M == png) ? va_arg(ap, double) : 1;
+	int step = (!N || N > (long)W->T) ? 1 : W->T/N;
+	int skip = Max < 0 ? ((int)(-Max*W->T/step))*step : 0;
+	format = va_arg(ap, char*);
+	vsnprintf(filename, sizeof filename, format, ap);
+	va_end(ap);
+	expandName(filename, f, s);
+	sliceq *q = track(W, filename, M, &head);
+	if (N) sprintf(string, "%05ld", (q->N-skip)/step), strcat(filename, string);
+	if (q->N % step) return;
+	alis_be_sync_world(W);
+	float max = 0;
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+		if (max < fabsf(S->F[i][j][k] = F(W, i, j, k))) max = fabsf(S->F[i][j][k]);
+	if (!Max) Max = max;
+	else if (Max < 0) {
+		Max = q->Max;
+		if (q->max < max) q->max = max;
+		if (q->N % skip == 0) q->Max = q->max, q->max = 0;
+	}
+	if (q->N > skip) M(W, S, Max ? Max : 1, f, filename, cmap);
+}
+
+void (sliceTimeAvg)(world W, field F, slice S, char *f, char *s, ...)
+{
+	static sliceq *head;
+	char *format, string[64], filename[1024];
+	va_list ap;
+	va_start(ap, s);
+	int N = staticField(F) ? 0 : va_arg(ap, int);
+	method M = va_arg(ap, method);
+	unsigned long int *cmap = (M == png) ? va_arg(ap, unsigned long int *) : 0;
+	float Max = (M == png) ? va_arg(ap, double) : 1;
+	format = va_arg(ap, char*);
+	vsnprintf(filename, sizeof filename, format, ap);
+	va_end(ap);
+	expandName(filename, f, s);
+	sliceq *q = track(W, filename, M, &head);
+	if (N) sprintf(string, "%05ld", q->N / N), strcat(filename, string);
+	if (q->N == 1) q->F = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+	alis_be_sync_world(W);
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+		q->F[i][j][k] += F(W, i, j, k);
+	if (!N || q->N % N) return;
+	float max = 0;
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+		if (max < fabsf(S->F[i][j][k] = q->F[i][j][k] / N)) max = fabsf(S->F[i][j][k]);
+	if (Max <= 0) Max = max;
+	M(W, S, Max ? Max : 1, f, filename, cmap);
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+		q->F[i][j][k] = 0;
+}
+
+void (sliceFreqDom)(world W, field F, slice S, char *f, char *s, int N, float L, ...)
+{
+	field *ok[30] = {Ex, Ey, Ez, Hx, Hy, Hz, iEx, iEy, iEz, iHx, iHy, iHz, rawEx, rawEy, rawEz, rawHx, rawHy, rawHz, Jx, Jy, Jz, rawJx, rawJy, rawJz, ScEx, ScEy, ScEz, SoEx, SoEy, SoEz};
+	int n = 0;
+	while (n < 30 && F != ok[n]) n++;
+	if (n == 30) printf("\nThe %s field is not supported in sliceFreqDom().\n", f), exit(0);
+	static sliceq *head;
+	char *format, string[1100], filename[1024];
+	va_list ap;
+	va_start(ap, L);
+	method M = va_arg(ap, method);
+	unsigned long int *cmap = (M == png) ? va_arg(ap, unsigned long int *) : 0;
+	float Max = (M == png) ? va_arg(ap, double) : 1;
+	format = va_arg(ap, char*);
+	vsnprintf(filename, sizeof filename, format, ap);
+	va_end(ap);
+	expandName(filename, f, s);
+	sliceq *q = track(W, filename, M, &head);
+	if (q->N == 1) {
+		q->F = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+		q->G = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+	}
+	alis_be_sync_world(W);
+	float re = cosf(2 * PI * q->N * W->dt / L);
+	float im = sinf(2 * PI * q->N * W->dt / L);
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++) {
+		q->F[i][j][k] += F(W, i, j, k) * re;
+		q->G[i][j][k] += F(W, i, j, k) * im;
+	}
+	if (q->N % N) return;
+	if (Max <= 0) {
+		float max = 0;
+		for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+			if (max < sq(q->F[i][j][k])+sq(q->G[i][j][k])) max = sq(q->F[i][j][k])+sq(q->G[i][j][k]);
+		if (Max < sqrtf(max) * 2 / q->N) Max = sqrtf(max) * 2 / q->N;
+	}
+	for (int p = 0; p < 12; p++) {
+		for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+			S->F[i][j][k] = (q->F[i][j][k] * cosf(p * PI / 6) + q->G[i][j][k] * sinf(p * PI / 6)) * 2 / q->N;
+		snprintf(string, sizeof string, "%s%02d", filename, p+1);
+		M(W, S, Max, f, string, cmap);
+	}
+}
+
+float sliceMax(world W, field F, slice S)
+{
+	alis_be_sync_world(W);
+	float Max = 0, f;
+	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+		if (Max < (f = fabsf(F(W, i, j, k)))) Max = f;
+	return Max;
+}
+
+static float sliceSumZ(world W, field F, slice S, int i, int j)
+{
+	float Sum = 0;
+	for (int k = S->kMin+1; k < S->kMax; k++) Sum += W->CE->dz[k] * F(W, i, j, k);
+	Sum += 0.5 * W->CE->dz[S->kMin] * F(W, i, j, S->kMin);
+	Sum += 0.5 * W->CE->dz[S->kMax] * F(W, i, j, S->kMax);
+	return Sum;
+}
+
+static float sliceSumY(world W, field F, slice S, int i)
+{
+	float Sum = 0;
+	for (int j = S->jMin+1; j < S->jMax; j++) Sum += W->CE->dy[j] * sliceSumZ(W, F, S, i, j);
+	Sum += 0.5 * W->CE->dy[S->jMin] * sliceSumZ(W, F, S, i, S->jMin);
+	Sum += 0.5 * W->CE->dy[S->jMax] * sliceSumZ(W, F, S, i, S->jMax);
+	return Sum;
+}
+
+float sliceSum(world W, field F, slice S)
+{
+	alis_be_sync_world(W);
+	float Sum = 0;
+	for (int i = S->iMin+1; i < S->iMax; i++) Sum += W->CE->dx[i] * sliceSumY(W, F, S, i);
+	Sum += 0.5 * W->CE->dx[S->iMin] * sliceSumY(W, F, S, S->iMin);
+	Sum += 0.5 * W->CE->dx[S->iMax] * sliceSumY(W, F, S, S->iMax);
+	if (S->iMin==S->iMax) Sum /= W->CE->dx[S->iMin];
+	if (S->jMin==S->jMax) Sum /= W->CE->dy[S->jMin];
+	if (S->kMin==S->kMax) Sum /= W->CE->dz[S->kMin];
+	return Sum;
+}

@@ -1,0 +1,222 @@
+/*
+ * scenes.c -- parity scenarios written against the public ALiS API.
+ *
+ * One source, three builds: the reference library (golden fixtures), the
+ * oracle restatement (CPU checker) and the GPU engine.  Each scenario
+ * builds a world, runs `steps` time steps with phaser accumulation, and
+ * dumps material maps, fields, ADE currents, phaser faces, fluxes and a
+ * few far-field values (dump.h format).
+ *
+ *   scenes <scene> <out.bin> [scale] [steps]
+ *
+ * Scenes (scaled-down versions of the benchmark configurations):
+ *   c1      vacuum plane wave, periodic x/y, CPML z, planar phasers
+ *   c2      gold block (Drude + 2 critical-point poles) in a TFSF box,
+ *           CPML on all faces, box phasers, far field
+ *   dipole  soft dipole, dielectric ball (12^3 supersampling) and a
+ *           Drude box, CPML box
+ *   bloch   oblique plane wave, Bloch x (complex fields), Lorentz pillar
+ *           on a substrate
+ *   sym     dipole on two symmetry planes, Drude-Lorentz sphere
+ *   hbc     hexagonal-Bloch lattice slab with an iHz dipole
+ *   multi   overlapping Drude-Lorentz spheres in a dielectric host
+ */
+#include <alis.h>
+#include "dump.h"
+
+static int scale = 1;
+
+/* seeded Drude + critical-point gold: CP amplitude A in [0.3,1.5], phase
+ * in [-pi,pi), mapped to ALiS (f, g) by g = -2A sin(phi),
+ * f = 2A cos(phi) + g Gamma/Omega */
+static matter seededGold(unsigned long long seed)
+{
+	lcgSeed(seed);
+	matter M = {{2.1452}, {{8.557, 0.0658}, {2.6203, 0.2147}, {3.1543, 1.1662}}};
+	for (int p = 1; p <= 2; p++) {
+		float A = 0.3f + 1.2f * lcgUniform();
+		float ph = -PI + 2 * PI * lcgUniform();
+		float g = -2 * A * sinf(ph);
+		M.P[p].g = g;
+		M.P[p].f = 2 * A * cosf(ph) + g * M.P[p].r / M.P[p].w;
+	}
+	return M;
+}
+
+static void farSamples(phaser P, const char *tag)
+{
+	float th[5] = { 0, 30, 60, 150, 180 }, ph[5] = { 0, 45, 0, 90, 0 };
+	char nm[64];
+	for (int a = 0; a < 5; a++) {
+		snprintf(nm, 64, "%s.ffP.%d", tag, a); dumpCScalar(nm, farField(P, Ppol, th[a], ph[a]));
+		snprintf(nm, 64, "%s.ffS.%d", tag, a); dumpCScalar(nm, farField(P, Spol, th[a], ph[a]));
+	}
+}
+
+static void run(world W, phaser P, int steps)
+{
+	for (int n = 1; n <= steps; n++) {
+		updateE(W);
+		updateH(W);
+		if (P) updatePhaser(W, P);
+	}
+}
+
+static void sceneC1(int steps)
+{
+	int half = 16 * scale;                       /* cells per lateral half */
+	dom D = {{-10*half, 10*(half-1)}, {-10*half, 10*(half-1)}, {-10*20*scale, 10*20*scale}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PBC}, {PBC}, {PML, PML}, {16}};
+	world W = createWorld(D, R, S, "");
+	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {W->ktoz(W, W->kMIN+20), W->zMax-30}};
+	planewave(W, T, Ppol, 180, 0, Pulse, 600, 90);
+	phaser P = createPhasers(W, 400, 800, 400.0/15, -INF, INF, -INF, INF, 100, 100);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpWorld(W->S->W, "A");
+	dumpPhasers(P, "P");
+}
+
+static void sceneC2(int steps)
+{
+	float L = 60 * scale;
+	dom D = {{-L, L-2}, {-L, L-2}, {-L, L-2}};
+	dom T = {{-L+10, L-12}, {-L+10, L-12}, {-L+10, L-12}};
+	res R = {1, {2}, {1240}};
+	sur S = {{PML}, {PML}, {PML}, {12}};
+	world W = createWorld(D, R, S, "");
+	object Block = {Box, {{-40, 40}, {-20, 20}, {-15, 15}}};
+	putObjects(W, seededGold(1234), Block, Air);
+	planewave(W, T, Ppol, 0, 0, Pulse, 600, 200);
+	phaser P = createPhasers(W, 400, 800, 400.0/7, -L+6, L-8, -L+6, L-8, -L+6, L-8);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpWorld(W->S->W, "A");
+	dumpPhasers(P, "P");
+	farSamples(P + 3, "F");
+}
+
+static void sceneDipole(int steps)
+{
+	float L = 100 * scale;
+	dom D = {{L}, {L}, {L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PML}};
+	world W = createWorld(D, R, S, "");
+	object Ball1 = {Ball, {{-60, 20}, {-40, 40}, {-30, 50}}};
+	object Bar = {Box, {{20, 70}, {-20, 20}, {-80, -40}}};
+	matter Ag1 = {{4.0323}, {{9.1864, 0.021}}};
+	putObjects(W, n(1.5), Ball1, Ag1, Bar, Air);
+	pointDipole(W, Ez, 5, 0, 0, Band, 400, 800);
+	pointDipole(W, Hx, -20, 10, 30, Pulse, 500, 100, 0.5, 30);
+	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+	farSamples(P + 1, "F");
+}
+
+static void sceneBloch(int steps)
+{
+	int half = 8 * scale;
+	dom D = {{-10*half, 10*(half-1)}, {-10*half, 10*(half-1)}, {-300, 300}};
+	res R = {5, {10}, {1240}};
+	sur S = {{BBC}, {PBC}, {PML}, {10}};
+	world W = createWorld(D, R, S, "");
+	object Pillar = {RodZ, {{-50, 40}, {-40, 50}, {-100, 100}}};
+	object Sub = {Box, {{-INF, INF}, {-INF, INF}, {-INF, -100}}};
+	matter TiO2 = {{5.5}, {{4.5, 0.05, 1.0}}};
+	putObjects(W, TiO2, Pillar, n(1.45), Sub, Air);
+	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {-200, 250}};
+	planewave(W, T, Ppol, 150, 0, Pulse, 550, 120);
+	phaser P = createPhasers(W, 450, 700, 125, -INF, INF, -INF, INF, -250, -250);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpWorld(W->S->W, "A");
+	dumpPhasers(P, "P");
+}
+
+static void sceneSym(int steps)
+{
+	float L = 80 * scale;
+	dom D = {{L}, {L}, {L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{SYM, PML}, {SYM, PML}, {PML}};
+	world W = createWorld(D, R, S, "");
+	object Sphere = {Ball, {{-40, 40}, {-40, 40}, {20, 60}}};
+	matter DL = {{2.0}, {{7.0, 0.1}, {3.0, 0.3, 1.5}}};
+	putObjects(W, DL, Sphere, Air);
+	pointDipole(W, Ex, 0, 0, -20, Band, 400, 800);
+	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+	farSamples(P + 1, "F");
+}
+
+static void sceneHBC(int steps)
+{
+	float kx = 0.2f, ky = 1;
+	dom D = {{100}, {0, 100*sqrtf(3)}, {200}};
+	res R = {5, {10, 5*sqrtf(3), 10}, {1240}};
+	sur S = {{BBC, 200*3/kx}, {HBC, 200*sqrtf(3)/ky}, {SYM, PML}};
+	world W = createWorld(D, R, S, "");
+	object Slab = {Difference, {2}, objects {
+		{Box, {{-INF, INF}, {-INF, INF}, {-40, 40}}},
+		{DLattice, {{200}, {200*sqrtf(3)}}, objects {{RodZ, {{-60, 60}, {-60, 60}, {-INF, INF}}}}},
+	}};
+	putObjects(W, n(3.5), Slab, Air);
+	pointDipole(W, iHz, 40, 20*sqrtf(3), 0, Band, 750, 2000);
+	run(W, 0, steps);
+	dumpWorld(W, "W");
+	(void)scale;
+}
+
+static void sceneMulti(int steps)
+{
+	float L = 80 * scale;
+	dom D = {{-L, L-5}, {-L, L-5}, {-L, L-5}};
+	res R = {2.5, {5}, {1240}};
+	sur S = {{PBC}, {PBC}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	lcgSeed(99);
+	object O[7];
+	matter M[7];
+	for (int q = 0; q < 6; q++) {
+		float r = 10 + 20 * lcgUniform(), x = -50 + 100 * lcgUniform(), y = -50 + 100 * lcgUniform(), z = -40 + 80 * lcgUniform();
+		O[q] = (object){Ball, {{x-r, x+r}, {y-r, y+r}, {z-r, z+r}}};
+		M[q] = (matter){{1.5f + lcgUniform()}, {{6 + 3*lcgUniform(), 0.05f + 0.1f*lcgUniform()}, {2.5f + lcgUniform(), 0.2f, 0.5f + lcgUniform()}}};
+	}
+	O[6] = (object){0};
+	M[6] = n(1.5);
+	putObjectArray(W, M, O);
+	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {-L+15, L-20}};
+	planewave(W, T, Spol, 180, 0, Pulse, 600, 150);
+	phaser P = createPhasers(W, 450, 750, 150, -INF, INF, -INF, INF, L-15, L-15);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
+int main(int argc, char **argv)
+{
+	if (argc < 3) {
+		fprintf(stderr, "usage: %s scene out.bin [scale] [steps]\n", argv[0]);
+		return 2;
+	}
+	if (argc > 3) scale = atoi(argv[3]);
+	int steps = argc > 4 ? atoi(argv[4]) : 100;
+	dumpOpen(argv[2]);
+	const char *s = argv[1];
+	if (!strcmp(s, "c1")) sceneC1(steps);
+	else if (!strcmp(s, "c2")) sceneC2(steps);
+	else if (!strcmp(s, "dipole")) sceneDipole(steps);
+	else if (!strcmp(s, "bloch")) sceneBloch(steps);
+	else if (!strcmp(s, "sym")) sceneSym(steps);
+	else if (!strcmp(s, "hbc")) sceneHBC(steps);
+	else if (!strcmp(s, "multi")) sceneMulti(steps);
+	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
+	dumpClose();
+	return 0;
+}
