@@ -1,0 +1,94 @@
+// common.cuh -- shared device-side definitions of the GB300 ALiS engine.
+//
+// Storage of one world on the device: every field component (E, H, the
+// eps^-1 maps) uses the same halo'd layout over
+// [iMIN-1, iMAX+1] x [jMIN-1, jMAX+1] x [kMIN-1, kMAX+1]; k is fastest and
+// each (i, j) row starts kOff = 31 floats before a 128-byte boundary so
+// that k = kMIN is 128-byte aligned (row pitch is a multiple of 32
+// floats).  Smaller arrays (CPML psi slabs, ADE maps and currents) are
+// compact box arrays with their own strides.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "alisgpu.h"
+
+#define ALIS_KOFF 31
+#define ALIS_MAXPOLES 6
+#define ALIS_MAXTFSF 4
+#define ALIS_TILE_OBJ 48
+
+struct Layout {
+	int i0, j0, k0;          // first stored index (MIN - 1)
+	int ni, nj, nk;          // stored extents
+	long long sj, si;        // row pitch and plane pitch (floats)
+	__host__ __device__ long long at(int i, int j, int k) const {
+		return (long long)(i - i0) * si + (long long)(j - j0) * sj + (k - k0) + ALIS_KOFF;
+	}
+	size_t elems() const { return (size_t)ni * (size_t)si; }
+};
+
+// compact box array: element (i,j,k) at p[(i-i0)*si + (j-j0)*sj + (k-k0)]
+struct BoxArr {
+	float *p;
+	int i0, i1, j0, j1, k0, k1;
+	long long sj, si;
+	__host__ __device__ long long at(int i, int j, int k) const {
+		return (long long)(i - i0) * si + (long long)(j - j0) * sj + (k - k0);
+	}
+	__host__ __device__ bool has(int i, int j, int k) const {
+		return i >= i0 && i <= i1 && j >= j0 && j <= j1 && k >= k0 && k <= k1;
+	}
+	size_t elems() const { return (size_t)(1 + i1 - i0) * (size_t)si; }
+};
+
+// one dispersive object as the kernels see it
+struct DevObj {
+	int i0, i1, j0, j1, k0, k1;          // box of maps and currents
+	int NJ, NK;
+	float a[3];
+	int cond;                             // any conductivity factor non-zero
+	float JJ[ALIS_MAXPOLES][3], JK[ALIS_MAXPOLES][3], JE[ALIS_MAXPOLES][3];
+	float KJ[ALIS_MAXPOLES][3], KK[ALIS_MAXPOLES][3], KE[ALIS_MAXPOLES][3];
+	float *fill[3];                       // compact over the box
+	float *J[2][ALIS_MAXPOLES][3];        // [m][pole][axis]
+	float *K[2][ALIS_MAXPOLES][3];
+	long long sj, si;                     // strides of the box arrays
+};
+
+// TFSF box as the main-world kernels see it
+struct DevTfsf {
+	int iMin, iMax, jMin, jMax, kMin, kMax;
+	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
+	int auxIMAX, auxJMAX, aliasX, aliasY;
+	Layout L;                             // layout of the auxiliary world
+	const float *G[2][3];                 // aux H (E step) or aux E (H step), [m][comp]
+	float dtdMin[3], dtdMax[3];           // dt/ds at the min face and max face
+};
+
+struct HalfStepParams {
+	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
+	int iMin, iMax, jMin, jMax, kMin, kMax;
+	Layout L;
+	int m;
+	float *F[3];
+	const float *G[3];
+	const float *C[3];                    // eps^-1 maps (E half step) or null
+	const float *dtd[3];                  // dt/ds tables indexed from MIN
+	const float *cp[9];                   // CPML b/c tables (xP,xPy,xPz,yP,yPz,yPx,zP,zPx,zPy)
+	int slabOn[6];                        // xMin,yMin,zMin,xMax,yMax,zMax
+	int slabLo[6], slabHi[6];             // slab range along the face axis
+	BoxArr psi[6][2];                     // (Py,Pz) (Pz,Px) (Px,Py) per face
+	int nobj;
+	const DevObj *obj;
+	int ntfsf;
+	DevTfsf tf[ALIS_MAXTFSF];
+	float *Fother[3];                     // E of set m during the H step (ADE drive)
+	unsigned int *err;                    // device error word
+};
+
+// ---- launch bookkeeping ----
+extern "C" void alisgpu__count_launch(void);
+extern "C" cudaStream_t alisgpu__stream(void);
+extern "C" int alisgpu__fail(int code, const char *fmt, ...);
+extern "C" int alisgpu__check(cudaError_t e, const char *what);
+#define ALIS_CUDA(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return alisgpu__check(e_, #call); } while (0)

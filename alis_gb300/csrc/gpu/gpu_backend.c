@@ -1,0 +1,549 @@
+/*
+ * gpu_backend.c -- the GPU stepping backend behind the ALiS API.
+ *
+ * Implements updateE / updateH / updatePhaser and the engine hooks of
+ * engine.h by translating the host data model (struct world, sources,
+ * TFSF boxes, phasers) into calls of the device C-ABI (alisgpu.h).
+ * Live state is in HBM; host arrays are mirrors refreshed on demand.
+ *
+ * Per half step (reference src/update.c:275-341) the host evaluates the
+ * source waveforms with the same C library calls as the reference, lists
+ * the boundary ghost copies with the world's current Bloch/symmetry
+ * factors, and issues one alisgpu_half_step_run per world (the main
+ * world, then each TFSF auxiliary world).  Time bookkeeping (n, t, E->t,
+ * H->t) is done here exactly as in the reference.
+ */
+#include <stdint.h>
+#include <string.h>
+#include "engine.h"
+#include "alisgpu.h"
+
+int alis_needs_currents(matter M);
+void alisgpu__forget_tfsf(const alisgpu_tfsf *s);
+
+#define MAX_TFSF 4
+#define MAX_GHOST 24
+
+typedef struct devWorld {
+	world W;
+	alisgpu_world *dw;
+	int objectsDirty;         /* eps maps / dispersive objects need upload */
+	int hostStale;            /* device ahead of the host mirrors */
+	int ntf;
+	alisgpu_tfsf tf[MAX_TFSF];
+	struct devWorld *next;
+} devWorld;
+
+typedef struct devPhaser {
+	phaser P;                 /* first element of the set */
+	int nfreq, nface;
+	int faceSlot[6];          /* cfield index (0..5: xMin,xMax,yMin,yMax,zMin,zMax) of each device face */
+	alisgpu_phaser *dp;
+	int hostStale;
+	float *phE, *phH;
+	struct devPhaser *next;
+} devPhaser;
+
+static devWorld *worlds, *lastWorld;
+static devPhaser *phasers;
+
+static void die(const char *what, int rc)
+{
+	fprintf(stderr, "alis: %s failed (%d): %s\n", what, rc, alisgpu_last_error());
+	exit(1);
+}
+#define CHECK(what, call) do { int rc_ = (call); if (rc_) die(what, rc_); } while (0)
+
+static devWorld *findWorld(world W)
+{
+	if (lastWorld && lastWorld->W == W) return lastWorld;
+	for (devWorld *d = worlds; d; d = d->next) if (d->W == W) return lastWorld = d;
+	return 0;
+}
+
+static devPhaser *findPhaser(phaser P)
+{
+	for (devPhaser *d = phasers; d; d = d->next) if (P >= d->P && P < d->P + d->nfreq) return d;
+	return 0;
+}
+
+/* ---- world lifecycle ---- */
+
+static void uploadLineTables(devWorld *d)
+{
+	world W = d->W;
+	for (int grid = 0; grid < 2; grid++) {
+		coeffs *C = grid ? W->CH : W->CE;
+		const float *dtd[3] = { &C->dtdx[W->iMIN], &C->dtdy[W->jMIN], &C->dtdz[W->kMIN] };
+		const float *cp[9] = {
+			C->xP ? &C->xP[W->iMIN] : 0, C->xPy ? &C->xPy[W->iMIN] : 0, C->xPz ? &C->xPz[W->iMIN] : 0,
+			C->yP ? &C->yP[W->jMIN] : 0, C->yPz ? &C->yPz[W->jMIN] : 0, C->yPx ? &C->yPx[W->jMIN] : 0,
+			C->zP ? &C->zP[W->kMIN] : 0, C->zPx ? &C->zPx[W->kMIN] : 0, C->zPy ? &C->zPy[W->kMIN] : 0 };
+		CHECK("set_line_tables", alisgpu_set_line_tables(d->dw, grid, dtd, cp));
+	}
+}
+
+void alis_be_world_created(world W)
+{
+	CHECK("init", alisgpu_init());
+	devWorld *d = calloc(1, sizeof *d);
+	d->W = W;
+	alisgpu_geometry g = {
+		W->iMIN, W->iMAX, W->jMIN, W->jMAX, W->kMIN, W->kMAX,
+		W->iMin, W->iMax, W->jMin, W->jMax, W->kMin, W->kMax,
+		W->complexField,
+		{ W->xMinSur==PML, W->yMinSur==PML, W->zMinSur==PML, W->xMaxSur==PML, W->yMaxSur==PML, W->zMaxSur==PML } };
+	CHECK("world_create", alisgpu_world_create(&g, &d->dw));
+	uploadLineTables(d);
+	d->next = worlds;
+	worlds = d;
+}
+
+void alis_be_world_deleted(world W)
+{
+	devWorld **pp = &worlds;
+	while (*pp && (*pp)->W != W) pp = &(*pp)->next;
+	if (!*pp) return;
+	devWorld *d = *pp;
+	*pp = d->next;
+	if (lastWorld == d) lastWorld = 0;
+	for (int q = 0; q < d->ntf; q++) alisgpu__forget_tfsf(&d->tf[q]);
+	alisgpu_world_destroy(d->dw);
+	free(d);
+}
+
+void alis_be_objects_changed(world W)
+{
+	devWorld *d = findWorld(W);
+	if (d) d->objectsDirty = 1;
+}
+
+static void buildTfsf(devWorld *d);
+
+void alis_be_sources_changed(world W)
+{
+	devWorld *d = findWorld(W);
+	if (d) buildTfsf(d);
+}
+
+void alis_be_world_reset(world W)
+{
+	devWorld *d = findWorld(W);
+	if (!d) return;
+	CHECK("world_reset", alisgpu_world_reset(d->dw));
+	d->hostStale = 0;
+}
+
+/* eps^-1 maps and dispersive objects (reference src/object.c:339-405) */
+static void uploadObjects(devWorld *d)
+{
+	world W = d->W;
+	coeffs *C = W->CE;
+	if (C->x) CHECK("set_eps", alisgpu_set_eps(d->dw, &C->x[W->iMIN][W->jMIN][W->kMIN], &C->y[W->iMIN][W->jMIN][W->kMIN], &C->z[W->iMIN][W->jMIN][W->kMIN]));
+	else CHECK("set_eps", alisgpu_set_eps(d->dw, 0, 0, 0));
+	alisgpu_dispersive *o = calloc(C->N ? C->N : 1, sizeof *o);
+	for (int n = 0; n < C->N; n++) {
+		o[n].iMin = C->iMin[n], o[n].iMax = C->iMax[n], o[n].jMin = C->jMin[n], o[n].jMax = C->jMax[n];
+		o[n].kMin = C->kMin[n], o[n].kMax = C->kMax[n];
+		o[n].NJ = C->NJ[n], o[n].NK = C->NK[n];
+		float ****fill[3] = { C->Jx, C->Jy, C->Jz };
+		float *a[3] = { C->ax, C->ay, C->az };
+		float **JJ[3] = { C->JJx, C->JJy, C->JJz }, **JK[3] = { C->JKx, C->JKy, C->JKz }, **JE[3] = { C->JEx, C->JEy, C->JEz };
+		float **KJ[3] = { C->KJx, C->KJy, C->KJz }, **KK[3] = { C->KKx, C->KKy, C->KKz }, **KE[3] = { C->KEx, C->KEy, C->KEz };
+		for (int q = 0; q < 3; q++) {
+			o[n].fill[q] = &fill[q][n][C->iMin[n]][C->jMin[n]][C->kMin[n]];
+			o[n].a[q] = a[q][n];
+			o[n].JJ[q] = JJ[q][n], o[n].JK[q] = JK[q][n], o[n].JE[q] = JE[q][n];
+			o[n].KJ[q] = KJ[q][n], o[n].KK[q] = KK[q][n], o[n].KE[q] = KE[q][n];
+		}
+	}
+	CHECK("set_dispersive", alisgpu_set_dispersive(d->dw, C->N, o));
+	free(o);
+	d->objectsDirty = 0;
+}
+
+/* TFSF boxes of W with their auxiliary worlds (reference src/source.c:269-334) */
+static void buildTfsf(devWorld *d)
+{
+	world W = d->W;
+	for (int q = 0; q < d->ntf; q++) alisgpu__forget_tfsf(&d->tf[q]);
+	d->ntf = 0;
+	for (tfsf S = W->S; S; S = S->S) {
+		if (d->ntf == MAX_TFSF) { fprintf(stderr, "alis: more than %d TFSF sources\n", MAX_TFSF); exit(1); }
+		devWorld *a = findWorld(S->W);
+		if (!a) continue;
+		alisgpu_tfsf *t = &d->tf[d->ntf++];
+		memset(t, 0, sizeof *t);
+		t->aux = a->dw;
+		t->iMin = S->iMin, t->iMax = S->iMax, t->jMin = S->jMin, t->jMax = S->jMax, t->kMin = S->kMin, t->kMax = S->kMax;
+		t->iMIN = S->iMIN, t->iMAX = S->iMAX, t->jMIN = S->jMIN, t->jMAX = S->jMAX, t->kMIN = S->kMIN, t->kMAX = S->kMAX;
+		t->auxIMAX = S->W->iMAX, t->auxJMAX = S->W->jMAX;
+		/* rows were aliased when the auxiliary world is narrower than W */
+		t->aliasX = S->W->iMAX < W->iMAX + 1 && S->W->iNUM < W->iNUM;
+		t->aliasY = S->W->jMAX < W->jMAX + 1 && S->W->jNUM < W->jNUM;
+	}
+}
+
+/* ---- host mirrors ---- */
+
+static void downloadWorld(devWorld *d)
+{
+	world W = d->W;
+	CHECK("synchronize", alisgpu_synchronize());
+	for (int m = 0; m <= W->complexField; m++) {
+		float ***E[3] = { W->E[m].x, W->E[m].y, W->E[m].z }, ***H[3] = { W->H[m].x, W->H[m].y, W->H[m].z };
+		for (int c = 0; c < 3; c++) {
+			CHECK("field_download", alisgpu_field_download(d->dw, 0, m, c, &E[c][W->iMIN-1][W->jMIN-1][W->kMIN-1]));
+			CHECK("field_download", alisgpu_field_download(d->dw, 1, m, c, &H[c][W->iMIN-1][W->jMIN-1][W->kMIN-1]));
+		}
+		coeffs *C = W->CE;
+		for (int n = 0; n < C->N; n++) {
+			float *****J[3] = { W->E[m].Jx, W->E[m].Jy, W->E[m].Jz }, *****K[3] = { W->E[m].Kx, W->E[m].Ky, W->E[m].Kz };
+			for (int p = 0; p < C->NK[n]; p++) for (int c = 0; c < 3; c++) {
+				CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 0, &J[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
+				if (p >= C->NJ[n])
+					CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 1, &K[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
+			}
+		}
+	}
+	d->hostStale = 0;
+}
+
+void alis_be_sync_world(world W)
+{
+	devWorld *d = findWorld(W);
+	if (d && d->hostStale) downloadWorld(d);
+}
+
+/* ---- half steps ---- */
+
+typedef struct {
+	alisgpu_source_patch p[64];
+	int n;
+	float *v;
+	int nv, cap;
+} patchList;
+
+static patchList srcList;
+
+/* E or H field set and component a source writes to */
+static int sourceTarget(world W, source S, int field, int *m, int *comp)
+{
+	for (int q = 0; q <= W->complexField; q++) {
+		vfield *V = field ? &W->H[q] : &W->E[q];
+		float ***c[3] = { V->x, V->y, V->z };
+		for (int a = 0; a < 3; a++) if (S->F == c[a]) { *m = q, *comp = a; return 1; }
+	}
+	return 0;
+}
+
+/* per-cell increments of the active sources of a chain, in chain order
+ * (reference src/update.c:161-179) */
+static void collectSources(world W, source S, int field, float t)
+{
+	srcList.n = 0, srcList.nv = 0;
+	for (; S; S = S->S) {
+		if (!(W->n < S->N)) continue;
+		int m, comp;
+		if (!sourceTarget(W, S, field, &m, &comp)) continue;
+		int cells = (1+S->iMax-S->iMin)*(1+S->jMax-S->jMin)*(1+S->kMax-S->kMin);
+		if (srcList.nv + cells > srcList.cap) {
+			srcList.cap = 2*(srcList.nv + cells);
+			srcList.v = realloc(srcList.v, srcList.cap * sizeof(float));
+		}
+		if (srcList.n == 64) { fprintf(stderr, "alis: more than 64 active sources on one field\n"); exit(1); }
+		alisgpu_source_patch *p = &srcList.p[srcList.n++];
+		*p = (alisgpu_source_patch){ m, comp, S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax, srcList.nv };
+		float *v = srcList.v + srcList.nv;
+		int q = 0;
+		if (S->Phase) {
+			for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+				v[q++] = (S->Amplitude ? S->Amplitude[i][j][k] : S->amplitude) * S->waveForm(W, S, t, S->Phase[i][j][k]);
+		} else {
+			float f = S->waveForm(W, S, t, S->phase);
+			for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+				v[q++] = S->Amplitude ? S->Amplitude[i][j][k] * f : S->amplitude * f;
+		}
+		srcList.nv += cells;
+	}
+}
+
+static int ghostList(world W, int field, alisgpu_ghost_copy *g)
+{
+	int n = 0;
+	int iAlt = (W->xMinSur==PBC || W->xMinSur==BBC ? W->iNUM-1 : 1);
+	int jAlt = (W->yMinSur==PBC || W->yMinSur==BBC ? W->jNUM-1 : 1);
+	int kAlt = (W->zMinSur==PBC || W->zMinSur==BBC ? W->kNUM-1 : 1);
+#define G(c, co, si, i0, i1, j0, j1, k0, k1, di, dj, dk) g[n++] = (alisgpu_ghost_copy){ c, i0, i1, j0, j1, k0, k1, di, dj, dk, co, si }
+	if (field == 0) {
+		/* reference src/update.c:284-297 */
+		G(0, W->coskx, -W->sinkx, W->iMAX+1, W->iMAX+1, W->jMIN, W->jMAX, W->kMIN, W->kMAX, -iAlt, 0, 0);
+		G(2, W->coskz, -W->sinkz, W->iMIN, W->iMAX, W->jMIN, W->jMAX, W->kMAX+1, W->kMAX+1, 0, 0, -kAlt);
+		if (W->yMinSur==HBC) {
+			G(1, W->coskym, -W->sinkym, W->iMIN, 0, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMAX, 1-W->jNUM, 0);
+			G(1, W->coskyp, -W->sinkyp, 1, W->iMAX+1, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMIN, 1-W->jNUM, 0);
+		} else {
+			G(1, W->cosky, -W->sinky, W->iMIN, W->iMAX, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, 0, -jAlt, 0);
+		}
+	} else {
+		/* reference src/update.c:311-339 */
+		G(1, W->xMaxSur==PEC?1:W->coskx, -W->sinkx, W->iMAX+1, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMIN, W->kMAX+1, -iAlt, 0, 0);
+		G(2, W->xMaxSur==PEC?1:W->coskx, -W->sinkx, W->iMAX+1, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMIN, W->kMAX+1, -iAlt, 0, 0);
+		G(0, W->zMaxSur==PEC?1:W->coskz, -W->sinkz, W->iMIN, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMAX+1, W->kMAX+1, 0, 0, -kAlt);
+		G(1, W->zMaxSur==PEC?1:W->coskz, -W->sinkz, W->iMIN, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMAX+1, W->kMAX+1, 0, 0, -kAlt);
+		G(1, W->coskx, W->sinkx, W->iMIN, W->iMIN, W->jMIN, W->jMAX+1, W->kMIN, W->kMAX+1, iAlt, 0, 0);
+		G(2, W->coskx, W->sinkx, W->iMIN, W->iMIN, W->jMIN, W->jMAX+1, W->kMIN, W->kMAX+1, iAlt, 0, 0);
+		G(0, W->coskz, W->sinkz, W->iMIN, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMIN, W->kMIN, 0, 0, kAlt);
+		G(1, W->coskz, W->sinkz, W->iMIN, W->iMAX+1, W->jMIN, W->jMAX+1, W->kMIN, W->kMIN, 0, 0, kAlt);
+		if (W->yMinSur==HBC) {
+			G(0, W->coskyp, W->sinkyp, W->iMIN, 0, W->jMIN, W->jMIN, W->kMIN, W->kMAX, W->iMAX, W->jNUM-1, 0);
+			G(2, W->coskyp, W->sinkyp, W->iMIN, 0, W->jMIN, W->jMIN, W->kMIN, W->kMAX, W->iMAX, W->jNUM-1, 0);
+			G(0, W->coskym, -W->sinkym, W->iMIN, 0, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMAX, 1-W->jNUM, 0);
+			G(2, W->coskym, -W->sinkym, W->iMIN, 0, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMAX, 1-W->jNUM, 0);
+			G(0, W->coskym, W->sinkym, 1, W->iMAX+1, W->jMIN, W->jMIN, W->kMIN, W->kMAX, W->iMIN, W->jNUM-1, 0);
+			G(2, W->coskym, W->sinkym, 1, W->iMAX+1, W->jMIN, W->jMIN, W->kMIN, W->kMAX, W->iMIN, W->jNUM-1, 0);
+			G(0, W->coskyp, -W->sinkyp, 1, W->iMAX+1, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMIN, 1-W->jNUM, 0);
+			G(2, W->coskyp, -W->sinkyp, 1, W->iMAX+1, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, W->iMIN, 1-W->jNUM, 0);
+		} else {
+			G(2, W->yMaxSur==PEC?1:W->cosky, -W->sinky, W->iMIN, W->iMAX+1, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX+1, 0, -jAlt, 0);
+			G(0, W->yMaxSur==PEC?1:W->cosky, -W->sinky, W->iMIN, W->iMAX+1, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX+1, 0, -jAlt, 0);
+			G(2, W->cosky, W->sinky, W->iMIN, W->iMAX+1, W->jMIN, W->jMIN, W->kMIN, W->kMAX+1, 0, jAlt, 0);
+			G(0, W->cosky, W->sinky, W->iMIN, W->iMAX+1, W->jMIN, W->jMIN, W->kMIN, W->kMAX+1, 0, jAlt, 0);
+		}
+	}
+#undef G
+	return n;
+}
+
+static void halfStep(world W, int field)
+{
+	devWorld *d = findWorld(W);
+	if (!d) { fprintf(stderr, "alis: world unknown to the GPU backend\n"); exit(1); }
+	if (d->objectsDirty) uploadObjects(d);
+	alisgpu_ghost_copy g[MAX_GHOST];
+	alisgpu_half_step s;
+	memset(&s, 0, sizeof s);
+	s.field = field;
+	s.ntfsf = d->ntf;
+	s.tfsf = d->tf;
+	collectSources(W, field ? W->SH : W->SE, field, field ? W->E->t : W->H->t);
+	s.nsrc = srcList.n;
+	s.src = srcList.p;
+	s.values = srcList.v;
+	s.nvalues = srcList.nv;
+	s.nghost = ghostList(W, field, g);
+	s.ghost = g;
+	CHECK("half_step", alisgpu_half_step_run(d->dw, &s));
+	d->hostStale = 1;
+}
+
+/* reference src/update.c:275-299 */
+void updateE(world W)
+{
+	halfStep(W, 0);
+	for (tfsf S = W->S; S; S = S->S) updateE(S->W);
+	W->t = W->E->t = ++W->n * W->dt;
+}
+
+/* reference src/update.c:302-341 */
+void updateH(world W)
+{
+	halfStep(W, 1);
+	for (tfsf S = W->S; S; S = S->S) updateH(S->W);
+	W->t = W->H->t = W->E->t + 0.5 * W->dt;
+}
+
+
+/* ---- phasers ---- */
+
+static int phaserRing(void)
+{
+	const char *e = getenv("ALISGPU_PHASER_RING");
+	int r = e ? atoi(e) : 64;
+	return r > 0 ? r : 64;
+}
+
+void alis_be_phaser_created(phaser P)
+{
+	devPhaser *d = calloc(1, sizeof *d);
+	d->P = P;
+	while (P[d->nfreq].f) d->nfreq++;
+	world W = P->W;
+	devWorld *dw = findWorld(W);
+	if (!dw) { fprintf(stderr, "alis: phaser on a world unknown to the GPU backend\n"); exit(1); }
+	alisgpu_face faces[6];
+	cfield *cf[6] = { &P->xMin, &P->xMax, &P->yMin, &P->yMax, &P->zMin, &P->zMax };
+	int boxes[6][6] = {
+		{ P->iMin, P->iMin, P->jMin, P->jMax, P->kMin, P->kMax }, { P->iMax, P->iMax, P->jMin, P->jMax, P->kMin, P->kMax },
+		{ P->iMin, P->iMax, P->jMin, P->jMin, P->kMin, P->kMax }, { P->iMin, P->iMax, P->jMax, P->jMax, P->kMin, P->kMax },
+		{ P->iMin, P->iMax, P->jMin, P->jMax, P->kMin, P->kMin }, { P->iMin, P->iMax, P->jMin, P->jMax, P->kMax, P->kMax } };
+	for (int s = 0; s < 6; s++) {
+		int axis = s / 2;
+		int present = axis == 0 ? cf[s]->Ey != 0 : axis == 1 ? cf[s]->Ez != 0 : cf[s]->Ex != 0;
+		if (!present) continue;
+		faces[d->nface] = (alisgpu_face){ axis, boxes[s][0], boxes[s][1], boxes[s][2], boxes[s][3], boxes[s][4], boxes[s][5] };
+		d->faceSlot[d->nface++] = s;
+	}
+	const char *k = getenv("ALISGPU_PHASER_KAHAN");
+	CHECK("phaser_create", alisgpu_phaser_create(dw->dw, d->nfreq, d->nface, faces, phaserRing(), k && k[0] == '1', &d->dp));
+	d->phE = calloc(2 * d->nfreq, sizeof(float));
+	d->phH = calloc(2 * d->nfreq, sizeof(float));
+	d->next = phasers;
+	phasers = d;
+}
+
+void alis_be_phaser_deleted(phaser P)
+{
+	devPhaser **pp = &phasers;
+	while (*pp && (*pp)->P != P) pp = &(*pp)->next;
+	if (!*pp) return;
+	devPhaser *d = *pp;
+	*pp = d->next;
+	alisgpu_phaser_destroy(d->dp);
+	free(d->phE);
+	free(d->phH);
+	free(d);
+}
+
+/* phase factors of every frequency of the set, as the reference computes
+ * them per call (src/phaser.c:97-98); frequencies before P are skipped */
+void updatePhaser(world W, phaser P)
+{
+	devPhaser *d = findPhaser(P);
+	if (!d) { fprintf(stderr, "alis: updatePhaser on an unknown phaser\n"); exit(1); }
+	int first = (int)(P - d->P);
+	for (int n = 0; n < d->nfreq; n++) {
+		float complex pE = 0, pH = 0;
+		if (n >= first) {
+			pE = cexpf(2 * PI * I * d->P[n].f * W->E->t);
+			pH = cexpf(2 * PI * I * d->P[n].f * W->H->t);
+		}
+		d->phE[2*n] = crealf(pE), d->phE[2*n+1] = cimagf(pE);
+		d->phH[2*n] = crealf(pH), d->phH[2*n+1] = cimagf(pH);
+	}
+	CHECK("phaser_record", alisgpu_phaser_record(d->dp, d->phE, d->phH));
+	d->hostStale = 1;
+}
+
+static void downloadPhaser(devPhaser *d)
+{
+	CHECK("phaser_flush", alisgpu_phaser_flush(d->dp));
+	for (int n = 0; n < d->nfreq; n++) {
+		phaser p = d->P + n;
+		cfield *cf[6] = { &p->xMin, &p->xMax, &p->yMin, &p->yMax, &p->zMin, &p->zMax };
+		int lo[6][3] = {
+			{ p->iMin, p->jMin, p->kMin }, { p->iMax, p->jMin, p->kMin }, { p->iMin, p->jMin, p->kMin },
+			{ p->iMin, p->jMax, p->kMin }, { p->iMin, p->jMin, p->kMin }, { p->iMin, p->jMin, p->kMax } };
+		for (int f = 0; f < d->nface; f++) {
+			int s = d->faceSlot[f], axis = s / 2;
+			cfield *c = cf[s];
+			float complex ***q[4];
+			if (axis == 0) q[0] = c->Ey, q[1] = c->Ez, q[2] = c->Hy, q[3] = c->Hz;
+			else if (axis == 1) q[0] = c->Ez, q[1] = c->Ex, q[2] = c->Hz, q[3] = c->Hx;
+			else q[0] = c->Ex, q[1] = c->Ey, q[2] = c->Hx, q[3] = c->Hy;
+			for (int r = 0; r < 4; r++)
+				CHECK("phaser_download", alisgpu_phaser_download(d->dp, n, f, r, (float *)&q[r][lo[s][0]][lo[s][1]][lo[s][2]]));
+		}
+	}
+	d->hostStale = 0;
+}
+
+void alis_be_sync_phaser(phaser P)
+{
+	devPhaser *d = findPhaser(P);
+	if (d && d->hostStale) downloadPhaser(d);
+}
+
+void alis_be_sync_all(void)
+{
+	CHECK("synchronize", alisgpu_synchronize());
+	for (devPhaser *d = phasers; d; d = d->next) if (d->hostStale) downloadPhaser(d);
+	for (devWorld *d = worlds; d; d = d->next) if (d->hostStale) downloadWorld(d);
+}
+
+
+/* ---- far field (reference src/farfld.c:248-459) ----
+ * FP64 face sums on the GPU over the phaser's device accumulators. */
+int alis_gpu_farfield(phaser P, int nA, const tfield *T, const float *kx, const float *ky, double complex *out);
+alisgpu_phaser *alis_gpu_phaser_handle(phaser P, int *index, int *faceSlot, int *nface);
+
+void alis_be_farfield_sums(phaser P, int nA, const tfield *T, const float *kx, const float *ky, double complex *out)
+{
+	devPhaser *d = findPhaser(P);
+	if (!d) { fprintf(stderr, "alis: far field of an unknown phaser\n"); exit(1); }
+	CHECK("phaser_flush", alisgpu_phaser_flush(d->dp));
+	if (alis_gpu_farfield(P, nA, T, kx, ky, out)) die("farfield_sums", ALISGPU_ECUDA);
+}
+
+/* device handle of a phaser set and the index of P in it */
+alisgpu_phaser *alis_gpu_phaser_handle(phaser P, int *index, int *faceSlot, int *nface)
+{
+	devPhaser *d = findPhaser(P);
+	if (!d) return 0;
+	*index = (int)(P - d->P);
+	*nface = d->nface;
+	memcpy(faceSlot, d->faceSlot, sizeof d->faceSlot);
+	return d->dp;
+}
+
+/* FP64 face sums of a batch of directions: host tables in double, the
+ * test fields widened to double, per-face partials from the device
+ * combined with the reference's face signs (-min, +max). */
+int alis_gpu_farfield(phaser P, int nA, const tfield *T, const float *kx, const float *ky, double complex *out)
+{
+	int index, slots[6], nface;
+	alisgpu_phaser *dp = alis_gpu_phaser_handle(P, &index, slots, &nface);
+	if (!dp) return -1;
+	world W = P->W;
+	alisgpu_farfield_geom g;
+	memset(&g, 0, sizeof g);
+	g.iMin = P->iMin, g.iMax = P->iMax, g.jMin = P->jMin, g.jMax = P->jMax, g.kMin = P->kMin, g.kMax = P->kMax, g.kMIN = P->kMIN;
+	g.sym[0] = W->xMinSur==SYM, g.sym[1] = W->yMinSur==SYM, g.sym[2] = W->zMinSur==SYM;
+	g.cosk[0] = W->coskx, g.cosk[1] = W->cosky, g.cosk[2] = W->coskz;
+	g.xLen = 1 + P->iMax - P->iMin, g.yLen = 1 + P->jMax - P->jMin, g.zLen = 2 + P->kMax - P->kMIN;
+	double *tab = calloc(4*g.xLen + 4*g.yLen + 2*g.zLen, sizeof(double));
+	double *xE = tab, *xH = xE + g.xLen, *dxE = xH + g.xLen, *dxH = dxE + g.xLen;
+	double *yE = dxH + g.xLen, *yH = yE + g.yLen, *dyE = yH + g.yLen, *dyH = dyE + g.yLen;
+	double *dzE = dyH + g.yLen, *dzH = dzE + g.zLen;
+	for (int i = P->iMin; i <= P->iMax; i++) {
+		int q = i - P->iMin;
+		xE[q] = W->itox(W, i), xH[q] = W->itox(W, i-0.5), dxE[q] = W->CE->dx[i], dxH[q] = W->CH->dx[i];
+	}
+	for (int j = P->jMin; j <= P->jMax; j++) {
+		int q = j - P->jMin;
+		yE[q] = W->jtoy(W, j), yH[q] = W->jtoy(W, j-0.5), dyE[q] = W->CE->dy[j], dyH[q] = W->CH->dy[j];
+	}
+	for (int k = P->kMIN; k <= P->kMax+1; k++) {
+		int q = k - P->kMIN;
+		dzE[q] = W->CE->dz[k], dzH[q] = W->CH->dz[k];
+	}
+	g.xE = xE, g.xH = xH, g.dxE = dxE, g.dxH = dxH, g.yE = yE, g.yH = yH, g.dyE = dyE, g.dyH = dyH, g.dzE = dzE, g.dzH = dzH;
+	int nk = g.zLen;
+	double *Td = calloc((size_t)nA * 6 * nk * 2, sizeof(double));
+	unsigned char *pr = calloc((size_t)nA * 6, 1);
+	double *kxd = calloc(nA, sizeof(double)), *kyd = calloc(nA, sizeof(double));
+	for (int a = 0; a < nA; a++) {
+		float complex *c[6] = { T[a].Ex, T[a].Ey, T[a].Ez, T[a].Hx, T[a].Hy, T[a].Hz };
+		for (int q = 0; q < 6; q++) {
+			if (!c[q]) continue;
+			pr[a*6+q] = 1;
+			for (int k = P->kMIN; k <= P->kMax+1; k++) {
+				size_t o = (((size_t)a*6 + q)*nk + (k - P->kMIN))*2;
+				Td[o] = crealf(c[q][k]), Td[o+1] = cimagf(c[q][k]);
+			}
+		}
+		kxd[a] = kx[a], kyd[a] = ky[a];
+	}
+	double *part = calloc((size_t)nA * 12, sizeof(double));
+	int rc = alisgpu_farfield_sums(dp, index, &g, nA, Td, nk, pr, kxd, kyd, part);
+	if (!rc) for (int a = 0; a < nA; a++) {
+		double complex s = 0;
+		for (int f = 0; f < nface; f++) {
+			double complex v = part[(a*6+f)*2] + I * part[(a*6+f)*2+1];
+			if (slots[f] % 2 == 0) s -= v; else s += v;
+		}
+		out[a] = s;
+	}
+	free(tab); free(Td); free(pr); free(kxd); free(kyd); free(part);
+	return rc;
+}

@@ -1,0 +1,837 @@
+// world.cu -- device worlds and the fused Yee half-step kernel.
+//
+// One launch per field set m updates every cell of a world in the order
+// of the reference's updateF / updateJ (src/update.c:87-158):
+//   conductivity factors of every dispersive object
+//   -> subtraction of every ADE current
+//   -> curl with dt/ds tables and eps^-1
+//   -> CPML psi recursions (faces xMin, yMin, zMin, xMax, yMax, zMax)
+//   -> TFSF incident-field corrections (src/update.c:194-272)
+//   -> (H half step) ADE current update driven by E.
+// The file is compiled with -fmad=false so that every add and multiply
+// rounds exactly as the reference's scalar code does; the arithmetic is
+// HBM-bound, so the lost FMAs cost nothing measurable.
+// Sources and ghost-cell copies follow as small launches, in the
+// reference order.
+#include <cstdio>
+#include <cstdarg>
+#include <cstring>
+#include <cstdlib>
+#include <vector>
+#include "common.cuh"
+
+// ---------------------------------------------------------------------
+// process-wide state: device, stream, error text, launch counter
+// ---------------------------------------------------------------------
+static cudaStream_t gStream;
+static int gInit;
+static char gErr[512];
+static unsigned long long gLaunches;
+static unsigned int *gErrWord;
+
+extern "C" int alisgpu__fail(int code, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(gErr, sizeof gErr, fmt, ap);
+	va_end(ap);
+	return code;
+}
+
+extern "C" int alisgpu__check(cudaError_t e, const char *what)
+{
+	int code = e == cudaErrorMemoryAllocation ? ALISGPU_ENOMEM : ALISGPU_ECUDA;
+	return alisgpu__fail(code, "%s: %s", what, cudaGetErrorString(e));
+}
+
+extern "C" const char *alisgpu_last_error(void) { return gErr; }
+extern "C" void alisgpu__count_launch(void) { gLaunches++; }
+extern "C" unsigned long long alisgpu_launch_count(void) { return gLaunches; }
+extern "C" cudaStream_t alisgpu__stream(void) { return gStream; }
+extern "C" void *alisgpu_stream(void) { return (void *)gStream; }
+
+extern "C" int alisgpu_init(void)
+{
+	if (gInit) return ALISGPU_OK;
+	int n = 0;
+	if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+		return alisgpu__fail(ALISGPU_ENODEV, "no CUDA device available");
+	const char *env = getenv("ALISGPU_DEVICE");
+	int dev = env ? atoi(env) : 0;
+	ALIS_CUDA(cudaSetDevice(dev));
+	ALIS_CUDA(cudaStreamCreateWithFlags(&gStream, cudaStreamNonBlocking));
+	ALIS_CUDA(cudaMalloc(&gErrWord, sizeof(unsigned int)));
+	ALIS_CUDA(cudaMemset(gErrWord, 0, sizeof(unsigned int)));
+	gInit = 1;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_synchronize(void)
+{
+	if (!gInit) return ALISGPU_OK;
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	unsigned int e = 0;
+	ALIS_CUDA(cudaMemcpy(&e, gErrWord, sizeof e, cudaMemcpyDeviceToHost));
+	if (e) return alisgpu__fail(ALISGPU_ERANGE, "device error word %#x", e);
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
+// world storage
+// ---------------------------------------------------------------------
+struct alisgpu_world {
+	alisgpu_geometry g;
+	Layout L;
+	float *E[2][3], *H[2][3];
+	float *C[3];
+	float *dtd[2][3];
+	float *cp[2][9];
+	BoxArr psi[2][2][6][2];           // [grid E/H][m][face][which]
+	std::vector<DevObj> objs;
+	DevObj *dObjs;
+	std::vector<void *> objMem;
+	size_t bytes;
+};
+
+static Layout makeLayout(const alisgpu_geometry *g)
+{
+	Layout L;
+	L.i0 = g->iMIN - 1, L.j0 = g->jMIN - 1, L.k0 = g->kMIN - 1;
+	L.ni = g->iMAX - g->iMIN + 3, L.nj = g->jMAX - g->jMIN + 3, L.nk = g->kMAX - g->kMIN + 3;
+	L.sj = ((ALIS_KOFF + L.nk + 31) / 32) * 32;
+	L.si = L.sj * L.nj;
+	return L;
+}
+
+static int devAlloc(alisgpu_world *w, float **p, size_t n)
+{
+	ALIS_CUDA(cudaMalloc(p, n * sizeof(float)));
+	ALIS_CUDA(cudaMemsetAsync(*p, 0, n * sizeof(float), gStream));
+	w->bytes += n * sizeof(float);
+	return ALISGPU_OK;
+}
+
+// psi slab boxes of face f for the E (Offset 0) or H (Offset 1) lattice,
+// same ranges as the host layer (reference src/world.c:174-186)
+static BoxArr slabBox(const alisgpu_geometry *g, int face, int Offset)
+{
+	int r[6] = { g->iMIN, g->iMAX, g->jMIN, g->jMAX, g->kMIN, g->kMAX };
+	int mins[3] = { g->iMin, g->jMin, g->kMin }, maxs[3] = { g->iMax, g->jMax, g->kMax };
+	int MINs[3] = { g->iMIN, g->jMIN, g->kMIN }, MAXs[3] = { g->iMAX, g->jMAX, g->kMAX };
+	int d = face % 3;
+	if (face < 3) r[2*d] = MINs[d] + Offset, r[2*d+1] = mins[d] + Offset - 2;
+	else r[2*d] = maxs[d] + 2, r[2*d+1] = MAXs[d];
+	BoxArr b;
+	b.p = 0;
+	b.i0 = r[0], b.i1 = r[1], b.j0 = r[2], b.j1 = r[3], b.k0 = r[4], b.k1 = r[5];
+	b.sj = 1 + b.k1 - b.k0;
+	b.si = b.sj * (1 + b.j1 - b.j0);
+	return b;
+}
+
+extern "C" int alisgpu_world_create(const alisgpu_geometry *g, alisgpu_world **out)
+{
+	int rc = alisgpu_init();
+	if (rc) return rc;
+	if (!g || !out) return alisgpu__fail(ALISGPU_EINVAL, "world_create: null argument");
+	if (g->iMAX < g->iMIN || g->jMAX < g->jMIN || g->kMAX < g->kMIN)
+		return alisgpu__fail(ALISGPU_EINVAL, "world_create: empty grid");
+	alisgpu_world *w = new alisgpu_world();
+	w->g = *g;
+	w->L = makeLayout(g);
+	size_t n = w->L.elems();
+	for (int m = 0; m <= g->complexField; m++) for (int c = 0; c < 3; c++) {
+		if ((rc = devAlloc(w, &w->E[m][c], n)) || (rc = devAlloc(w, &w->H[m][c], n))) { alisgpu_world_destroy(w); return rc; }
+	}
+	for (int grid = 0; grid < 2; grid++) for (int m = 0; m <= g->complexField; m++) for (int f = 0; f < 6; f++) {
+		if (!g->pml[f]) continue;
+		for (int q = 0; q < 2; q++) {
+			BoxArr b = slabBox(g, f, grid);
+			if (b.i1 < b.i0 || b.j1 < b.j0 || b.k1 < b.k0) continue;
+			if ((rc = devAlloc(w, &b.p, b.elems()))) { alisgpu_world_destroy(w); return rc; }
+			w->psi[grid][m][f][q] = b;
+		}
+	}
+	*out = w;
+	return ALISGPU_OK;
+}
+
+static void freeObjects(alisgpu_world *w)
+{
+	for (void *p : w->objMem) cudaFree(p);
+	w->objMem.clear();
+	w->objs.clear();
+	if (w->dObjs) cudaFree(w->dObjs), w->dObjs = 0;
+}
+
+extern "C" int alisgpu_world_destroy(alisgpu_world *w)
+{
+	if (!w) return ALISGPU_OK;
+	cudaStreamSynchronize(gStream);
+	for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+		if (w->E[m][c]) cudaFree(w->E[m][c]);
+		if (w->H[m][c]) cudaFree(w->H[m][c]);
+	}
+	for (int c = 0; c < 3; c++) if (w->C[c]) cudaFree(w->C[c]);
+	for (int grid = 0; grid < 2; grid++) {
+		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) cudaFree(w->dtd[grid][c]);
+		for (int c = 0; c < 9; c++) if (w->cp[grid][c]) cudaFree(w->cp[grid][c]);
+		for (int m = 0; m < 2; m++) for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++)
+			if (w->psi[grid][m][f][q].p) cudaFree(w->psi[grid][m][f][q].p);
+	}
+	freeObjects(w);
+	delete w;
+	return ALISGPU_OK;
+}
+
+extern "C" size_t alisgpu_world_bytes(const alisgpu_world *w) { return w ? w->bytes : 0; }
+
+extern "C" int alisgpu_world_reset(alisgpu_world *w)
+{
+	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_reset: null world");
+	size_t n = w->L.elems() * sizeof(float);
+	for (int m = 0; m <= w->g.complexField; m++) for (int c = 0; c < 3; c++) {
+		ALIS_CUDA(cudaMemsetAsync(w->E[m][c], 0, n, gStream));
+		ALIS_CUDA(cudaMemsetAsync(w->H[m][c], 0, n, gStream));
+	}
+	for (int grid = 0; grid < 2; grid++) for (int m = 0; m < 2; m++) for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) {
+		BoxArr &b = w->psi[grid][m][f][q];
+		if (b.p) ALIS_CUDA(cudaMemsetAsync(b.p, 0, b.elems() * sizeof(float), gStream));
+	}
+	for (DevObj &o : w->objs) {
+		size_t cells = (size_t)(1 + o.i1 - o.i0) * o.si;
+		for (int m = 0; m < 2; m++) for (int p = 0; p < ALIS_MAXPOLES; p++) for (int a = 0; a < 3; a++) {
+			if (o.J[m][p][a]) ALIS_CUDA(cudaMemsetAsync(o.J[m][p][a], 0, cells * sizeof(float), gStream));
+			if (o.K[m][p][a]) ALIS_CUDA(cudaMemsetAsync(o.K[m][p][a], 0, cells * sizeof(float), gStream));
+		}
+	}
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
+// uploads and downloads
+// ---------------------------------------------------------------------
+static int upload1D(alisgpu_world *w, float **dst, const float *src, int n)
+{
+	if (*dst) { cudaFree(*dst); *dst = 0; }
+	if (!src) return ALISGPU_OK;
+	ALIS_CUDA(cudaMalloc(dst, n * sizeof(float)));
+	ALIS_CUDA(cudaMemcpy(*dst, src, n * sizeof(float), cudaMemcpyHostToDevice));
+	(void)w;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *const dtd[3], const float *const cpml[9])
+{
+	if (!w || grid < 0 || grid > 1 || !dtd) return alisgpu__fail(ALISGPU_EINVAL, "set_line_tables: bad argument");
+	int len[3] = { w->g.iMAX - w->g.iMIN + 1, w->g.jMAX - w->g.jMIN + 1, w->g.kMAX - w->g.kMIN + 1 };
+	int rc;
+	for (int a = 0; a < 3; a++) if ((rc = upload1D(w, &w->dtd[grid][a], dtd[a], len[a]))) return rc;
+	for (int q = 0; q < 9; q++) if ((rc = upload1D(w, &w->cp[grid][q], cpml ? cpml[q] : 0, len[q / 3]))) return rc;
+	return ALISGPU_OK;
+}
+
+// host box [i0,i1]x[j0,j1]x[k0,k1] -> device halo'd layout
+static int uploadBoxToLayout(alisgpu_world *w, float *dev, const float *host, int i0, int i1, int j0, int j1, int k0, int k1)
+{
+	int nj = 1 + j1 - j0, nk = 1 + k1 - k0;
+	for (int i = i0; i <= i1; i++) {
+		const float *src = host + (size_t)(i - i0) * nj * nk;
+		float *dst = dev + w->L.at(i, j0, k0);
+		ALIS_CUDA(cudaMemcpy2DAsync(dst, w->L.sj * sizeof(float), src, nk * sizeof(float), nk * sizeof(float), nj,
+		                            cudaMemcpyHostToDevice, gStream));
+	}
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *cy, const float *cz)
+{
+	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "set_eps: null world");
+	const alisgpu_geometry &g = w->g;
+	const float *src[3] = { cx, cy, cz };
+	int rc;
+	for (int a = 0; a < 3; a++) {
+		if (!src[a]) {
+			if (w->C[a]) { cudaStreamSynchronize(gStream); cudaFree(w->C[a]); w->bytes -= w->L.elems() * sizeof(float); w->C[a] = 0; }
+			continue;
+		}
+		if (!w->C[a] && (rc = devAlloc(w, &w->C[a], w->L.elems()))) return rc;
+		int i1 = g.iMAX + (a == 0), j1 = g.jMAX + (a == 1), k1 = g.kMAX + (a == 2);
+		if ((rc = uploadBoxToLayout(w, w->C[a], src[a], g.iMIN, i1, g.jMIN, j1, g.kMIN, k1))) return rc;
+	}
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *objs)
+{
+	if (!w || n < 0 || (n && !objs)) return alisgpu__fail(ALISGPU_EINVAL, "set_dispersive: bad argument");
+	cudaStreamSynchronize(gStream);
+	freeObjects(w);
+	for (int q = 0; q < n; q++) {
+		const alisgpu_dispersive &s = objs[q];
+		if (s.NK > ALIS_MAXPOLES || s.NJ > s.NK || s.NJ < 0)
+			return alisgpu__fail(ALISGPU_ERANGE, "set_dispersive: object %d has %d poles (max %d)", q, s.NK, ALIS_MAXPOLES);
+		DevObj o;
+		memset(&o, 0, sizeof o);
+		o.i0 = s.iMin, o.i1 = s.iMax, o.j0 = s.jMin, o.j1 = s.jMax, o.k0 = s.kMin, o.k1 = s.kMax;
+		o.NJ = s.NJ, o.NK = s.NK;
+		o.sj = 1 + o.k1 - o.k0;
+		o.si = o.sj * (1 + o.j1 - o.j0);
+		size_t cells = (size_t)(1 + o.i1 - o.i0) * o.si;
+		for (int a = 0; a < 3; a++) {
+			o.a[a] = s.a[a];
+			for (int p = 0; p < s.NK; p++) {
+				o.JJ[p][a] = s.JJ[a][p], o.JK[p][a] = s.JK[a] ? s.JK[a][p] : 0, o.JE[p][a] = s.JE[a][p];
+				if (p >= s.NJ) o.KJ[p][a] = s.KJ[a][p], o.KK[p][a] = s.KK[a][p], o.KE[p][a] = s.KE[a][p];
+			}
+			float *d;
+			int rc = devAlloc(w, &d, cells);
+			if (rc) return rc;
+			w->objMem.push_back(d);
+			ALIS_CUDA(cudaMemcpy(d, s.fill[a], cells * sizeof(float), cudaMemcpyHostToDevice));
+			o.fill[a] = d;
+		}
+		o.cond = s.a[0] != 0 || s.a[1] != 0 || s.a[2] != 0;
+		for (int m = 0; m <= w->g.complexField; m++) for (int p = 0; p < s.NK; p++) for (int a = 0; a < 3; a++) {
+			float *d;
+			int rc = devAlloc(w, &d, cells);
+			if (rc) return rc;
+			w->objMem.push_back(d);
+			o.J[m][p][a] = d;
+			if (p >= s.NJ) {
+				if ((rc = devAlloc(w, &d, cells))) return rc;
+				w->objMem.push_back(d);
+				o.K[m][p][a] = d;
+			}
+		}
+		w->objs.push_back(o);
+	}
+	if (n) {
+		ALIS_CUDA(cudaMalloc(&w->dObjs, n * sizeof(DevObj)));
+		ALIS_CUDA(cudaMemcpy(w->dObjs, w->objs.data(), n * sizeof(DevObj), cudaMemcpyHostToDevice));
+	}
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
+{
+	if (field < 0 || field > 1 || m < 0 || m > w->g.complexField || comp < 0 || comp > 2) return 0;
+	return field ? w->H[m][comp] : w->E[m][comp];
+}
+
+extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
+{
+	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
+	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_download: bad argument");
+	const Layout &L = w->L;
+	ALIS_CUDA(cudaMemcpy2DAsync(host, L.nk * sizeof(float), d + ALIS_KOFF, L.sj * sizeof(float), L.nk * sizeof(float),
+	                            (size_t)L.ni * L.nj, cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
+{
+	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
+	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_upload: bad argument");
+	const Layout &L = w->L;
+	ALIS_CUDA(cudaMemcpy2DAsync(d + ALIS_KOFF, L.sj * sizeof(float), host, L.nk * sizeof(float), L.nk * sizeof(float),
+	                            (size_t)L.ni * L.nj, cudaMemcpyHostToDevice, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host)
+{
+	if (!w || !host || n < 0 || n >= (int)w->objs.size() || m < 0 || m > w->g.complexField || comp < 0 || comp > 2)
+		return alisgpu__fail(ALISGPU_EINVAL, "current_download: bad argument");
+	DevObj &o = w->objs[n];
+	if (p < 0 || p >= o.NK || (isK && p < o.NJ)) return alisgpu__fail(ALISGPU_EINVAL, "current_download: bad pole");
+	float *d = isK ? o.K[m][p][comp] : o.J[m][p][comp];
+	size_t cells = (size_t)(1 + o.i1 - o.i0) * o.si;
+	ALIS_CUDA(cudaMemcpyAsync(host, d, cells * sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
+// the fused half-step kernel
+// ---------------------------------------------------------------------
+#define TX 32
+#define TY 8
+
+// aux-world index of a main-world cell, with the row aliasing of the
+// reference's expandFieldX/Y (src/source.c:223-249)
+__device__ __forceinline__ long long auxAt(const DevTfsf &t, int i, int j, int k, int altX, int altY)
+{
+	if (t.aliasX && i > t.auxIMAX) i = t.auxIMAX + altX;
+	if (t.aliasY && j > t.auxJMAX) j = t.auxJMAX + altY;
+	// outside the auxiliary grid the reference reads undefined memory;
+	// here the sample is skipped and the error word records it
+	if (i < t.L.i0 || i >= t.L.i0 + t.L.ni || j < t.L.j0 || j >= t.L.j0 + t.L.nj || k < t.L.k0 || k >= t.L.k0 + t.L.nk)
+		return -1;
+	return t.L.at(i, j, k);
+}
+
+// aux sample, 0 (and error bit 1) when outside the auxiliary grid
+__device__ __forceinline__ float auxGet(const float *A, long long q, unsigned int *err)
+{
+	if (q < 0) { atomicOr(err, 1u); return 0.0f; }
+	return A[q];
+}
+
+// Alt = +1: E half step (neighbours at +1, ALT=1); Alt = -1: H half step.
+template <int ALT>
+__global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
+{
+	__shared__ int list[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
+	const int j = P.jMIN + blockIdx.y * TY + threadIdx.y;
+	const int i = P.iMIN + blockIdx.z;
+
+	// objects whose box meets this tile, in list order (one warp builds it)
+	if (P.nobj) {
+		if (threadIdx.y == 0) {
+			int tj0 = P.jMIN + blockIdx.y * TY, tj1 = min(tj0 + TY - 1, P.jMAX);
+			int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
+			int cnt = 0;
+			for (int base = 0; base < P.nobj; base += 32) {
+				int n = base + threadIdx.x;
+				bool hit = false;
+				if (n < P.nobj) {
+					const DevObj &o = P.obj[n];
+					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
+				}
+				unsigned bal = __ballot_sync(0xffffffffu, hit);
+				if (hit) {
+					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
+					if (pos < ALIS_TILE_OBJ) list[pos] = n;
+				}
+				cnt += __popc(bal);
+			}
+			if (threadIdx.x == 0) nlist = cnt;
+		}
+		__syncthreads();
+	}
+	if (k > P.kMAX || j > P.jMAX) return;
+
+	const long long c = P.L.at(i, j, k);
+	const long long si = P.L.si, sj = P.L.sj;
+	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const int nl = P.nobj ? nlist : 0;
+	const bool overflow = nl > ALIS_TILE_OBJ;
+	const int nIter = overflow ? P.nobj : nl;
+
+	// conductivity factors (reference src/update.c:89-98).  Only the E
+	// coefficient set holds objects; H is updated with CH, whose object
+	// list is always empty, so both loops are skipped in the H step.
+	for (int q = 0; q < (ALT == 1 ? nIter : 0); q++) {
+		const DevObj &o = P.obj[overflow ? q : list[q]];
+		if (!o.cond) continue;
+		if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
+		long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
+		float gx = o.fill[0][b], gy = o.fill[1][b], gz = o.fill[2][b];
+		fx *= (1 - o.a[0] * gx) / (1 + o.a[0] * gx);
+		fy *= (1 - o.a[1] * gy) / (1 + o.a[1] * gy);
+		fz *= (1 - o.a[2] * gz) / (1 + o.a[2] * gz);
+	}
+	// polarisation currents (reference src/update.c:99-108)
+	for (int q = 0; q < (ALT == 1 ? nIter : 0); q++) {
+		const DevObj &o = P.obj[overflow ? q : list[q]];
+		if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
+		long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
+		for (int p = 0; p < o.NK; p++) {
+			fx -= o.J[P.m][p][0][b];
+			fy -= o.J[P.m][p][1][b];
+			fz -= o.J[P.m][p][2][b];
+		}
+	}
+
+	// curl (reference src/update.c:109-118)
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	const float gx0 = Gx[c], gy0 = Gy[c], gz0 = Gz[c];
+	const float dx = P.dtd[0][i - P.iMIN], dy = P.dtd[1][j - P.jMIN], dz = P.dtd[2][k - P.kMIN];
+	const float gyk = Gy[c + ALT], gzj = Gz[c + ALT * sj], gzi = Gz[c + ALT * si];
+	const float gxk = Gx[c + ALT], gxj = Gx[c + ALT * sj], gyi = Gy[c + ALT * si];
+	const bool hasC = P.C[0] != 0;
+	float cx = 1, cy = 1, cz = 1;
+	if (hasC) {
+		cx = P.C[0][c], cy = P.C[1][c], cz = P.C[2][c];
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
+	} else {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
+	}
+
+	// CPML (reference src/update.c:48-84, 119-124), faces in reference order
+#pragma unroll
+	for (int f = 0; f < 6; f++) {
+		if (!P.slabOn[f]) continue;
+		const int ax = f % 3;
+		const int pos = ax == 0 ? i : ax == 1 ? j : k;
+		if (pos < P.slabLo[f] || pos > P.slabHi[f]) continue;
+		const BoxArr &A = P.psi[f][0], &B = P.psi[f][1];
+		const long long a = A.at(i, j, k);
+		if (ax == 0) {
+			const int q = i - P.iMIN;
+			float py = P.cp[0][q] * A.p[a] + P.cp[1][q] * (gz0 - gzi);
+			float pz = P.cp[0][q] * B.p[a] + P.cp[2][q] * (gy0 - gyi);
+			A.p[a] = py, B.p[a] = pz;
+			if (hasC) fy += py * cy, fz += pz * cz; else fy += py, fz += pz;
+		} else if (ax == 1) {
+			const int q = j - P.jMIN;
+			float pz = P.cp[3][q] * A.p[a] + P.cp[4][q] * (gx0 - gxj);
+			float px = P.cp[3][q] * B.p[a] + P.cp[5][q] * (gz0 - gzj);
+			A.p[a] = pz, B.p[a] = px;
+			if (hasC) fz += pz * cz, fx += px * cx; else fz += pz, fx += px;
+		} else {
+			const int q = k - P.kMIN;
+			float px = P.cp[6][q] * A.p[a] + P.cp[7][q] * (gy0 - gyk);
+			float py = P.cp[6][q] * B.p[a] + P.cp[8][q] * (gx0 - gxk);
+			A.p[a] = px, B.p[a] = py;
+			if (hasC) fx += px * cx, fy += py * cy; else fx += px, fy += py;
+		}
+	}
+
+	// TFSF incident-field corrections (reference src/update.c:205-272).
+	// E step: aux H; H step: aux E.  Face-by-face in the reference order;
+	// (dtds * G) * C rounds like the reference's `dtds * G[..] * C[..]`.
+	for (int s = 0; s < P.ntfsf; s++) {
+		const DevTfsf &T = P.tf[s];
+		const float *A0 = T.G[P.m][0], *A1 = T.G[P.m][1], *A2 = T.G[P.m][2];
+		if (ALT == 1) {
+			// E half step; alias Alt of H components: X (0,1,1), Y (1,0,1)
+			if (T.iMin > P.iMIN && i == T.iMin) {
+				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) { float v = -T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 1, 0), P.err); fz += hasC ? v * cz : v; }
+				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) { float v = T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 1, 1), P.err); fy += hasC ? v * cy : v; }
+			}
+			if (T.jMin > P.jMIN && j == T.jMin) {
+				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) { float v = -T.dtdMin[1] * auxGet(A2, auxAt(T, i, j, k, 1, 1), P.err); fx += hasC ? v * cx : v; }
+				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) { float v = T.dtdMin[1] * auxGet(A0, auxAt(T, i, j, k, 0, 1), P.err); fz += hasC ? v * cz : v; }
+			}
+			if (T.kMin > P.kMIN && k == T.kMin) {
+				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) { float v = -T.dtdMin[2] * auxGet(A0, auxAt(T, i, j, k, 0, 1), P.err); fy += hasC ? v * cy : v; }
+				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) { float v = T.dtdMin[2] * auxGet(A1, auxAt(T, i, j, k, 1, 0), P.err); fx += hasC ? v * cx : v; }
+			}
+			if (T.iMax < P.iMAX && i == T.iMax) {
+				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) { float v = T.dtdMax[0] * auxGet(A1, auxAt(T, i + 1, j, k, 1, 0), P.err); fz += hasC ? v * cz : v; }
+				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) { float v = -T.dtdMax[0] * auxGet(A2, auxAt(T, i + 1, j, k, 1, 1), P.err); fy += hasC ? v * cy : v; }
+			}
+			if (T.jMax < P.jMAX && j == T.jMax) {
+				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) { float v = T.dtdMax[1] * auxGet(A2, auxAt(T, i, j + 1, k, 1, 1), P.err); fx += hasC ? v * cx : v; }
+				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) { float v = -T.dtdMax[1] * auxGet(A0, auxAt(T, i, j + 1, k, 0, 1), P.err); fz += hasC ? v * cz : v; }
+			}
+			if (T.kMax < P.kMAX && k == T.kMax) {
+				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) { float v = T.dtdMax[2] * auxGet(A0, auxAt(T, i, j, k + 1, 0, 1), P.err); fy += hasC ? v * cy : v; }
+				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) { float v = -T.dtdMax[2] * auxGet(A1, auxAt(T, i, j, k + 1, 1, 0), P.err); fx += hasC ? v * cx : v; }
+			}
+		} else {
+			// H half step; alias Alt of E components: X (1,0,0), Y (0,1,0)
+			if (T.iMin > P.iMIN && i == T.iMin) {
+				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) fz += T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 0, 1), P.err);
+				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) fy += -T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 0, 0), P.err);
+			}
+			if (T.jMin > P.jMIN && j == T.jMin) {
+				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) fx += T.dtdMin[1] * auxGet(A2, auxAt(T, i, j, k, 0, 0), P.err);
+				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) fz += -T.dtdMin[1] * auxGet(A0, auxAt(T, i, j, k, 1, 0), P.err);
+			}
+			if (T.kMin > P.kMIN && k == T.kMin) {
+				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) fy += T.dtdMin[2] * auxGet(A0, auxAt(T, i, j, k, 1, 0), P.err);
+				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) fx += -T.dtdMin[2] * auxGet(A1, auxAt(T, i, j, k, 0, 1), P.err);
+			}
+			if (T.iMax < P.iMAX && i == T.iMax + 1) {
+				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) fz += -T.dtdMax[0] * auxGet(A1, auxAt(T, i - 1, j, k, 0, 1), P.err);
+				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) fy += T.dtdMax[0] * auxGet(A2, auxAt(T, i - 1, j, k, 0, 0), P.err);
+			}
+			if (T.jMax < P.jMAX && j == T.jMax + 1) {
+				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) fx += -T.dtdMax[1] * auxGet(A2, auxAt(T, i, j - 1, k, 0, 0), P.err);
+				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) fz += T.dtdMax[1] * auxGet(A0, auxAt(T, i, j - 1, k, 1, 0), P.err);
+			}
+			if (T.kMax < P.kMAX && k == T.kMax + 1) {
+				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) fy += -T.dtdMax[2] * auxGet(A0, auxAt(T, i, j, k - 1, 1, 0), P.err);
+				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) fx += T.dtdMax[2] * auxGet(A1, auxAt(T, i, j, k - 1, 0, 1), P.err);
+			}
+		}
+	}
+
+	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+
+	// ADE currents driven by E, run inside updateH (reference src/update.c:128-158)
+	if (ALT == -1) {
+		for (int q = 0; q < nIter; q++) {
+			const DevObj &o = P.obj[overflow ? q : list[q]];
+			if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
+			long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
+			const float e[3] = { gx0, gy0, gz0 };
+#pragma unroll
+			for (int a = 0; a < 3; a++) {
+				const float fe = o.fill[a][b];
+				for (int p = 0; p < o.NJ; p++) {
+					float *J = o.J[P.m][p][a];
+					J[b] = o.JJ[p][a] * J[b] + o.JE[p][a] * fe * e[a];
+				}
+				for (int p = o.NJ; p < o.NK; p++) {
+					float *J = o.J[P.m][p][a], *K = o.K[P.m][p][a];
+					float jn = o.JJ[p][a] * J[b] + o.JK[p][a] * K[b] + o.JE[p][a] * fe * e[a];
+					J[b] = jn;
+					K[b] = o.KJ[p][a] * jn + o.KK[p][a] * K[b] + o.KE[p][a] * fe * e[a];
+				}
+			}
+		}
+	}
+}
+
+// sources, in list order; one block so later patches see earlier ones
+// (reference src/update.c:161-179)
+#define ALIS_MAXSRC 32
+#define ALIS_MAXSRCV 2048
+struct SourceParams {
+	int n;
+	Layout L;
+	float *F[2][3];
+	alisgpu_source_patch p[ALIS_MAXSRC];
+	const float *vdev;                       // values beyond the inline buffer
+	unsigned int *err;
+	float v[ALIS_MAXSRCV];
+};
+
+__global__ void k_sources(const SourceParams P)
+{
+	for (int q = 0; q < P.n; q++) {
+		const alisgpu_source_patch &s = P.p[q];
+		int nk = 1 + s.k1 - s.k0, nj = 1 + s.j1 - s.j0, ni = 1 + s.i1 - s.i0;
+		int cells = ni * nj * nk;
+		float *F = P.F[s.m][s.comp];
+		for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+			int kk = t % nk, jj = (t / nk) % nj, ii = t / (nk * nj);
+			float v = P.vdev ? P.vdev[s.voff + t] : P.v[s.voff + t];
+			int i = s.i0 + ii, j = s.j0 + jj, k = s.k0 + kk;
+			if (i < P.L.i0 || i >= P.L.i0 + P.L.ni || j < P.L.j0 || j >= P.L.j0 + P.L.nj || k < P.L.k0 || k >= P.L.k0 + P.L.nk) {
+				atomicOr(P.err, 4u);
+				continue;
+			}
+			F[P.L.at(i, j, k)] += v;
+		}
+		__syncthreads();
+	}
+}
+
+// one group of independent ghost copies (reference src/update.c:182-191)
+#define ALIS_GHOST_GROUP 4
+struct GhostParams {
+	int n;
+	Layout L;
+	float *F[2][3];
+	int complexField;
+	alisgpu_ghost_copy c[ALIS_GHOST_GROUP];
+	long long start[ALIS_GHOST_GROUP + 1];
+	unsigned int *err;
+};
+
+__global__ void k_ghost(const GhostParams P)
+{
+	long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= P.start[P.n]) return;
+	int q = 0;
+	while (t >= P.start[q + 1]) q++;
+	const alisgpu_ghost_copy &g = P.c[q];
+	long long r = t - P.start[q];
+	int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
+	int kk = (int)(r % nk), jj = (int)((r / nk) % nj), ii = (int)(r / ((long long)nk * nj));
+	int i = g.i0 + ii, j = g.j0 + jj, k = g.k0 + kk;
+	int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
+	if (i < P.L.i0 || i >= P.L.i0 + P.L.ni || j < P.L.j0 || j >= P.L.j0 + P.L.nj || k < P.L.k0 || k >= P.L.k0 + P.L.nk ||
+	    si < P.L.i0 || si >= P.L.i0 + P.L.ni || sj < P.L.j0 || sj >= P.L.j0 + P.L.nj || sk < P.L.k0 || sk >= P.L.k0 + P.L.nk) {
+		atomicOr(P.err, 2u);
+		return;
+	}
+	long long d = P.L.at(i, j, k), s = P.L.at(si, sj, sk);
+	float *F = P.F[0][g.comp];
+	if (P.complexField) {
+		float *G = P.F[1][g.comp];
+		float f = F[s], gg = G[s];
+		F[d] = g.cosk * f + g.sink * gg;
+		G[d] = g.cosk * gg - g.sink * f;
+	} else {
+		F[d] = g.cosk * F[s];
+	}
+}
+
+// ---------------------------------------------------------------------
+// host driver of one half step
+// ---------------------------------------------------------------------
+static void fillTfsf(DevTfsf &T, const alisgpu_tfsf &s, int field, const float *dtdMain[3], const alisgpu_geometry &g)
+{
+	T.iMin = s.iMin, T.iMax = s.iMax, T.jMin = s.jMin, T.jMax = s.jMax, T.kMin = s.kMin, T.kMax = s.kMax;
+	T.iMIN = s.iMIN, T.iMAX = s.iMAX, T.jMIN = s.jMIN, T.jMAX = s.jMAX, T.kMIN = s.kMIN, T.kMAX = s.kMAX;
+	T.auxIMAX = s.auxIMAX, T.auxJMAX = s.auxJMAX, T.aliasX = s.aliasX, T.aliasY = s.aliasY;
+	T.L = s.aux->L;
+	for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+		int mm = m <= s.aux->g.complexField ? m : 0;
+		T.G[m][c] = field == 0 ? s.aux->H[mm][c] : s.aux->E[mm][c];
+	}
+	// dt/ds at the faces: E step uses iMin / iMax, H step iMin / iMax+1
+	int lo[3] = { s.iMin, s.jMin, s.kMin };
+	int hi[3] = { s.iMax + field, s.jMax + field, s.kMax + field };
+	int base[3] = { g.iMIN, g.jMIN, g.kMIN };
+	int top[3] = { g.iMAX, g.jMAX, g.kMAX };
+	for (int a = 0; a < 3; a++) {
+		float v0 = 0, v1 = 0;
+		if (lo[a] >= base[a] && lo[a] <= top[a]) cudaMemcpy(&v0, dtdMain[a] + (lo[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
+		if (hi[a] >= base[a] && hi[a] <= top[a]) cudaMemcpy(&v1, dtdMain[a] + (hi[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
+		T.dtdMin[a] = v0, T.dtdMax[a] = v1;
+	}
+}
+
+// cached dt/ds face values: the TFSF box is fixed once set up
+struct TfsfCache { const alisgpu_tfsf *key; int field; DevTfsf T; };
+static std::vector<TfsfCache> gTfsfCache;
+
+static const DevTfsf &tfsfFor(alisgpu_world *w, const alisgpu_tfsf &s, int field)
+{
+	for (TfsfCache &c : gTfsfCache)
+		if (c.key == &s && c.field == field && c.T.iMin == s.iMin && c.T.kMax == s.kMax && c.T.L.ni == s.aux->L.ni) return c.T;
+	TfsfCache c;
+	c.key = &s, c.field = field;
+	const float *dtd[3] = { w->dtd[field][0], w->dtd[field][1], w->dtd[field][2] };
+	fillTfsf(c.T, s, field, dtd, w->g);
+	gTfsfCache.push_back(c);
+	return gTfsfCache.back().T;
+}
+
+extern "C" void alisgpu__forget_tfsf(const alisgpu_tfsf *s)
+{
+	for (size_t q = 0; q < gTfsfCache.size();)
+		if (gTfsfCache[q].key == s) gTfsfCache.erase(gTfsfCache.begin() + q); else q++;
+}
+
+extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s)
+{
+	if (!w || !s || s->field < 0 || s->field > 1) return alisgpu__fail(ALISGPU_EINVAL, "half_step: bad argument");
+	if (s->ntfsf > ALIS_MAXTFSF) return alisgpu__fail(ALISGPU_ERANGE, "half_step: %d TFSF boxes (max %d)", s->ntfsf, ALIS_MAXTFSF);
+	const alisgpu_geometry &g = w->g;
+	const int field = s->field;
+	if (!w->dtd[field][0]) return alisgpu__fail(ALISGPU_EINVAL, "half_step: line tables not set");
+	HalfStepParams P;
+	memset(&P, 0, sizeof P);
+	P.iMIN = g.iMIN, P.iMAX = g.iMAX, P.jMIN = g.jMIN, P.jMAX = g.jMAX, P.kMIN = g.kMIN, P.kMAX = g.kMAX;
+	P.iMin = g.iMin, P.iMax = g.iMax, P.jMin = g.jMin, P.jMax = g.jMax, P.kMin = g.kMin, P.kMax = g.kMax;
+	P.L = w->L;
+	for (int a = 0; a < 3; a++) P.dtd[a] = w->dtd[field][a];
+	for (int q = 0; q < 9; q++) P.cp[q] = w->cp[field][q];
+	int mins[3] = { g.iMin, g.jMin, g.kMin }, maxs[3] = { g.iMax, g.jMax, g.kMax };
+	int MINs[3] = { g.iMIN, g.jMIN, g.kMIN }, MAXs[3] = { g.iMAX, g.jMAX, g.kMAX };
+	const int Alt = field == 0 ? 1 : -1;
+	for (int f = 0; f < 6; f++) {
+		int a = f % 3;
+		bool on = f < 3 ? MINs[a] < mins[a] : MAXs[a] > maxs[a];
+		if (!on) continue;
+		if (!w->psi[field][0][f][0].p) continue;
+		P.slabOn[f] = 1;
+		if (f < 3) P.slabLo[f] = MINs[a] - (Alt - 1) / 2, P.slabHi[f] = mins[a] - (Alt + 3) / 2;
+		else P.slabLo[f] = maxs[a] + 2, P.slabHi[f] = MAXs[a];
+	}
+	P.nobj = (int)w->objs.size();
+	P.obj = w->dObjs;
+	P.ntfsf = s->ntfsf;
+	for (int q = 0; q < s->ntfsf; q++) P.tf[q] = tfsfFor(w, s->tfsf[q], field);
+	P.err = gErrWord;
+
+	dim3 block(TX, TY, 1);
+	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + TY) / TY, g.iMAX - g.iMIN + 1);
+	for (int m = 0; m <= g.complexField; m++) {
+		P.m = m;
+		for (int c = 0; c < 3; c++) {
+			P.F[c] = field == 0 ? w->E[m][c] : w->H[m][c];
+			P.G[c] = field == 0 ? w->H[m][c] : w->E[m][c];
+			P.C[c] = field == 0 ? w->C[c] : 0;
+			P.Fother[c] = w->E[m][c];
+		}
+		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
+		if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
+		else k_half_step<-1><<<grid, block, 0, gStream>>>(P);
+		alisgpu__count_launch();
+	}
+	ALIS_CUDA(cudaGetLastError());
+
+	// sources
+	if (s->nsrc > 0) {
+		if (s->nsrc > ALIS_MAXSRC) return alisgpu__fail(ALISGPU_ERANGE, "half_step: %d source patches (max %d)", s->nsrc, ALIS_MAXSRC);
+		static SourceParams SP;
+		SP.n = s->nsrc;
+		SP.L = w->L;
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			SP.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		memcpy(SP.p, s->src, s->nsrc * sizeof(alisgpu_source_patch));
+		SP.vdev = 0;
+		SP.err = gErrWord;
+		static float *vbuf;
+		static int vcap;
+		if (s->nvalues <= ALIS_MAXSRCV) {
+			memcpy(SP.v, s->values, s->nvalues * sizeof(float));
+		} else {
+			// large patches: values staged in device memory (ordered on the stream)
+			if (s->nvalues > vcap) {
+				cudaStreamSynchronize(gStream);
+				if (vbuf) cudaFree(vbuf);
+				ALIS_CUDA(cudaMalloc(&vbuf, s->nvalues * sizeof(float)));
+				vcap = s->nvalues;
+			}
+			ALIS_CUDA(cudaMemcpyAsync(vbuf, s->values, s->nvalues * sizeof(float), cudaMemcpyHostToDevice, gStream));
+			ALIS_CUDA(cudaStreamSynchronize(gStream));
+			SP.vdev = vbuf;
+		}
+		k_sources<<<1, 256, 0, gStream>>>(SP);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+
+	// ghost copies: consecutive copies of distinct components share a launch
+	int q = 0;
+	while (q < s->nghost) {
+		GhostParams GP;
+		memset(&GP, 0, sizeof GP);
+		GP.L = w->L;
+		GP.err = gErrWord;
+		GP.complexField = g.complexField;
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			GP.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		int used = 0;
+		while (q < s->nghost && GP.n < ALIS_GHOST_GROUP && !(used & (1 << s->ghost[q].comp))) {
+			const alisgpu_ghost_copy &c = s->ghost[q];
+			used |= 1 << c.comp;
+			GP.c[GP.n] = c;
+			long long cells = (c.i1 < c.i0 || c.j1 < c.j0 || c.k1 < c.k0) ? 0 :
+				(long long)(1 + c.i1 - c.i0) * (1 + c.j1 - c.j0) * (1 + c.k1 - c.k0);
+			GP.start[GP.n + 1] = GP.start[GP.n] + cells;
+			GP.n++;
+			q++;
+		}
+		long long total = GP.start[GP.n];
+		if (total > 0) {
+			k_ghost<<<(unsigned)((total + 255) / 256), 256, 0, gStream>>>(GP);
+			alisgpu__count_launch();
+			ALIS_CUDA(cudaGetLastError());
+		}
+	}
+	return ALISGPU_OK;
+}
+
+// field pointers of set m for the phaser gather kernel
+extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L)
+{
+	if (!w || m < 0 || m > w->g.complexField) return alisgpu__fail(ALISGPU_EINVAL, "world_fields: bad argument");
+	for (int c = 0; c < 3; c++) E[c] = w->E[m][c], H[c] = w->H[m][c];
+	*L = w->L;
+	return ALISGPU_OK;
+}

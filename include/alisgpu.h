@@ -1,0 +1,207 @@
+/*
+ * alisgpu.h -- device C-ABI of the GB300 ALiS engine (sm_103a).
+ *
+ * The ALiS public API (alis_c.h) is the drop-in boundary a user program
+ * links against.  Underneath it, the host layer drives the GPU only
+ * through the entry points below: plain C structs, host pointers and
+ * sizes, status codes.  Each entry point names the reference loops it
+ * replaces.  All work is ordered on one CUDA stream per process
+ * (alisgpu_stream); calls return before the GPU finishes unless they
+ * return data to the host.
+ *
+ * Array conventions.  A host "box array" is one contiguous float block
+ * covering an index box [i0,i1] x [j0,j1] x [k0,k1] with k fastest, which
+ * is exactly the data block behind ALiS's float*** arrays
+ * (&F[i0][j0][k0]).  On the device every field of a world is stored with
+ * a one-cell halo and a row pitch padded to 32 floats, so that the first
+ * interior cell of each row is 128-byte aligned.
+ *
+ * Status: ALISGPU_OK (0) or a negative ALISGPU_E* code;
+ * alisgpu_last_error() returns a message for the last failure.
+ */
+#ifndef ALISGPU_H
+#define ALISGPU_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+	ALISGPU_OK = 0,
+	ALISGPU_EINVAL = -1,    /* bad argument */
+	ALISGPU_ENOMEM = -2,    /* device allocation failed */
+	ALISGPU_ECUDA = -3,     /* CUDA runtime error */
+	ALISGPU_ENODEV = -4,    /* no usable GPU */
+	ALISGPU_ERANGE = -5     /* request beyond a fixed capacity */
+};
+
+const char *alisgpu_last_error(void);
+/* Initialise the device (first call selects GPU 0 or $ALISGPU_DEVICE). */
+int alisgpu_init(void);
+/* Wait for all queued work. */
+int alisgpu_synchronize(void);
+/* The CUDA stream (cudaStream_t) every kernel of the engine runs on. */
+void *alisgpu_stream(void);
+/* Kernel launches issued so far by this library (for launch accounting). */
+unsigned long long alisgpu_launch_count(void);
+
+/* ---- worlds (reference src/world.c:164-280) ---- */
+
+typedef struct alisgpu_geometry {
+	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;   /* grid including CPML cells */
+	int iMin, iMax, jMin, jMax, kMin, kMax;   /* physical domain */
+	int complexField;                          /* 1: second (imaginary) field set */
+	int pml[6];                                /* CPML on xMin,yMin,zMin,xMax,yMax,zMax */
+} alisgpu_geometry;
+
+typedef struct alisgpu_world alisgpu_world;
+
+/* Allocate zeroed E, H and CPML psi storage. */
+int alisgpu_world_create(const alisgpu_geometry *g, alisgpu_world **w);
+int alisgpu_world_destroy(alisgpu_world *w);
+/* Zero fields, psi and ADE currents (reference src/world.c:334-380). */
+int alisgpu_world_reset(alisgpu_world *w);
+/* Device bytes held by the world (fields, psi, maps, currents). */
+size_t alisgpu_world_bytes(const alisgpu_world *w);
+
+/* 1-D tables of the E (grid 0) or H (grid 1) lattice: dtd[3] = dt/dx,
+ * dt/dy, dt/dz indexed from iMIN/jMIN/kMIN; cpml[9] = xP, xPy, xPz, yP,
+ * yPz, yPx, zP, zPx, zPy (NULL where an axis has no CPML)
+ * (reference src/world.c:98-161). */
+int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *const dtd[3], const float *const cpml[9]);
+
+/* Inverse-permittivity maps of the E lattice as host box arrays over
+ * [iMIN,iMAX+1]x[jMIN,jMAX]x[kMIN,kMAX], [iMIN,iMAX]x[jMIN,jMAX+1]x..,
+ * [..]x[kMIN,kMAX+1]; all NULL removes them (vacuum branch)
+ * (reference src/object.c:168-175, 374-399). */
+int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *cy, const float *cz);
+
+/* One dispersive object: fill maps and ADE recursion coefficients
+ * (reference src/object.c:178-226, 290-336). */
+typedef struct alisgpu_dispersive {
+	int iMin, iMax, jMin, jMax, kMin, kMax;    /* box of maps and currents */
+	int NJ, NK;                                /* Drude-type poles, all poles */
+	const float *fill[3];                      /* host box arrays (x, y, z) */
+	float a[3];                                /* conductivity factors ax, ay, az */
+	const float *JJ[3], *JK[3], *JE[3];        /* [NK] per axis */
+	const float *KJ[3], *KK[3], *KE[3];        /* [NK] per axis, entries >= NJ used */
+} alisgpu_dispersive;
+
+/* Replace the dispersive objects of a world (n may be 0). */
+int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *objs);
+
+/* Copy one field component between device and a host box array over the
+ * halo'd grid [iMIN-1,iMAX+1]x[jMIN-1,jMAX+1]x[kMIN-1,kMAX+1].
+ * field 0 = E, 1 = H; m = 0 real / 1 imaginary set; comp 0..2. */
+int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host);
+int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host);
+/* ADE current J (isK 0) or K (isK 1) of object n, pole p, axis comp,
+ * set m, as a host box array over the object's box. */
+int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host);
+
+/* ---- half steps (reference src/update.c:87-341) ---- */
+
+/* TFSF box of a world and its auxiliary incident-field world
+ * (reference src/source.c:269-334, src/update.c:205-272).  Aux field
+ * rows are aliased as in the reference: i > auxIMAX reads row
+ * auxIMAX+Alt of the component, same for j. */
+typedef struct alisgpu_tfsf {
+	alisgpu_world *aux;
+	int iMin, iMax, jMin, jMax, kMin, kMax;
+	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
+	int auxIMAX, auxJMAX;
+	int aliasX, aliasY;                         /* aux rows aliased along x / y */
+} alisgpu_tfsf;
+
+/* Soft-source increments for this half step, added in list order
+ * (reference src/update.c:161-179): F[field,m,comp] over the box +=
+ * values[voff + cell] (box order, k fastest). */
+typedef struct alisgpu_source_patch {
+	int m, comp;
+	int i0, i1, j0, j1, k0, k1;
+	int voff;
+} alisgpu_source_patch;
+
+/* Ghost-cell copy F = cos F' + sin G', G = cos G' - sin F' from
+ * (i+di, j+dj, k+dk) over a box (reference src/update.c:182-191). */
+typedef struct alisgpu_ghost_copy {
+	int comp;
+	int i0, i1, j0, j1, k0, k1;
+	int di, dj, dk;
+	float cosk, sink;
+} alisgpu_ghost_copy;
+
+typedef struct alisgpu_half_step {
+	int field;                                  /* 0: E half step, 1: H */
+	int ntfsf;
+	const alisgpu_tfsf *tfsf;
+	int nsrc;
+	const alisgpu_source_patch *src;
+	const float *values;                        /* host source increments */
+	int nvalues;
+	int nghost;
+	const alisgpu_ghost_copy *ghost;
+} alisgpu_half_step;
+
+/* One half step of a world: conductivity, ADE subtraction, curl with
+ * eps^-1, CPML psi (and, for H, the ADE current update driven by E),
+ * TFSF face corrections, sources, ghost copies -- bit-identical to the
+ * reference order.  Replaces reference src/update.c:275-341. */
+int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s);
+
+/* ---- phasers (reference src/phaser.c:21-110) ---- */
+
+typedef struct alisgpu_phaser alisgpu_phaser;
+
+/* One face of a phaser box: axis 0/1/2 (x/y/z normal) and its planar
+ * index box; components (E1, E2, H1, H2) are (Ey, Ez, Hy, Hz) for x
+ * faces, (Ez, Ex, Hz, Hx) for y, (Ex, Ey, Hx, Hy) for z. */
+typedef struct alisgpu_face {
+	int axis;
+	int i0, i1, j0, j1, k0, k1;
+} alisgpu_face;
+
+/* Accumulators for nfreq frequencies over nface faces of world w.
+ * ring: time steps buffered on the device between DFT flushes.
+ * kahan: 1 adds compensated summation (not bit-identical to the
+ * reference's plain float sums; more accurate). */
+int alisgpu_phaser_create(alisgpu_world *w, int nfreq, int nface, const alisgpu_face *faces, int ring, int kahan, alisgpu_phaser **p);
+int alisgpu_phaser_destroy(alisgpu_phaser *p);
+/* Record the face fields of the current time step with its phase
+ * factors exp(2 pi i f t_E) and exp(2 pi i f t_H) (interleaved re, im;
+ * [nfreq] each).  Flushes automatically when the ring is full. */
+int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, const float *phaseH);
+/* Accumulate every buffered step into the DFT sums. */
+int alisgpu_phaser_flush(alisgpu_phaser *p);
+/* Copy accumulator (frequency f, face, component q = E1,E2,H1,H2) as
+ * interleaved complex host box array over the face box. */
+int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q, float *host);
+int alisgpu_phaser_zero(alisgpu_phaser *p);
+
+/* ---- near-to-far-field sums in FP64 (reference src/farfld.c:248-459) ---- */
+
+/* For each direction a: sum over the phaser's faces (sign -1 for min
+ * faces) of the face bilinear forms with test fields T (interleaved
+ * complex, indexed k - kMIN, length nk per component; 6 components
+ * Ex..Hz, missing ones flagged by present[a*6+c] = 0), lateral wave
+ * numbers kx, ky and the world line tables.  See alisgpu_farfield_geom. */
+typedef struct alisgpu_farfield_geom {
+	int iMin, iMax, jMin, jMax, kMin, kMax, kMIN;
+	int faceOn[6];                              /* xMin,xMax,yMin,yMax,zMin,zMax */
+	int sym[3];                                 /* symmetry planes x,y,z */
+	double cosk[3];                             /* coskx, cosky, coskz */
+	const double *xE, *xH, *yE, *yH;            /* coordinates itox(i), itox(i-0.5), ... */
+	const double *dxE, *dxH, *dyE, *dyH, *dzE, *dzH; /* CE/CH spacings */
+	int xLen, yLen, zLen;                       /* table lengths, indexed from iMin, jMin, kMIN */
+} alisgpu_farfield_geom;
+
+int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
+                          const double *T, int nk, const unsigned char *present,
+                          const double *kx, const double *ky, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALISGPU_H */

@@ -1,0 +1,95 @@
+"""Build and run the parity scenes (tests/drivers/scenes.c) against the
+GPU engine, the CPU oracle or the reference library, and compare dumps."""
+import hashlib
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+from alis_dump import read_dump
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRIVER = os.path.join(ROOT, "tests", "drivers", "scenes.c")
+BIN = os.path.join(ROOT, "tests", "drivers", "bin")
+
+# (scene, scale, steps) run by the parity tests; small enough that the
+# oracle finishes each in about a second
+CASES = [
+    ("c1", 1, 80),
+    ("c2", 1, 80),
+    ("dipole", 1, 80),
+    ("bloch", 1, 80),
+    ("sym", 1, 80),
+    ("hbc", 1, 60),
+    ("multi", 1, 80),
+]
+
+
+def binary(against):
+    from alis_gb300 import build
+    out = os.path.join(BIN, "scenes_" + against)
+    if against == "engine":
+        build.build_engine()
+    elif against == "oracle":
+        build.build_oracle()
+    elif against == "reference":
+        if build.build_reference() is None:
+            return None
+    if not os.path.exists(out) or os.path.getmtime(out) < max(
+            os.path.getmtime(DRIVER), os.path.getmtime(os.path.join(ROOT, "tests", "drivers", "dump.h"))):
+        build.link_program(DRIVER, out, against)
+    return out
+
+
+def run(against, scene, scale, steps, env=None):
+    exe = binary(against)
+    if exe is None:
+        return None
+    e = dict(os.environ)
+    if against == "reference":
+        e["OMP_NUM_THREADS"] = "1"   # reductions in the order of a sequential run
+    e.update(env or {})
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "dump.bin")
+        r = subprocess.run([exe, scene, out, str(scale), str(steps)], cwd=d, env=e,
+                            capture_output=True, text=True, timeout=900)
+        if r.returncode:
+            raise RuntimeError("%s %s failed (%d):\n%s%s" % (against, scene, r.returncode, r.stdout[-2000:], r.stderr[-2000:]))
+        return read_dump(out)
+
+
+def digest(arr):
+    return hashlib.sha256(np.ascontiguousarray(arr).tobytes()).hexdigest()
+
+
+def summary(arr):
+    a = arr.astype(np.complex128)
+    return {
+        "shape": list(arr.shape),
+        "dtype": str(arr.dtype),
+        "sha256": digest(arr),
+        "sum": [float(a.sum().real), float(a.sum().imag)],
+        "l1": float(np.abs(a).sum()),
+        "max": float(np.abs(a).max()) if a.size else 0.0,
+    }
+
+
+def compare_exact(a, b):
+    """Names whose bytes differ between two dumps (and missing names)."""
+    bad = sorted(set(a) ^ set(b))
+    for k in set(a) & set(b):
+        if a[k].shape != b[k].shape or a[k].dtype != b[k].dtype or \
+                not np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)):
+            bad.append(k)
+    return sorted(bad)
+
+
+def max_rel(a, b):
+    """Largest |a-b| / max|b| over arrays (a dict of name -> value)."""
+    out = {}
+    for k in set(a) & set(b):
+        x, y = a[k].astype(np.complex128), b[k].astype(np.complex128)
+        scale = np.abs(y).max()
+        out[k] = float(np.abs(x - y).max() / scale) if scale > 0 else float(np.abs(x).max())
+    return out

@@ -1,0 +1,55 @@
+"""GPU engine against the oracle and the golden fixtures.
+
+The engine (CUDA kernels built for sm_103a, reached through the ALiS C
+API) runs every parity scene; the oracle runs the same scene on the
+host cores of the same machine.  Both use the same C library for the
+waveforms and phase factors, so every dumped array must be identical
+byte for byte: fields, CPML-affected cells, ADE currents, TFSF boxes,
+Bloch/HBC/symmetry ghosts, phaser accumulators and fluxes.  Far-field
+values are FP64 sums on the GPU and are compared at 1e-5 relative to
+the oracle's FP64 restatement.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import scenes
+
+GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scenes.json")))
+FAR = ("F.ffP", "F.ffS")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale,steps", scenes.CASES, ids=[c[0] for c in scenes.CASES])
+def test_engine_bit_identical_to_oracle(scene, scale, steps):
+    gpu = scenes.run("engine", scene, scale, steps)
+    cpu = scenes.run("oracle", scene, scale, steps)
+    near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
+    bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith(FAR)})
+    assert not bad, "differs from the oracle: %s" % bad[:10]
+    far = [k for k in gpu if k.startswith(FAR)]
+    if far:
+        wide = scenes.run("oracle", scene, scale, steps, env={"ALIS_ORACLE_FF64": "1"})
+        for k in far:
+            x, y = complex(gpu[k].reshape(-1)[0]), complex(wide[k].reshape(-1)[0])
+            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-30), (k, x, y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale,steps", scenes.CASES[:2], ids=[c[0] for c in scenes.CASES[:2]])
+def test_engine_matches_reference_fixture(scene, scale, steps):
+    gpu = scenes.run("engine", scene, scale, steps)
+    gold = GOLDEN["%s/%d/%d" % (scene, scale, steps)]
+    exact = 0
+    for name, g in gold.items():
+        if name.startswith(FAR):
+            continue
+        s = scenes.summary(gpu[name])
+        if s["sha256"] == g["sha256"]:
+            exact += 1
+            continue
+        scale_ = max(g["l1"], 1e-30)
+        assert abs(s["l1"] - g["l1"]) <= 1e-5 * scale_, (name, s["l1"], g["l1"])
+    assert exact > 0
