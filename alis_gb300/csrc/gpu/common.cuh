@@ -84,10 +84,21 @@ struct HalfStepParams {
 	DevTfsf tf[ALIS_MAXTFSF];
 	float *Fother[3];                     // E of set m during the H step (ADE drive)
 	unsigned int *err;                    // device error word
+	// per-axis classification of cells (indexed from MIN): bits 0-7 object
+	// n's range, bit 8 any object n >= 8, bit 13/14 CPML slab of the min/max
+	// face, bit 15 TFSF face plane
+	const unsigned short *cls[3];
 };
+#define CLS_OBJ8 0x100u
+#define CLS_PML_LO 0x2000u
+#define CLS_PML_HI 0x4000u
+#define CLS_TFSF 0x8000u
 
 // ---- launch bookkeeping ----
 extern "C" void alisgpu__count_launch(void);
+// event pair around a launch when profiling is on: slot = prof_start(); launch; prof_stop(slot, kind)
+extern "C" int alisgpu__prof_start(void);
+extern "C" void alisgpu__prof_stop(int slot, int kind);
 extern "C" cudaStream_t alisgpu__stream(void);
 extern "C" int alisgpu__fail(int code, const char *fmt, ...);
 extern "C" int alisgpu__check(cudaError_t e, const char *what);

@@ -270,7 +270,9 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 	ALIS_CUDA(cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	if (P.nface) {
 		dim3 grid(nA, P.nface);
+		int slot = alisgpu__prof_start();
 		k_farfield<<<grid, FF_THREADS, smem, st>>>(P);
+		alisgpu__prof_stop(slot, ALISGPU_K_FARFIELD);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
 	}

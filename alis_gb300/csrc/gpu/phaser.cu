@@ -72,12 +72,14 @@ __global__ void k_phaser_gather(const GatherParams P)
 	reinterpret_cast<float4 *>(P.out)[t] = v;
 }
 
-// fl(a + p * 0.5) with the rounding of the double expression
+// fl(a + p * 0.5) with the rounding of the reference's double expression
+// (float)((double)a + (double)p * 0.5): p * 0.5 is exact in double and
+// the double sum of two floats rounds innocuously to float, so the result
+// is the exactly rounded a + p/2 -- which is what one fused multiply-add
+// computes, including when p/2 is subnormal.
 __device__ __forceinline__ float addHalf(float a, float p)
 {
-	float h = p * 0.5f;
-	if (h * 2.0f == p) return a + h;
-	return (float)((double)a + (double)p * 0.5);
+	return __fmaf_rn(p, 0.5f, a);
 }
 
 #define FLUSH_THREADS 128
@@ -187,8 +189,10 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 	long long n4 = p->cells * 4;
 	dim3 grid((unsigned)((n4 + FLUSH_THREADS - 1) / FLUSH_THREADS), (p->nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ);
 	size_t smem = (size_t)p->used * FLUSH_FREQ * 2 * sizeof(float2);
+	int slot = alisgpu__prof_start();
 	if (p->kahan) k_phaser_flush<true><<<grid, FLUSH_THREADS, smem, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
 	else k_phaser_flush<false><<<grid, FLUSH_THREADS, smem, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
+	alisgpu__prof_stop(slot, ALISGPU_K_FLUSH);
 	alisgpu__count_launch();
 	ALIS_CUDA(cudaGetLastError());
 	p->used = 0;
@@ -216,7 +220,9 @@ extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, con
 			memcpy(G.box[f], b, sizeof b);
 		}
 		G.out = p->buf + (size_t)p->used * p->cells * 4;
+		int slot = alisgpu__prof_start();
 		k_phaser_gather<<<(unsigned)((p->cells + 255) / 256), 256, 0, alisgpu__stream()>>>(G);
+		alisgpu__prof_stop(slot, ALISGPU_K_GATHER);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
 	}

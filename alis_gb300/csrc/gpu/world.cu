@@ -66,6 +66,57 @@ extern "C" int alisgpu_init(void)
 	return ALISGPU_OK;
 }
 
+// ---- optional per-kernel event timing ----
+struct ProfSlot { cudaEvent_t a, b; int kind; };
+static std::vector<ProfSlot> gProf;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> gProfFree;
+static int gProfOn;
+static double gProfMs[ALISGPU_K_KINDS];
+static unsigned long long gProfN[ALISGPU_K_KINDS];
+
+extern "C" int alisgpu_profile(int enable) { gProfOn = enable; return ALISGPU_OK; }
+
+extern "C" int alisgpu__prof_start(void)
+{
+	if (!gProfOn) return -1;
+	ProfSlot s;
+	if (!gProfFree.empty()) { s.a = gProfFree.back().first; s.b = gProfFree.back().second; gProfFree.pop_back(); }
+	else { cudaEventCreate(&s.a); cudaEventCreate(&s.b); }
+	s.kind = -1;
+	cudaEventRecord(s.a, gStream);
+	gProf.push_back(s);
+	return (int)gProf.size() - 1;
+}
+
+extern "C" void alisgpu__prof_stop(int slot, int kind)
+{
+	if (slot < 0) return;
+	gProf[slot].kind = kind;
+	cudaEventRecord(gProf[slot].b, gStream);
+}
+
+static void profDrain(void)
+{
+	if (gProf.empty()) return;
+	cudaStreamSynchronize(gStream);
+	for (ProfSlot &s : gProf) {
+		float ms = 0;
+		if (s.kind >= 0 && cudaEventElapsedTime(&ms, s.a, s.b) == cudaSuccess) gProfMs[s.kind] += ms, gProfN[s.kind]++;
+		gProfFree.push_back(std::make_pair(s.a, s.b));
+	}
+	gProf.clear();
+}
+
+extern "C" int alisgpu_profile_read(int kind, double *ms, unsigned long long *launches)
+{
+	if (kind < 0 || kind >= ALISGPU_K_KINDS) return alisgpu__fail(ALISGPU_EINVAL, "profile_read: bad kind");
+	profDrain();
+	if (ms) *ms = gProfMs[kind];
+	if (launches) *launches = gProfN[kind];
+	gProfMs[kind] = 0, gProfN[kind] = 0;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu_synchronize(void)
 {
 	if (!gInit) return ALISGPU_OK;
@@ -91,6 +142,8 @@ struct alisgpu_world {
 	DevObj *dObjs;
 	std::vector<void *> objMem;
 	size_t bytes;
+	unsigned short *cls[2][3];             // per-axis cell classes of the E / H step
+	std::vector<unsigned short> clsHost[2][3];
 };
 
 static Layout makeLayout(const alisgpu_geometry *g)
@@ -98,7 +151,9 @@ static Layout makeLayout(const alisgpu_geometry *g)
 	Layout L;
 	L.i0 = g->iMIN - 1, L.j0 = g->jMIN - 1, L.k0 = g->kMIN - 1;
 	L.ni = g->iMAX - g->iMIN + 3, L.nj = g->jMAX - g->jMIN + 3, L.nk = g->kMAX - g->kMIN + 3;
-	L.sj = ((ALIS_KOFF + L.nk + 31) / 32) * 32;
+	// row pitch: padding keeps the last float4 of a row and its k+1
+	// neighbour inside the row
+	L.sj = ((ALIS_KOFF + L.nk + 4 + 31) / 32) * 32;
 	L.si = L.sj * L.nj;
 	return L;
 }
@@ -180,6 +235,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 			if (w->psi[grid][m][f][q].p) cudaFree(w->psi[grid][m][f][q].p);
 	}
 	freeObjects(w);
+	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) cudaFree(w->cls[f][a]);
 	delete w;
 	return ALISGPU_OK;
 }
@@ -359,8 +415,6 @@ extern "C" int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, i
 // ---------------------------------------------------------------------
 // the fused half-step kernel
 // ---------------------------------------------------------------------
-#define TX 32
-#define TY 8
 
 // aux-world index of a main-world cell, with the row aliasing of the
 // reference's expandFieldX/Y (src/source.c:223-249)
@@ -382,131 +436,109 @@ __device__ __forceinline__ float auxGet(const float *A, long long q, unsigned in
 	return A[q];
 }
 
-// Alt = +1: E half step (neighbours at +1, ALT=1); Alt = -1: H half step.
-template <int ALT>
-__global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
+// Pieces of the per-cell half step, in the reference order.  ALT = +1: E
+// half step (neighbours at +1); ALT = -1: H half step (neighbours at -1).
+// g*0 are the other field at the cell, gyk/gxk its k neighbours, gzj/gxj
+// its j neighbours, gzi/gyi its i neighbours.
+
+// objects whose box holds the cell, in list order: the tile's list when the
+// world has more than 8 objects, else every object whose class bit is set
+#define FOR_CELL_OBJECTS(...)                                                               \
+	for (int q_ = 0; q_ < nIter; q_++) {                                                    \
+		const int n_ = list ? list[q_] : q_;                                                \
+		if (!list && n_ < 8 && !((objm >> n_) & 1u)) continue;                              \
+		const DevObj &o = P.obj[n_];                                                        \
+		if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) ||       \
+		    k < o.k0 || k > min(o.k1, P.kMAX)) continue;                                    \
+		const int b = (i - o.i0) * (int)o.si + (j - o.j0) * (int)o.sj + (k - o.k0);         \
+		__VA_ARGS__                                                                         \
+	}
+
+// conductivity factors, then polarisation currents (reference
+// src/update.c:89-108); E half step only -- H is updated with CH, whose
+// object list is always empty
+__device__ __forceinline__ void objectsBeforeCurl(const HalfStepParams &P, int i, int j, int k,
+	float &fx, float &fy, float &fz, unsigned objm, const int *list, int nIter)
 {
-	__shared__ int list[ALIS_TILE_OBJ];
-	__shared__ int nlist;
-	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
-	const int j = P.jMIN + blockIdx.y * TY + threadIdx.y;
-	const int i = P.iMIN + blockIdx.z;
-
-	// objects whose box meets this tile, in list order (one warp builds it)
-	if (P.nobj) {
-		if (threadIdx.y == 0) {
-			int tj0 = P.jMIN + blockIdx.y * TY, tj1 = min(tj0 + TY - 1, P.jMAX);
-			int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
-			int cnt = 0;
-			for (int base = 0; base < P.nobj; base += 32) {
-				int n = base + threadIdx.x;
-				bool hit = false;
-				if (n < P.nobj) {
-					const DevObj &o = P.obj[n];
-					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
-				}
-				unsigned bal = __ballot_sync(0xffffffffu, hit);
-				if (hit) {
-					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
-					if (pos < ALIS_TILE_OBJ) list[pos] = n;
-				}
-				cnt += __popc(bal);
-			}
-			if (threadIdx.x == 0) nlist = cnt;
-		}
-		__syncthreads();
-	}
-	if (k > P.kMAX || j > P.jMAX) return;
-
-	const long long c = P.L.at(i, j, k);
-	const long long si = P.L.si, sj = P.L.sj;
-	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
-	const int nl = P.nobj ? nlist : 0;
-	const bool overflow = nl > ALIS_TILE_OBJ;
-	const int nIter = overflow ? P.nobj : nl;
-
-	// conductivity factors (reference src/update.c:89-98).  Only the E
-	// coefficient set holds objects; H is updated with CH, whose object
-	// list is always empty, so both loops are skipped in the H step.
-	for (int q = 0; q < (ALT == 1 ? nIter : 0); q++) {
-		const DevObj &o = P.obj[overflow ? q : list[q]];
-		if (!o.cond) continue;
-		if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
-		long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
-		float gx = o.fill[0][b], gy = o.fill[1][b], gz = o.fill[2][b];
-		fx *= (1 - o.a[0] * gx) / (1 + o.a[0] * gx);
-		fy *= (1 - o.a[1] * gy) / (1 + o.a[1] * gy);
-		fz *= (1 - o.a[2] * gz) / (1 + o.a[2] * gz);
-	}
-	// polarisation currents (reference src/update.c:99-108)
-	for (int q = 0; q < (ALT == 1 ? nIter : 0); q++) {
-		const DevObj &o = P.obj[overflow ? q : list[q]];
-		if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
-		long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
+	FOR_CELL_OBJECTS(
+		if (o.cond) {
+			float ux = o.fill[0][b], uy = o.fill[1][b], uz = o.fill[2][b];
+			fx *= (1 - o.a[0] * ux) / (1 + o.a[0] * ux);
+			fy *= (1 - o.a[1] * uy) / (1 + o.a[1] * uy);
+			fz *= (1 - o.a[2] * uz) / (1 + o.a[2] * uz);
+		})
+	FOR_CELL_OBJECTS(
 		for (int p = 0; p < o.NK; p++) {
 			fx -= o.J[P.m][p][0][b];
 			fy -= o.J[P.m][p][1][b];
 			fz -= o.J[P.m][p][2][b];
-		}
-	}
+		})
+}
 
-	// curl (reference src/update.c:109-118)
-	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
-	const float gx0 = Gx[c], gy0 = Gy[c], gz0 = Gz[c];
-	const float dx = P.dtd[0][i - P.iMIN], dy = P.dtd[1][j - P.jMIN], dz = P.dtd[2][k - P.kMIN];
-	const float gyk = Gy[c + ALT], gzj = Gz[c + ALT * sj], gzi = Gz[c + ALT * si];
-	const float gxk = Gx[c + ALT], gxj = Gx[c + ALT * sj], gyi = Gy[c + ALT * si];
-	const bool hasC = P.C[0] != 0;
-	float cx = 1, cy = 1, cz = 1;
-	if (hasC) {
-		cx = P.C[0][c], cy = P.C[1][c], cz = P.C[2][c];
-		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
-		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
-		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
-	} else {
-		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
-		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
-		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
-	}
-
-	// CPML (reference src/update.c:48-84, 119-124), faces in reference order
+// ADE currents driven by E, run inside updateH (reference src/update.c:128-158)
+__device__ __forceinline__ void objectsAfterCurl(const HalfStepParams &P, int i, int j, int k,
+	float gx0, float gy0, float gz0, unsigned objm, const int *list, int nIter)
+{
+	FOR_CELL_OBJECTS(
+		const float e[3] = { gx0, gy0, gz0 };
 #pragma unroll
-	for (int f = 0; f < 6; f++) {
-		if (!P.slabOn[f]) continue;
-		const int ax = f % 3;
-		const int pos = ax == 0 ? i : ax == 1 ? j : k;
-		if (pos < P.slabLo[f] || pos > P.slabHi[f]) continue;
-		const BoxArr &A = P.psi[f][0], &B = P.psi[f][1];
-		const long long a = A.at(i, j, k);
-		if (ax == 0) {
-			const int q = i - P.iMIN;
-			float py = P.cp[0][q] * A.p[a] + P.cp[1][q] * (gz0 - gzi);
-			float pz = P.cp[0][q] * B.p[a] + P.cp[2][q] * (gy0 - gyi);
-			A.p[a] = py, B.p[a] = pz;
-			if (hasC) fy += py * cy, fz += pz * cz; else fy += py, fz += pz;
-		} else if (ax == 1) {
-			const int q = j - P.jMIN;
-			float pz = P.cp[3][q] * A.p[a] + P.cp[4][q] * (gx0 - gxj);
-			float px = P.cp[3][q] * B.p[a] + P.cp[5][q] * (gz0 - gzj);
-			A.p[a] = pz, B.p[a] = px;
-			if (hasC) fz += pz * cz, fx += px * cx; else fz += pz, fx += px;
-		} else {
-			const int q = k - P.kMIN;
-			float px = P.cp[6][q] * A.p[a] + P.cp[7][q] * (gy0 - gyk);
-			float py = P.cp[6][q] * B.p[a] + P.cp[8][q] * (gx0 - gxk);
-			A.p[a] = px, B.p[a] = py;
-			if (hasC) fx += px * cx, fy += py * cy; else fx += px, fy += py;
-		}
-	}
+		for (int a = 0; a < 3; a++) {
+			const float fe = o.fill[a][b];
+			for (int p = 0; p < o.NJ; p++) {
+				float *J = o.J[P.m][p][a];
+				J[b] = o.JJ[p][a] * J[b] + o.JE[p][a] * fe * e[a];
+			}
+			for (int p = o.NJ; p < o.NK; p++) {
+				float *J = o.J[P.m][p][a], *K = o.K[P.m][p][a];
+				float jn = o.JJ[p][a] * J[b] + o.JK[p][a] * K[b] + o.JE[p][a] * fe * e[a];
+				J[b] = jn;
+				K[b] = o.KJ[p][a] * jn + o.KK[p][a] * K[b] + o.KE[p][a] * fe * e[a];
+			}
+		})
+}
 
-	// TFSF incident-field corrections (reference src/update.c:205-272).
-	// E step: aux H; H step: aux E.  Face-by-face in the reference order;
-	// (dtds * G) * C rounds like the reference's `dtds * G[..] * C[..]`.
+// CPML of face F (xMin,yMin,zMin,xMax,yMax,zMax), reference src/update.c:48-84, 119-124
+template <int F>
+__device__ __forceinline__ void pmlFace(const HalfStepParams &P, int i, int j, int k,
+	float &fx, float &fy, float &fz, float gx0, float gy0, float gz0,
+	float gyk, float gxk, float gzj, float gxj, float gzi, float gyi,
+	bool hasC, float cx, float cy, float cz)
+{
+	const BoxArr &A = P.psi[F][0], &B = P.psi[F][1];
+	const int a = (i - A.i0) * (int)A.si + (j - A.j0) * (int)A.sj + (k - A.k0);
+	if (F % 3 == 0) {
+		const int q = i - P.iMIN;
+		float py = P.cp[0][q] * A.p[a] + P.cp[1][q] * (gz0 - gzi);
+		float pz = P.cp[0][q] * B.p[a] + P.cp[2][q] * (gy0 - gyi);
+		A.p[a] = py, B.p[a] = pz;
+		if (hasC) fy += py * cy, fz += pz * cz; else fy += py, fz += pz;
+	} else if (F % 3 == 1) {
+		const int q = j - P.jMIN;
+		float pz = P.cp[3][q] * A.p[a] + P.cp[4][q] * (gx0 - gxj);
+		float px = P.cp[3][q] * B.p[a] + P.cp[5][q] * (gz0 - gzj);
+		A.p[a] = pz, B.p[a] = px;
+		if (hasC) fz += pz * cz, fx += px * cx; else fz += pz, fx += px;
+	} else {
+		const int q = k - P.kMIN;
+		float px = P.cp[6][q] * A.p[a] + P.cp[7][q] * (gy0 - gyk);
+		float py = P.cp[6][q] * B.p[a] + P.cp[8][q] * (gx0 - gxk);
+		A.p[a] = px, B.p[a] = py;
+		if (hasC) fx += px * cx, fy += py * cy; else fx += px, fy += py;
+	}
+}
+
+// TFSF incident-field corrections (reference src/update.c:205-272).
+// E step: aux H; H step: aux E.  Face-by-face in the reference order;
+// (dtds * G) * C rounds like the reference's `dtds * G[..] * C[..]`.
+template <int ALT>
+__device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, int k,
+	float &fx, float &fy, float &fz, bool hasC, float cx, float cy, float cz)
+{
 	for (int s = 0; s < P.ntfsf; s++) {
 		const DevTfsf &T = P.tf[s];
 		const float *A0 = T.G[P.m][0], *A1 = T.G[P.m][1], *A2 = T.G[P.m][2];
 		if (ALT == 1) {
-			// E half step; alias Alt of H components: X (0,1,1), Y (1,0,1)
+			// alias Alt of the aux H components: x rows (0,1,1), y rows (1,0,1)
 			if (T.iMin > P.iMIN && i == T.iMin) {
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) { float v = -T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 1, 0), P.err); fz += hasC ? v * cz : v; }
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) { float v = T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 1, 1), P.err); fy += hasC ? v * cy : v; }
@@ -532,7 +564,7 @@ __global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
 				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) { float v = -T.dtdMax[2] * auxGet(A1, auxAt(T, i, j, k + 1, 1, 0), P.err); fx += hasC ? v * cx : v; }
 			}
 		} else {
-			// H half step; alias Alt of E components: X (1,0,0), Y (0,1,0)
+			// alias Alt of the aux E components: x rows (1,0,0), y rows (0,1,0)
 			if (T.iMin > P.iMIN && i == T.iMin) {
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) fz += T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 0, 1), P.err);
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) fy += -T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 0, 0), P.err);
@@ -559,32 +591,99 @@ __global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
 			}
 		}
 	}
+}
 
-	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
-
-	// ADE currents driven by E, run inside updateH (reference src/update.c:128-158)
-	if (ALT == -1) {
-		for (int q = 0; q < nIter; q++) {
-			const DevObj &o = P.obj[overflow ? q : list[q]];
-			if (i < o.i0 || i > min(o.i1, P.iMAX) || j < o.j0 || j > min(o.j1, P.jMAX) || k < o.k0 || k > min(o.k1, P.kMAX)) continue;
-			long long b = (long long)(i - o.i0) * o.si + (long long)(j - o.j0) * o.sj + (k - o.k0);
-			const float e[3] = { gx0, gy0, gz0 };
-#pragma unroll
-			for (int a = 0; a < 3; a++) {
-				const float fe = o.fill[a][b];
-				for (int p = 0; p < o.NJ; p++) {
-					float *J = o.J[P.m][p][a];
-					J[b] = o.JJ[p][a] * J[b] + o.JE[p][a] * fe * e[a];
+// Fused half step, one thread per cell, one i plane per block of TX x TY
+// threads.  Three per-axis bit tables classify every cell by its i, j and
+// k: CPML slab side, TFSF face plane, dispersive object range.  Every cell
+// takes the curl; only the cells whose bits ask for it run the CPML face
+// updates, the TFSF corrections and the ADE loops, each in the reference
+// order.  Index arithmetic is 32-bit (at most 2^31 elements per array,
+// checked on the host).  Worlds with more than 8 objects add a per-block
+// list of the objects that meet the tile.
+#define TX 32
+#define TY 8
+template <int ALT>
+__global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
+{
+	__shared__ int tileList[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
+	const int j = P.jMIN + blockIdx.y * TY + threadIdx.y;
+	const int i = P.iMIN + blockIdx.z;
+	const bool manyObj = P.nobj > 8;
+	if (manyObj) {
+		// objects whose box meets this tile, in list order (one warp)
+		if (threadIdx.y == 0) {
+			const int tj0 = P.jMIN + blockIdx.y * TY, tj1 = min(tj0 + TY - 1, P.jMAX);
+			const int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
+			int cnt = 0;
+			for (int base = 0; base < P.nobj; base += 32) {
+				int n = base + threadIdx.x;
+				bool hit = false;
+				if (n < P.nobj) {
+					const DevObj &o = P.obj[n];
+					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
 				}
-				for (int p = o.NJ; p < o.NK; p++) {
-					float *J = o.J[P.m][p][a], *K = o.K[P.m][p][a];
-					float jn = o.JJ[p][a] * J[b] + o.JK[p][a] * K[b] + o.JE[p][a] * fe * e[a];
-					J[b] = jn;
-					K[b] = o.KJ[p][a] * jn + o.KK[p][a] * K[b] + o.KE[p][a] * fe * e[a];
+				unsigned bal = __ballot_sync(0xffffffffu, hit);
+				if (hit) {
+					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
+					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
 				}
+				cnt += __popc(bal);
 			}
+			if (threadIdx.x == 0) nlist = cnt;
 		}
+		__syncthreads();
 	}
+	if (k > P.kMAX || j > P.jMAX) return;
+
+	const int sj = (int)P.L.sj, si = (int)P.L.si;
+	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
+	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
+	const unsigned any = bi | bj | bk;
+	const unsigned objm = bi & bj & bk & 0x1FFu;
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
+	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
+	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
+	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
+	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const bool hasC = P.C[0] != 0;
+	float cx = 1, cy = 1, cz = 1;
+	if (hasC) cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
+
+	// object loops: the tile's list, or all objects filtered by class bits
+	const int *list = 0;
+	int nIter = P.nobj;
+	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
+	if (ALT == 1 && objm) objectsBeforeCurl(P, i, j, k, fx, fy, fz, objm, list, nIter);
+
+	// curl (reference src/update.c:109-118)
+	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
+	if (hasC) {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
+	} else {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
+	}
+	// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
+	if (any & (CLS_PML_LO | CLS_PML_HI)) {
+#define PML_ARGS P, i, j, k, fx, fy, fz, gx0, gy0, gz0, gyk, gxk, gzj, gxj, gzi, gyi, hasC, cx, cy, cz
+		if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
+		if (bj & CLS_PML_LO) pmlFace<1>(PML_ARGS);
+		if (bk & CLS_PML_LO) pmlFace<2>(PML_ARGS);
+		if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
+		if (bj & CLS_PML_HI) pmlFace<4>(PML_ARGS);
+		if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
+#undef PML_ARGS
+	}
+	if (any & CLS_TFSF) tfsfCell<ALT>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
+	if (ALT == -1 && objm) objectsAfterCurl(P, i, j, k, gx0, gy0, gz0, objm, list, nIter);
+	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -743,8 +842,43 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	for (int q = 0; q < s->ntfsf; q++) P.tf[q] = tfsfFor(w, s->tfsf[q], field);
 	P.err = gErrWord;
 
+	// per-axis classification: CPML slabs, TFSF planes, object ranges
+	{
+		int n[3] = { g.iMAX - g.iMIN + 1, g.jMAX - g.jMIN + 1, g.kMAX - g.kMIN + 1 };
+		int lo0[3] = { g.iMIN, g.jMIN, g.kMIN }, hi0[3] = { g.iMAX, g.jMAX, g.kMAX };
+		std::vector<unsigned short> t[3];
+		for (int a = 0; a < 3; a++) t[a].assign(n[a], 0);
+		auto mark = [&](int a, int lo, int hi, unsigned short bit) {
+			for (int q = max(lo, lo0[a]); q <= min(hi, hi0[a]); q++) t[a][q - lo0[a]] |= bit;
+		};
+		for (int f = 0; f < 6; f++) if (P.slabOn[f]) mark(f % 3, P.slabLo[f], P.slabHi[f], f < 3 ? CLS_PML_LO : CLS_PML_HI);
+		for (int q = 0; q < P.ntfsf; q++) {
+			const DevTfsf &T = P.tf[q];
+			int mn[3] = { T.iMin, T.jMin, T.kMin }, mx[3] = { T.iMax, T.jMax, T.kMax };
+			for (int a = 0; a < 3; a++) {
+				if (mn[a] > lo0[a]) mark(a, mn[a], mn[a], CLS_TFSF);
+				if (mx[a] < hi0[a]) mark(a, mx[a] + field, mx[a] + field, CLS_TFSF);
+			}
+		}
+		for (size_t q = 0; q < w->objs.size(); q++) {
+			const DevObj &o = w->objs[q];
+			unsigned short bit = q < 8 ? (unsigned short)(1u << q) : (unsigned short)CLS_OBJ8;
+			mark(0, o.i0, o.i1, bit), mark(1, o.j0, o.j1, bit), mark(2, o.k0, o.k1, bit);
+		}
+		for (int a = 0; a < 3; a++) {
+			if (!w->cls[field][a]) ALIS_CUDA(cudaMalloc(&w->cls[field][a], n[a] * sizeof(unsigned short)));
+			if (w->clsHost[field][a] != t[a]) {
+				w->clsHost[field][a] = t[a];
+				ALIS_CUDA(cudaMemcpyAsync(w->cls[field][a], w->clsHost[field][a].data(), n[a] * sizeof(unsigned short), cudaMemcpyHostToDevice, gStream));
+			}
+			P.cls[a] = w->cls[field][a];
+		}
+	}
+	if (w->L.elems() >= (1ull << 31))
+		return alisgpu__fail(ALISGPU_ERANGE, "half_step: %zu elements per field exceed 32-bit indexing", w->L.elems());
+	const int ni = g.iMAX - g.iMIN + 1;
 	dim3 block(TX, TY, 1);
-	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + TY) / TY, g.iMAX - g.iMIN + 1);
+	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + TY) / TY, ni);
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -754,8 +888,11 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			P.Fother[c] = w->E[m][c];
 		}
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
+		int slot = alisgpu__prof_start();
 		if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
 		else k_half_step<-1><<<grid, block, 0, gStream>>>(P);
+		long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
+		alisgpu__prof_stop(slot, cells < 65536 ? ALISGPU_K_STEP_AUX : field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 	}
 	ALIS_CUDA(cudaGetLastError());
@@ -789,7 +926,9 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			ALIS_CUDA(cudaStreamSynchronize(gStream));
 			SP.vdev = vbuf;
 		}
+		int slot = alisgpu__prof_start();
 		k_sources<<<1, 256, 0, gStream>>>(SP);
+		alisgpu__prof_stop(slot, ALISGPU_K_SOURCE);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
 	}
@@ -819,7 +958,9 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		}
 		long long total = GP.start[GP.n];
 		if (total > 0) {
+			int slot = alisgpu__prof_start();
 			k_ghost<<<(unsigned)((total + 255) / 256), 256, 0, gStream>>>(GP);
+			alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
 			alisgpu__count_launch();
 			ALIS_CUDA(cudaGetLastError());
 		}

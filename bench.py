@@ -1,0 +1,303 @@
+"""Benchmark of the GB300 ALiS engine on the dispersive-scatterer workload.
+
+One step = updateE + updateH + updatePhaser of the 256^3-cell world of
+alis_gb300/bench/c2.c (gold block with Drude + 2 critical-point poles,
+TFSF plane wave, CPML on all faces, 64-frequency box phasers), driven
+through the public ALiS C API exactly as a user program does.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+value     cells x steps / device time of K steps (CUDA events on the
+          engine stream; fields resident in HBM; the 1.5 GB per step of
+          field traffic exceeds the 129 MB L2, so no L2 flush is needed)
+e2e       the same through the public API timed on the host: K steps plus
+          the read-back of the phaser accumulators and the flux result
+roofline  the fused half-step kernel: algorithmic bytes per step (84 B per
+          cell, +32 B per CPML slab, ADE terms) over the mean E + H launch
+          time, against the measured HBM copy bandwidth
+cpu_baseline  the oracle restatement of the reference loops on the host
+          cores (OpenMP), bounded sample of the same world
+--impl reference  times that CPU implementation alone as the reference arm.
+
+Multi-GPU: replicas only (each rank runs its own world on its own GPU);
+value is the sum of all ranks' cell updates over the slowest rank's time.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HALF = 230          # domain half size in nm: 256^3 cells with the CPML
+NFREQ = 64
+WORKLOAD = "dispersive scatterer 256^3 (gold Drude+2CP, TFSF, CPML 12, 64-f box phasers)"
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def build_bench_lib():
+    from alis_gb300 import build
+    so = build.build_engine()
+    src = os.path.join(ROOT, "alis_gb300", "bench", "c2.c")
+    out = os.path.join(ROOT, "alis_gb300", "lib", "libalis_c2bench.so")
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(src), os.path.getmtime(so)):
+        cuda = build._cuda_home()
+        build._run(["gcc", "-std=gnu99", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-w",
+                    "-I" + os.path.join(ROOT, "include"), src, "-o", out,
+                    "-L" + os.path.dirname(so), "-lalis_gb300", "-Wl,-rpath," + os.path.dirname(so),
+                    "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-lm"])
+    return out
+
+
+def build_cpu_baseline():
+    from alis_gb300 import build
+    build.build_oracle()
+    out = os.path.join(ROOT, "oracle", "build", "c2_cpu")
+    src = os.path.join(ROOT, "oracle", "c2_cpu.c")
+    deps = [src, os.path.join(ROOT, "alis_gb300", "bench", "c2.c"), os.path.join(ROOT, "oracle", "build", "liboracle_alis.a")]
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps):
+        build._run(["gcc", "-std=gnu99", "-O3", "-fopenmp", "-ffp-contract=off", "-w",
+                    "-I" + os.path.join(ROOT, "include"), src, "-o", out,
+                    os.path.join(ROOT, "oracle", "build", "liboracle_alis.a"), "-lm"])
+    return out
+
+
+def run_cpu(half, steps, warmup):
+    exe = build_cpu_baseline()
+    env = dict(os.environ)
+    env.setdefault("OMP_PROC_BIND", "close")
+    cores = os.cpu_count() or 1
+    env.setdefault("OMP_NUM_THREADS", str(cores))
+    r = subprocess.run([exe, str(half), str(steps), str(warmup)], capture_output=True, text=True, env=env, timeout=1800)
+    if r.returncode:
+        raise RuntimeError("CPU baseline failed: %s" % r.stderr[-2000:])
+    line = [l for l in r.stdout.splitlines() if l.startswith("{")][-1]
+    return json.loads(line)
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons while running."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[q] for r in self.rows for q in range(4) if r[3 + q].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes per half-step launch from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_half_step_c2.txt")
+    try:
+        for line in open(p):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+def reduce_max(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    # bounded sample: at most 32 timed and 3 warm-up steps of the full world
+    cpu = run_cpu(HALF, min(max(args.steps, 1), 32), min(args.warmup, 3))
+    rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
+    sample = "%d timed steps (after %d warm-up) of the full %d^3-cell world" % (cpu["steps"], min(args.warmup, 3), round(cpu["cells"] ** (1 / 3)))
+    line = {
+        "impl": "reference", "metric": "Gcell-updates/s", "value": rate, "unit": "Gcell/s", "n_gpus": args.gpus,
+        "steps": cpu["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * cpu["seconds"] / cpu["steps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": cpu["cells"], "parallelism": "host cores (OpenMP)"},
+        "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def engine_arm(args, rank, world, local):
+    os.environ.setdefault("ALISGPU_DEVICE", str(local))
+    so = build_bench_lib()
+    import alis_gb300
+    eng = alis_gb300.library()
+    lib = ctypes.CDLL(so)
+    lib.c2_build.restype = ctypes.c_long
+    lib.c2_result.restype = ctypes.c_double
+    lib.c2_step_bytes.restype = ctypes.c_double
+    lib.c2_step_h2d_bytes.restype = ctypes.c_double
+    lib.c2_result_d2h_bytes.restype = ctypes.c_double
+    eng.alisgpu_stream.restype = ctypes.c_void_p
+    eng.alisgpu_launch_count.restype = ctypes.c_ulonglong
+    cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
+
+    cells = lib.c2_build(HALF, NFREQ)
+    stream = ctypes.c_void_p(eng.alisgpu_stream())
+    ev0, ev1 = ctypes.c_void_p(), ctypes.c_void_p()
+    cudart.cudaEventCreate(ctypes.byref(ev0))
+    cudart.cudaEventCreate(ctypes.byref(ev1))
+    K, W = args.steps, args.warmup
+
+    lib.c2_steps(W)
+    eng.alisgpu_synchronize()
+    with Clocks(local) as clk:
+        # kernel-only throughput: device time of K steps
+        barrier(world)
+        eng.alisgpu_synchronize()
+        l0 = eng.alisgpu_launch_count()
+        cudart.cudaEventRecord(ev0, stream)
+        lib.c2_steps(K)
+        cudart.cudaEventRecord(ev1, stream)
+        cudart.cudaEventSynchronize(ev1)
+        launches = eng.alisgpu_launch_count() - l0
+        ms = ctypes.c_float()
+        cudart.cudaEventElapsedTime(ctypes.byref(ms), ev0, ev1)
+        dev_s = reduce_max(ms.value / 1e3, world)
+        # end to end through the public API, host timed, result read back
+        barrier(world)
+        eng.alisgpu_synchronize()
+        t0 = time.perf_counter()
+        lib.c2_steps(K)
+        flux = lib.c2_result()
+        e2e_s = reduce_max(time.perf_counter() - t0, world)
+        # per-kernel device times for the roofline
+        eng.alisgpu_profile(1)
+        lib.c2_steps(K)
+        kinds = {}
+        for kind, name in enumerate(["step_E", "step_H", "ghost", "source", "gather", "flush", "farfield", "step_aux"]):
+            t, n = ctypes.c_double(), ctypes.c_ulonglong()
+            eng.alisgpu_profile_read(kind, ctypes.byref(t), ctypes.byref(n))
+            kinds[name] = (t.value, n.value)
+        eng.alisgpu_profile(0)
+    clocks = clk.summary()
+    if rank != 0:
+        return
+    step_bytes = lib.c2_step_bytes()
+    tE, nE = kinds["step_E"]
+    tH, nH = kinds["step_H"]
+    pair_ms = tE / max(nE, 1) + tH / max(nH, 1)
+    achieved = step_bytes / (pair_ms / 1e3) / 1e9
+    pk, pk_kind = peaks()
+    peak = pk.get("hbm_gbs", 6800.0)
+    traffic = traffic_per_launch()
+    total_ms = sum(t for t, _ in kinds.values())
+    cpu = run_cpu(HALF, args.cpu_steps, 1)
+    cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
+    value = cells * K * world / dev_s / 1e9
+    line = {
+        "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
+        "ms_per_step": dev_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
+                   "phaser": "64 frequencies, time-blocked ring of %s steps" % os.environ.get("ALISGPU_PHASER_RING", "64")},
+        "e2e": {"value": cells * K * world / e2e_s / 1e9, "unit": "Gcell/s",
+                "h2d_bytes_per_step": lib.c2_step_h2d_bytes(),
+                "d2h_bytes_per_step": lib.c2_result_d2h_bytes() / K},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": pk_kind, "traffic": traffic,
+                     "kernel": "k_half_step (E + H launches, mean per launch pair)",
+                     "algorithmic_bytes_per_step": step_bytes, "launch_pair_ms": pair_ms},
+        "kernel_share": {k: round(t / total_ms, 4) for k, (t, n) in kinds.items() if n},
+        "cpu_baseline": {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
+                         "sample": "%d steps of the full world after 1 warm-up step (oracle restatement, OpenMP)" % cpu["steps"]},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "result_flux": flux,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--warmup", type=int, default=64)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--cpu-steps", type=int, default=4)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = env_rank()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+    else:
+        engine_arm(args, rank, world, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -47,6 +47,24 @@ void *alisgpu_stream(void);
 /* Kernel launches issued so far by this library (for launch accounting). */
 unsigned long long alisgpu_launch_count(void);
 
+/* Per-kernel timing with CUDA events recorded around each launch on the
+ * engine stream (off by default; adds two event records per launch).
+ * alisgpu_profile_read synchronises, returns the summed device time and
+ * launch count of one kernel kind since the last read, and resets it. */
+enum {
+	ALISGPU_K_STEP_E = 0,      /* fused E half step, worlds of >= 65536 cells */
+	ALISGPU_K_STEP_H = 1,      /* fused H half step (with ADE update) */
+	ALISGPU_K_GHOST = 2,       /* boundary ghost copies */
+	ALISGPU_K_SOURCE = 3,      /* soft sources */
+	ALISGPU_K_GATHER = 4,      /* phaser face gather */
+	ALISGPU_K_FLUSH = 5,       /* phaser DFT flush */
+	ALISGPU_K_FARFIELD = 6,    /* FP64 far-field sums */
+	ALISGPU_K_STEP_AUX = 7,    /* half steps of small (TFSF auxiliary) worlds */
+	ALISGPU_K_KINDS = 8
+};
+int alisgpu_profile(int enable);
+int alisgpu_profile_read(int kind, double *ms, unsigned long long *launches);
+
 /* ---- worlds (reference src/world.c:164-280) ---- */
 
 typedef struct alisgpu_geometry {
