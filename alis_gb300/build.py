@@ -63,8 +63,9 @@ def _objdir(name):
     return d
 
 
-def build_engine(force=False, verbose=False):
-    """Compile the CUDA engine into alis_gb300/lib/libalis_gb300.{so,a}."""
+def build_engine(force=False, verbose=False, nvcc_extra=()):
+    """Compile the CUDA engine into alis_gb300/lib/libalis_gb300.{so,a}.
+    nvcc_extra: further nvcc arguments (e.g. -D tuning macros)."""
     cuda = _cuda_home()
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(LIB, exist_ok=True)
@@ -87,7 +88,7 @@ def build_engine(force=False, verbose=False):
             cmd += ["-fmad=false"] if exact else ["-fmad=true"]
             if os.environ.get("ALISGPU_PTXAS_VERBOSE"):
                 cmd += ["-Xptxas", "-v"]
-            jobs.append(cmd)
+            jobs.append(cmd + list(nvcc_extra))
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         for r in ex.map(_run, jobs):
             if verbose and (r.stdout or r.stderr):

@@ -593,51 +593,15 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 	}
 }
 
-// Fused half step, one thread per cell, one i plane per block of TX x TY
-// threads.  Three per-axis bit tables classify every cell by its i, j and
-// k: CPML slab side, TFSF face plane, dispersive object range.  Every cell
-// takes the curl; only the cells whose bits ask for it run the CPML face
-// updates, the TFSF corrections and the ADE loops, each in the reference
-// order.  Index arithmetic is 32-bit (at most 2^31 elements per array,
-// checked on the host).  Worlds with more than 8 objects add a per-block
-// list of the objects that meet the tile.
-#define TX 32
-#define TY 8
+// One cell of a half step, in the reference order: conductivity and -J
+// (E), curl, CPML faces, TFSF corrections, ADE update (H).  Three per-axis
+// bit tables classify the cell by its i, j and k (CPML slab side, TFSF face
+// plane, dispersive object range); a cell with none of these bits takes
+// only the curl.  list/nIter: the objects to visit (a tile's list, or all
+// objects filtered by the class bits when list is null).
 template <int ALT>
-__global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
+__device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, int k, const int *list, int nIter)
 {
-	__shared__ int tileList[ALIS_TILE_OBJ];
-	__shared__ int nlist;
-	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
-	const int j = P.jMIN + blockIdx.y * TY + threadIdx.y;
-	const int i = P.iMIN + blockIdx.z;
-	const bool manyObj = P.nobj > 8;
-	if (manyObj) {
-		// objects whose box meets this tile, in list order (one warp)
-		if (threadIdx.y == 0) {
-			const int tj0 = P.jMIN + blockIdx.y * TY, tj1 = min(tj0 + TY - 1, P.jMAX);
-			const int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
-			int cnt = 0;
-			for (int base = 0; base < P.nobj; base += 32) {
-				int n = base + threadIdx.x;
-				bool hit = false;
-				if (n < P.nobj) {
-					const DevObj &o = P.obj[n];
-					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
-				}
-				unsigned bal = __ballot_sync(0xffffffffu, hit);
-				if (hit) {
-					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
-					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
-				}
-				cnt += __popc(bal);
-			}
-			if (threadIdx.x == 0) nlist = cnt;
-		}
-		__syncthreads();
-	}
-	if (k > P.kMAX || j > P.jMAX) return;
-
 	const int sj = (int)P.L.sj, si = (int)P.L.si;
 	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
 	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
@@ -653,10 +617,6 @@ __global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
 	float cx = 1, cy = 1, cz = 1;
 	if (hasC) cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
 
-	// object loops: the tile's list, or all objects filtered by class bits
-	const int *list = 0;
-	int nIter = P.nobj;
-	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
 	if (ALT == 1 && objm) objectsBeforeCurl(P, i, j, k, fx, fy, fz, objm, list, nIter);
 
 	// curl (reference src/update.c:109-118)
@@ -684,6 +644,57 @@ __global__ void __launch_bounds__(TX * TY) k_half_step(const HalfStepParams P)
 	if (any & CLS_TFSF) tfsfCell<ALT>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
 	if (ALT == -1 && objm) objectsAfterCurl(P, i, j, k, gx0, gy0, gz0, objm, list, nIter);
 	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+}
+
+// Fused half step of a large world, one thread per cell, one i plane per
+// block of TX x TY threads.  Index arithmetic is 32-bit (at most 2^31
+// elements per array, checked on the host).  Worlds with more than 8
+// objects add a per-block list of the objects that meet the tile.
+#define TX 32
+// launch shapes (measured on the 256^3 dispersive world): E 32x8 threads
+// capped at 40 registers (6 blocks per SM); H 32x4 capped at 40 (12 blocks)
+#define STEP_TY(ALT) ((ALT) == 1 ? 8 : 4)
+#define STEP_MINB(ALT) ((ALT) == 1 ? 6 : 12)
+template <int ALT>
+__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const HalfStepParams P)
+{
+	constexpr int TY_ = STEP_TY(ALT);
+	__shared__ int tileList[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
+	const int j = P.jMIN + blockIdx.y * TY_ + threadIdx.y;
+	const int i = P.iMIN + blockIdx.z;
+	const bool manyObj = P.nobj > 8;
+	if (manyObj) {
+		// objects whose box meets this tile, in list order (one warp)
+		if (threadIdx.y == 0) {
+			const int tj0 = P.jMIN + blockIdx.y * TY_, tj1 = min(tj0 + TY_ - 1, P.jMAX);
+			const int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
+			int cnt = 0;
+			for (int base = 0; base < P.nobj; base += 32) {
+				int n = base + threadIdx.x;
+				bool hit = false;
+				if (n < P.nobj) {
+					const DevObj &o = P.obj[n];
+					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
+				}
+				unsigned bal = __ballot_sync(0xffffffffu, hit);
+				if (hit) {
+					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
+					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
+				}
+				cnt += __popc(bal);
+			}
+			if (threadIdx.x == 0) nlist = cnt;
+		}
+		__syncthreads();
+	}
+	if (k > P.kMAX || j > P.jMAX) return;
+	// object loops: the tile's list, or all objects filtered by class bits
+	const int *list = 0;
+	int nIter = P.nobj;
+	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
+	stepCell<ALT>(P, i, j, k, list, nIter);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -759,6 +770,78 @@ __global__ void k_ghost(const GhostParams P)
 		G[d] = g.cosk * gg - g.sink * f;
 	} else {
 		F[d] = g.cosk * F[s];
+	}
+}
+
+// Small worlds (the TFSF auxiliary columns, tiny test worlds): the whole
+// half step -- every cell of every m, then the source patches in list
+// order, then the ghost copies one after another -- in one block, with a
+// barrier between the dependent phases.  Same per-cell code as the large
+// path; one launch instead of one per phase and ghost group.
+#define ALIS_SMALL_CELLS 65536
+#define ALIS_SMALL_GHOSTS 48
+struct SmallStepParams {
+	HalfStepParams P[2];                      // per m
+	int nm;                                   // 1 + complexField
+	int nsrc, nghost;
+	float *F[2][3];                           // the stepped field per m (m clamped)
+	alisgpu_source_patch src[ALIS_MAXSRC];
+	alisgpu_ghost_copy ghost[ALIS_SMALL_GHOSTS];
+	float v[ALIS_MAXSRCV];
+};
+
+template <int ALT>
+__global__ void __launch_bounds__(1024) k_small_step(const __grid_constant__ SmallStepParams S)
+{
+	const Layout &L = S.P[0].L;
+	for (int m = 0; m < S.nm; m++) {
+		const HalfStepParams &P = S.P[m];
+		const int nk = P.kMAX - P.kMIN + 1, nj = P.jMAX - P.jMIN + 1, ni = P.iMAX - P.iMIN + 1;
+		const int cells = ni * nj * nk;
+		for (int t = threadIdx.x; t < cells; t += blockDim.x)
+			stepCell<ALT>(P, P.iMIN + t / (nk * nj), P.jMIN + (t / nk) % nj, P.kMIN + t % nk, 0, P.nobj);
+	}
+	__syncthreads();
+	// sources (reference src/update.c:161-179), later patches see earlier ones
+	for (int q = 0; q < S.nsrc; q++) {
+		const alisgpu_source_patch &p = S.src[q];
+		const int nk = 1 + p.k1 - p.k0, nj = 1 + p.j1 - p.j0, ni = 1 + p.i1 - p.i0;
+		float *F = S.F[p.m][p.comp];
+		for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
+			const int i = p.i0 + t / (nk * nj), j = p.j0 + (t / nk) % nj, k = p.k0 + t % nk;
+			if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk) {
+				atomicOr(S.P[0].err, 4u);
+				continue;
+			}
+			F[L.at(i, j, k)] += S.v[p.voff + t];
+		}
+		__syncthreads();
+	}
+	// ghost copies in list order (reference src/update.c:182-191)
+	for (int q = 0; q < S.nghost; q++) {
+		const alisgpu_ghost_copy &g = S.ghost[q];
+		const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0, ni = 1 + g.i1 - g.i0;
+		const int cells = (ni > 0 && nj > 0 && nk > 0) ? ni * nj * nk : 0;
+		for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+			const int i = g.i0 + t / (nk * nj), j = g.j0 + (t / nk) % nj, k = g.k0 + t % nk;
+			const int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
+			if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk ||
+			    si < L.i0 || si >= L.i0 + L.ni || sj < L.j0 || sj >= L.j0 + L.nj || sk < L.k0 || sk >= L.k0 + L.nk) {
+				atomicOr(S.P[0].err, 2u);
+				continue;
+			}
+			const long long d = L.at(i, j, k), src = L.at(si, sj, sk);
+			float *F = S.F[0][g.comp];
+			if (S.nm > 1) {
+				float *G = S.F[1][g.comp];
+				const float f = F[src], gg = G[src];
+				F[d] = g.cosk * f + g.sink * gg;
+				G[d] = g.cosk * gg - g.sink * f;
+			} else {
+				F[d] = g.cosk * F[src];
+			}
+		}
+		__syncthreads();
 	}
 }
 
@@ -876,9 +959,42 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	}
 	if (w->L.elems() >= (1ull << 31))
 		return alisgpu__fail(ALISGPU_ERANGE, "half_step: %zu elements per field exceed 32-bit indexing", w->L.elems());
+	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
+	if (cells <= ALIS_SMALL_CELLS && s->nsrc <= ALIS_MAXSRC && s->nvalues <= ALIS_MAXSRCV && s->nghost <= ALIS_SMALL_GHOSTS) {
+		static SmallStepParams S;
+		S.nm = 1 + g.complexField;
+		for (int m = 0; m < S.nm; m++) {
+			S.P[m] = P;
+			HalfStepParams &Q = S.P[m];
+			Q.m = m;
+			for (int c = 0; c < 3; c++) {
+				Q.F[c] = field == 0 ? w->E[m][c] : w->H[m][c];
+				Q.G[c] = field == 0 ? w->H[m][c] : w->E[m][c];
+				Q.C[c] = field == 0 ? w->C[c] : 0;
+				Q.Fother[c] = w->E[m][c];
+			}
+			for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) Q.psi[f][q] = w->psi[field][m][f][q];
+		}
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			S.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		S.nsrc = s->nsrc, S.nghost = s->nghost;
+		if (s->nsrc) memcpy(S.src, s->src, s->nsrc * sizeof(alisgpu_source_patch));
+		if (s->nghost) memcpy(S.ghost, s->ghost, s->nghost * sizeof(alisgpu_ghost_copy));
+		if (s->nvalues) memcpy(S.v, s->values, s->nvalues * sizeof(float));
+		int slot = alisgpu__prof_start();
+		if (field == 0) k_small_step<1><<<1, 1024, 0, gStream>>>(S);
+		else k_small_step<-1><<<1, 1024, 0, gStream>>>(S);
+		alisgpu__prof_stop(slot, ALISGPU_K_STEP_AUX);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+		return ALISGPU_OK;
+	}
 	const int ni = g.iMAX - g.iMIN + 1;
-	dim3 block(TX, TY, 1);
-	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + TY) / TY, ni);
+	const int ty = STEP_TY(field == 0 ? 1 : -1);
+	dim3 block(TX, ty, 1);
+	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + ty) / ty, ni);
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -891,8 +1007,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		int slot = alisgpu__prof_start();
 		if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
 		else k_half_step<-1><<<grid, block, 0, gStream>>>(P);
-		long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
-		alisgpu__prof_stop(slot, cells < 65536 ? ALISGPU_K_STEP_AUX : field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
+		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 	}
 	ALIS_CUDA(cudaGetLastError());

@@ -136,12 +136,13 @@ def peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def traffic_per_launch():
-    """DRAM bytes per half-step launch from the committed ncu summary."""
+def traffic_per_launch_pair():
+    """DRAM bytes of one E + one H half-step launch from the committed ncu
+    summary of this workload."""
     p = os.path.join(ROOT, "profiles", "k_half_step_c2.txt")
     try:
         for line in open(p):
-            if line.startswith("dram_bytes_per_launch:"):
+            if line.startswith("dram_bytes_per_launch_pair:"):
                 return float(line.split(":")[1])
     except OSError:
         pass
@@ -246,10 +247,14 @@ def engine_arm(args, rank, world, local):
     achieved = step_bytes / (pair_ms / 1e3) / 1e9
     pk, pk_kind = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
-    traffic = traffic_per_launch()
+    traffic = traffic_per_launch_pair()
     total_ms = sum(t for t, _ in kinds.values())
-    cpu = run_cpu(HALF, args.cpu_steps, 1)
-    cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
+    cpu_baseline = None
+    if args.cpu_steps > 0:
+        cpu = run_cpu(HALF, args.cpu_steps, 1)
+        cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
+        cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
+                        "sample": "%d steps of the full world after 1 warm-up step (oracle restatement, OpenMP)" % cpu["steps"]}
     value = cells * K * world / dev_s / 1e9
     line = {
         "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
@@ -266,8 +271,7 @@ def engine_arm(args, rank, world, local):
                      "kernel": "k_half_step (E + H launches, mean per launch pair)",
                      "algorithmic_bytes_per_step": step_bytes, "launch_pair_ms": pair_ms},
         "kernel_share": {k: round(t / total_ms, 4) for k, (t, n) in kinds.items() if n},
-        "cpu_baseline": {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
-                         "sample": "%d steps of the full world after 1 warm-up step (oracle restatement, OpenMP)" % cpu["steps"]},
+        "cpu_baseline": cpu_baseline,
         "gpu_launches": int(launches),
         "clocks": clocks,
         "result_flux": flux,
@@ -281,7 +285,7 @@ def main():
     ap.add_argument("--steps", type=int, default=256)
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=4)
+    ap.add_argument("--cpu-steps", type=int, default=4, help="steps of the CPU baseline sample (0: skip it)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -23,7 +23,11 @@ CASES = [
     ("sym", 1, 80),
     ("hbc", 1, 60),
     ("multi", 1, 80),
+    # rows longer than one warp's 128 cells, with a ragged float4 at the end
+    ("c2", 2, 30),
+    ("c1", 3, 40),
 ]
+IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
 
 def binary(against):

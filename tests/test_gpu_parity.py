@@ -22,7 +22,7 @@ FAR = ("F.ffP", "F.ffS")
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene,scale,steps", scenes.CASES, ids=[c[0] for c in scenes.CASES])
+@pytest.mark.parametrize("scene,scale,steps", scenes.CASES, ids=scenes.IDS)
 def test_engine_bit_identical_to_oracle(scene, scale, steps):
     gpu = scenes.run("engine", scene, scale, steps)
     cpu = scenes.run("oracle", scene, scale, steps)
@@ -31,14 +31,17 @@ def test_engine_bit_identical_to_oracle(scene, scale, steps):
     assert not bad, "differs from the oracle: %s" % bad[:10]
     far = [k for k in gpu if k.startswith(FAR)]
     if far:
+        # 1e-5 relative to the value, or to 1e-6 of the scene's largest
+        # far-field sample for directions whose exact value is near zero
         wide = scenes.run("oracle", scene, scale, steps, env={"ALIS_ORACLE_FF64": "1"})
+        top = max(abs(complex(wide[k].reshape(-1)[0])) for k in far)
         for k in far:
             x, y = complex(gpu[k].reshape(-1)[0]), complex(wide[k].reshape(-1)[0])
-            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-30), (k, x, y)
+            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-6 * top, 1e-30), (k, x, y)
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene,scale,steps", scenes.CASES[:2], ids=[c[0] for c in scenes.CASES[:2]])
+@pytest.mark.parametrize("scene,scale,steps", scenes.CASES[:2], ids=scenes.IDS[:2])
 def test_engine_matches_reference_fixture(scene, scale, steps):
     gpu = scenes.run("engine", scene, scale, steps)
     gold = GOLDEN["%s/%d/%d" % (scene, scale, steps)]
