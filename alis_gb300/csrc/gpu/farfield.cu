@@ -288,3 +288,102 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 	}
 	return ALISGPU_OK;
 }
+
+// ---------------------------------------------------------------------
+// Scratch-free variant: the same sums with every device buffer taken from
+// one file-scope array instead of cudaMalloc.  The array is set up once
+// per device (cudaGetSymbolAddress with that device current) by the first
+// call made on it; make that first call before any stream capture starts.
+// Calls share the array, so overlapping calls (several host threads, or
+// a call issued while another is in flight) race; calls from one thread
+// are serialised by the synchronisation at the end of each call.
+// ---------------------------------------------------------------------
+static __device__ __align__(256) unsigned char ffStaticScratch[ALISGPU_FF_STATIC_BYTES];
+#define FF_MAX_DEVICES 64
+static unsigned char *ffStaticBase[FF_MAX_DEVICES];
+
+extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
+                                            const double *T, int nk, const unsigned char *present,
+                                            const double *kx, const double *ky, double *out)
+{
+	if (!p || !g || nA < 0 || !T || !present || !kx || !ky || !out || nk < 0)
+		return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums_static: bad argument");
+	if (!nA) return ALISGPU_OK;
+	int dev = 0;
+	ALIS_CUDA(cudaGetDevice(&dev));
+	if (dev < 0 || dev >= FF_MAX_DEVICES) return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: device %d beyond %d", dev, FF_MAX_DEVICES);
+	if (!ffStaticBase[dev]) {
+		void *base = 0;
+		ALIS_CUDA(cudaGetSymbolAddress(&base, ffStaticScratch));
+		ffStaticBase[dev] = (unsigned char *)base;
+	}
+	// carve the scratch: tables, test fields, flags, wave numbers, partials
+	size_t off = 0;
+	auto take = [&](size_t bytes) -> size_t { size_t at = off; off += (bytes + 255) & ~(size_t)255; return at; };
+	const size_t xb = (size_t)g->xLen * sizeof(double), yb = (size_t)g->yLen * sizeof(double), zb = (size_t)g->zLen * sizeof(double);
+	size_t oTab[10];
+	for (int q = 0; q < 4; q++) oTab[q] = take(xb);
+	for (int q = 4; q < 8; q++) oTab[q] = take(yb);
+	for (int q = 8; q < 10; q++) oTab[q] = take(zb);
+	const size_t oT = take((size_t)nA * 6 * nk * sizeof(double2));
+	const size_t oPr = take((size_t)nA * 6);
+	const size_t oKx = take((size_t)nA * sizeof(double)), oKy = take((size_t)nA * sizeof(double));
+	const size_t oPart = take((size_t)nA * 6 * sizeof(double2));
+	if (off > (size_t)ALISGPU_FF_STATIC_BYTES)
+		return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: %d directions need %zu bytes of scratch, the static buffer holds %u; "
+		                     "split the batch", nA, off, (unsigned)ALISGPU_FF_STATIC_BYTES);
+	cudaStream_t st = alisgpu__stream();
+	unsigned char *base = ffStaticBase[dev];
+	FFParams P;
+	memset(&P, 0, sizeof P);
+	P.nface = alisgpu__phaser_nface(p);
+	int maxn = 1;
+	for (int q = 0; q < P.nface; q++) {
+		const alisgpu_face *fc = alisgpu__phaser_face(p, q);
+		FFFace &F = P.face[q];
+		F.axis = fc->axis;
+		F.i0 = fc->i0, F.i1 = fc->i1, F.j0 = fc->j0, F.j1 = fc->j1, F.k0 = fc->k0, F.k1 = fc->k1;
+		long long cells;
+		F.acc = alisgpu__phaser_acc(p, f, q, &cells);
+		int n1 = F.axis == 0 ? 1 + F.j1 - F.j0 : 1 + F.i1 - F.i0;
+		int n2 = F.axis == 2 ? 1 + F.j1 - F.j0 : 1 + F.k1 - F.k0;
+		maxn = n1 + n2 > maxn ? n1 + n2 : maxn;
+	}
+	size_t smem = (size_t)4 * maxn * sizeof(double2);
+	if (smem > 200 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: face of %d cells per side too large", maxn);
+	const double *src[10] = { g->xE, g->xH, g->dxE, g->dxH, g->yE, g->yH, g->dyE, g->dyH, g->dzE, g->dzH };
+	const size_t len[10] = { xb, xb, xb, xb, yb, yb, yb, yb, zb, zb };
+	const double *dev10[10];
+	for (int q = 0; q < 10; q++) {
+		dev10[q] = (const double *)(base + oTab[q]);
+		if (len[q]) ALIS_CUDA(cudaMemcpyAsync(base + oTab[q], src[q], len[q], cudaMemcpyHostToDevice, st));
+	}
+	P.g = *g;
+	P.g.xE = dev10[0], P.g.xH = dev10[1], P.g.dxE = dev10[2], P.g.dxH = dev10[3];
+	P.g.yE = dev10[4], P.g.yH = dev10[5], P.g.dyE = dev10[6], P.g.dyH = dev10[7];
+	P.g.dzE = dev10[8], P.g.dzH = dev10[9];
+	P.nk = nk;
+	ALIS_CUDA(cudaMemcpyAsync(base + oT, T, (size_t)nA * 6 * nk * sizeof(double2), cudaMemcpyHostToDevice, st));
+	ALIS_CUDA(cudaMemcpyAsync(base + oPr, present, (size_t)nA * 6, cudaMemcpyHostToDevice, st));
+	ALIS_CUDA(cudaMemcpyAsync(base + oKx, kx, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st));
+	ALIS_CUDA(cudaMemcpyAsync(base + oKy, ky, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st));
+	// the partials of missing faces must read as zero
+	ALIS_CUDA(cudaMemsetAsync(base + oPart, 0, (size_t)nA * 6 * sizeof(double2), st));
+	P.T = (const double2 *)(base + oT);
+	P.present = base + oPr;
+	P.kx = (const double *)(base + oKx), P.ky = (const double *)(base + oKy);
+	P.part = (double2 *)(base + oPart);
+	ALIS_CUDA(cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	if (P.nface) {
+		dim3 grid(nA, P.nface);
+		int slot = alisgpu__prof_start();
+		k_farfield<<<grid, FF_THREADS, smem, st>>>(P);
+		alisgpu__prof_stop(slot, ALISGPU_K_FARFIELD);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	// out[(a*6 + face)*2 + re/im] has the layout of the double2 partials
+	ALIS_CUDA(cudaMemcpyAsync(out, base + oPart, (size_t)nA * 6 * sizeof(double2), cudaMemcpyDeviceToHost, st));
+	ALIS_CUDA(cudaStreamSynchronize(st));
+	return ALISGPU_OK;
+}

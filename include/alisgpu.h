@@ -219,6 +219,22 @@ int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_farfield_geom 
                           const double *T, int nk, const unsigned char *present,
                           const double *kx, const double *ky, double *out);
 
+/* Scratch-free variant of alisgpu_farfield_sums (no counterpart in the
+ * reference): same arguments and results, but it allocates nothing --
+ * its device buffers (tables, test fields, partial sums) live in one
+ * static device array of ALISGPU_FF_STATIC_BYTES.  For callers that must
+ * not allocate: code that captures the step into a CUDA graph (cudaMalloc
+ * and cudaFree are not stream-ordered, and cudaFree synchronises the
+ * device), and serving loops whose device memory is fully admitted to
+ * jobs.  A batch whose buffers exceed the array is refused with
+ * ALISGPU_ERANGE (about 650 directions of a 256-cell-high phaser box fit).
+ * The first call on a device sets the array up; make it before any
+ * stream capture.  Overlapping calls race on the shared array. */
+#define ALISGPU_FF_STATIC_BYTES (16u << 20)
+int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
+                                 const double *T, int nk, const unsigned char *present,
+                                 const double *kx, const double *ky, double *out);
+
 #ifdef __cplusplus
 }
 #endif
