@@ -530,7 +530,8 @@ __device__ __forceinline__ void pmlFace(const HalfStepParams &P, int i, int j, i
 // TFSF incident-field corrections (reference src/update.c:205-272).
 // E step: aux H; H step: aux E.  Face-by-face in the reference order;
 // (dtds * G) * C rounds like the reference's `dtds * G[..] * C[..]`.
-template <int ALT>
+// KONLY: the cell lies on no i or j face plane, only the k faces apply.
+template <int ALT, bool KONLY = false>
 __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, int k,
 	float &fx, float &fy, float &fz, bool hasC, float cx, float cy, float cz)
 {
@@ -539,11 +540,11 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 		const float *A0 = T.G[P.m][0], *A1 = T.G[P.m][1], *A2 = T.G[P.m][2];
 		if (ALT == 1) {
 			// alias Alt of the aux H components: x rows (0,1,1), y rows (1,0,1)
-			if (T.iMin > P.iMIN && i == T.iMin) {
+			if (!KONLY && T.iMin > P.iMIN && i == T.iMin) {
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) { float v = -T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 1, 0), P.err); fz += hasC ? v * cz : v; }
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) { float v = T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 1, 1), P.err); fy += hasC ? v * cy : v; }
 			}
-			if (T.jMin > P.jMIN && j == T.jMin) {
+			if (!KONLY && T.jMin > P.jMIN && j == T.jMin) {
 				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) { float v = -T.dtdMin[1] * auxGet(A2, auxAt(T, i, j, k, 1, 1), P.err); fx += hasC ? v * cx : v; }
 				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) { float v = T.dtdMin[1] * auxGet(A0, auxAt(T, i, j, k, 0, 1), P.err); fz += hasC ? v * cz : v; }
 			}
@@ -551,11 +552,11 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) { float v = -T.dtdMin[2] * auxGet(A0, auxAt(T, i, j, k, 0, 1), P.err); fy += hasC ? v * cy : v; }
 				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) { float v = T.dtdMin[2] * auxGet(A1, auxAt(T, i, j, k, 1, 0), P.err); fx += hasC ? v * cx : v; }
 			}
-			if (T.iMax < P.iMAX && i == T.iMax) {
+			if (!KONLY && T.iMax < P.iMAX && i == T.iMax) {
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) { float v = T.dtdMax[0] * auxGet(A1, auxAt(T, i + 1, j, k, 1, 0), P.err); fz += hasC ? v * cz : v; }
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) { float v = -T.dtdMax[0] * auxGet(A2, auxAt(T, i + 1, j, k, 1, 1), P.err); fy += hasC ? v * cy : v; }
 			}
-			if (T.jMax < P.jMAX && j == T.jMax) {
+			if (!KONLY && T.jMax < P.jMAX && j == T.jMax) {
 				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) { float v = T.dtdMax[1] * auxGet(A2, auxAt(T, i, j + 1, k, 1, 1), P.err); fx += hasC ? v * cx : v; }
 				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) { float v = -T.dtdMax[1] * auxGet(A0, auxAt(T, i, j + 1, k, 0, 1), P.err); fz += hasC ? v * cz : v; }
 			}
@@ -565,11 +566,11 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 			}
 		} else {
 			// alias Alt of the aux E components: x rows (1,0,0), y rows (0,1,0)
-			if (T.iMin > P.iMIN && i == T.iMin) {
+			if (!KONLY && T.iMin > P.iMIN && i == T.iMin) {
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) fz += T.dtdMin[0] * auxGet(A1, auxAt(T, i, j, k, 0, 1), P.err);
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) fy += -T.dtdMin[0] * auxGet(A2, auxAt(T, i, j, k, 0, 0), P.err);
 			}
-			if (T.jMin > P.jMIN && j == T.jMin) {
+			if (!KONLY && T.jMin > P.jMIN && j == T.jMin) {
 				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) fx += T.dtdMin[1] * auxGet(A2, auxAt(T, i, j, k, 0, 0), P.err);
 				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) fz += -T.dtdMin[1] * auxGet(A0, auxAt(T, i, j, k, 1, 0), P.err);
 			}
@@ -577,11 +578,11 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 				if (i >= T.iMIN && i <= T.iMAX && j >= T.jMin && j <= T.jMax) fy += T.dtdMin[2] * auxGet(A0, auxAt(T, i, j, k, 1, 0), P.err);
 				if (i >= T.iMin && i <= T.iMax && j >= T.jMIN && j <= T.jMAX) fx += -T.dtdMin[2] * auxGet(A1, auxAt(T, i, j, k, 0, 1), P.err);
 			}
-			if (T.iMax < P.iMAX && i == T.iMax + 1) {
+			if (!KONLY && T.iMax < P.iMAX && i == T.iMax + 1) {
 				if (j >= T.jMIN && j <= T.jMAX && k >= T.kMin && k <= T.kMax) fz += -T.dtdMax[0] * auxGet(A1, auxAt(T, i - 1, j, k, 0, 1), P.err);
 				if (j >= T.jMin && j <= T.jMax && k >= T.kMIN && k <= T.kMAX) fy += T.dtdMax[0] * auxGet(A2, auxAt(T, i - 1, j, k, 0, 0), P.err);
 			}
-			if (T.jMax < P.jMAX && j == T.jMax + 1) {
+			if (!KONLY && T.jMax < P.jMAX && j == T.jMax + 1) {
 				if (i >= T.iMin && i <= T.iMax && k >= T.kMIN && k <= T.kMAX) fx += -T.dtdMax[1] * auxGet(A2, auxAt(T, i, j - 1, k, 0, 0), P.err);
 				if (i >= T.iMIN && i <= T.iMAX && k >= T.kMin && k <= T.kMax) fz += T.dtdMax[1] * auxGet(A0, auxAt(T, i, j - 1, k, 1, 0), P.err);
 			}
@@ -646,17 +647,38 @@ __device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, 
 	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
 }
 
-// Fused half step of a large world, one thread per cell, one i plane per
-// block of TX x TY threads.  Index arithmetic is 32-bit (at most 2^31
-// elements per array, checked on the host).  Worlds with more than 8
-// objects add a per-block list of the objects that meet the tile.
-#define TX 32
-// launch shapes (measured on the 256^3 dispersive world): E 32x8 threads
-// capped at 40 registers (6 blocks per SM); H 32x4 capped at 40 (12 blocks)
-#define STEP_TY(ALT) ((ALT) == 1 ? 8 : 4)
-#define STEP_MINB(ALT) ((ALT) == 1 ? 6 : 12)
+// Cells on a TFSF face plane or inside a dispersive object box run the
+// full sequence out of line (their neighbours' lean code stays small);
+// P is the kernel's __grid_constant__ parameter, passed by reference.
 template <int ALT>
-__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const HalfStepParams P)
+__device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int k, const int *list, int nIter)
+{
+	stepCell<ALT>(P, i, j, k, list, nIter);
+}
+
+// Fused half step of a large world, one thread per cell, one i plane per
+// block of TX x TY threads.  Tiers by the cell's class bits: plain cells
+// take the curl only; CPML cells and cells on TFSF k face planes add
+// their face updates, all inline; cells on TFSF i or j face planes (whole
+// blocks or warps) and dispersive cells go to hardCell.  Index
+// arithmetic is 32-bit (at most 2^31 elements per array, checked on the
+// host).  Worlds with more than 8 objects add a per-block list of the
+// objects that meet the tile.
+#define TX 32
+// launch shapes, measured on the 256^3 dispersive world: 32x4 threads,
+// 16 blocks per SM (32 registers) for both fields; -D overrides for tuning
+#ifndef ALIS_E_TY
+#define ALIS_E_TY 4
+#define ALIS_E_MINB 16
+#endif
+#ifndef ALIS_H_TY
+#define ALIS_H_TY 4
+#define ALIS_H_MINB 16
+#endif
+#define STEP_TY(ALT) ((ALT) == 1 ? ALIS_E_TY : ALIS_H_TY)
+#define STEP_MINB(ALT) ((ALT) == 1 ? ALIS_E_MINB : ALIS_H_MINB)
+template <int ALT>
+__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
 	constexpr int TY_ = STEP_TY(ALT);
 	__shared__ int tileList[ALIS_TILE_OBJ];
@@ -690,11 +712,51 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 		__syncthreads();
 	}
 	if (k > P.kMAX || j > P.jMAX) return;
-	// object loops: the tile's list, or all objects filtered by class bits
-	const int *list = 0;
-	int nIter = P.nobj;
-	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
-	stepCell<ALT>(P, i, j, k, list, nIter);
+	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
+	if (((bi | bj) & CLS_TFSF) || (bi & bj & bk & 0x1FFu)) {
+		// object loops: the tile's list, or all objects filtered by class bits
+		const int *list = 0;
+		int nIter = P.nobj;
+		if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
+		hardCell<ALT>(P, i, j, k, list, nIter);
+		return;
+	}
+	const int sj = (int)P.L.sj, si = (int)P.L.si;
+	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
+	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
+	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
+	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
+	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const bool hasC = P.C[0] != 0;
+	float cx = 1, cy = 1, cz = 1;
+	if (hasC) cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
+	// curl (reference src/update.c:109-118)
+	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
+	if (hasC) {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
+	} else {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
+	}
+	// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
+	if ((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI)) {
+#define PML_ARGS P, i, j, k, fx, fy, fz, gx0, gy0, gz0, gyk, gxk, gzj, gxj, gzi, gyi, hasC, cx, cy, cz
+		if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
+		if (bj & CLS_PML_LO) pmlFace<1>(PML_ARGS);
+		if (bk & CLS_PML_LO) pmlFace<2>(PML_ARGS);
+		if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
+		if (bj & CLS_PML_HI) pmlFace<4>(PML_ARGS);
+		if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
+#undef PML_ARGS
+	}
+	// TFSF k face planes (cells on an i or j face plane went to hardCell)
+	if (bk & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
+	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
 }
 
 // sources, in list order; one block so later patches see earlier ones
