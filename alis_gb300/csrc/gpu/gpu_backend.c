@@ -31,6 +31,7 @@ typedef struct devWorld {
 	int hostStale;            /* device ahead of the host mirrors */
 	int ntf;
 	alisgpu_tfsf tf[MAX_TFSF];
+	int isAux;                /* the auxiliary world of a TFSF box */
 	struct devWorld *next;
 } devWorld;
 
@@ -175,6 +176,7 @@ static void buildTfsf(devWorld *d)
 		alisgpu_tfsf *t = &d->tf[d->ntf++];
 		memset(t, 0, sizeof *t);
 		t->aux = a->dw;
+		a->isAux = 1;
 		t->iMin = S->iMin, t->iMax = S->iMax, t->jMin = S->jMin, t->jMax = S->jMax, t->kMin = S->kMin, t->kMax = S->kMax;
 		t->iMIN = S->iMIN, t->iMAX = S->iMAX, t->jMIN = S->jMIN, t->jMAX = S->jMAX, t->kMIN = S->kMIN, t->kMAX = S->kMAX;
 		t->auxIMAX = S->W->iMAX, t->auxJMAX = S->W->jMAX;
@@ -333,6 +335,7 @@ static void halfStep(world W, int field)
 	s.nvalues = srcList.nv;
 	s.nghost = ghostList(W, field, g);
 	s.ghost = g;
+	s.concurrent = d->isAux;
 	CHECK("half_step", alisgpu_half_step_run(d->dw, &s));
 	d->hostStale = 1;
 }

@@ -44,6 +44,27 @@ extern "C" int alisgpu__check(cudaError_t e, const char *what)
 	return alisgpu__fail(code, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// Side stream for the half steps of TFSF auxiliary worlds, which run
+// concurrently with their parent's half steps.  Ordering: an auxiliary
+// step of field F waits for the parent's last step of the other field
+// (which read the auxiliary F it is about to overwrite); a parent step of
+// field F waits for the last auxiliary step of the other field (whose
+// result it reads).  Any other call that touches world data joins the two
+// streams first, and the next auxiliary step then waits for everything
+// issued before it.
+static cudaStream_t gSide;
+static cudaEvent_t gEvMainDone[2], gEvAuxDone[2], gEvJoin;
+static int gMainRec[2], gAuxRec[2], gSideUsed, gSideWaitsAll = 1;
+
+static void fullJoin(void)
+{
+	if (gSideUsed) {
+		cudaEventRecord(gEvJoin, gSide);
+		cudaStreamWaitEvent(gStream, gEvJoin, 0);
+	}
+	gSideWaitsAll = 1;
+}
+
 extern "C" const char *alisgpu_last_error(void) { return gErr; }
 extern "C" void alisgpu__count_launch(void) { gLaunches++; }
 extern "C" unsigned long long alisgpu_launch_count(void) { return gLaunches; }
@@ -60,6 +81,12 @@ extern "C" int alisgpu_init(void)
 	int dev = env ? atoi(env) : 0;
 	ALIS_CUDA(cudaSetDevice(dev));
 	ALIS_CUDA(cudaStreamCreateWithFlags(&gStream, cudaStreamNonBlocking));
+	ALIS_CUDA(cudaStreamCreateWithFlags(&gSide, cudaStreamNonBlocking));
+	for (int f = 0; f < 2; f++) {
+		ALIS_CUDA(cudaEventCreateWithFlags(&gEvMainDone[f], cudaEventDisableTiming));
+		ALIS_CUDA(cudaEventCreateWithFlags(&gEvAuxDone[f], cudaEventDisableTiming));
+	}
+	ALIS_CUDA(cudaEventCreateWithFlags(&gEvJoin, cudaEventDisableTiming));
 	ALIS_CUDA(cudaMalloc(&gErrWord, sizeof(unsigned int)));
 	ALIS_CUDA(cudaMemset(gErrWord, 0, sizeof(unsigned int)));
 	gInit = 1;
@@ -74,7 +101,13 @@ static int gProfOn;
 static double gProfMs[ALISGPU_K_KINDS];
 static unsigned long long gProfN[ALISGPU_K_KINDS];
 
-extern "C" int alisgpu_profile(int enable) { gProfOn = enable; return ALISGPU_OK; }
+extern "C" int alisgpu_profile(int enable)
+{
+	// auxiliary steps change streams with the mode: order them across it
+	if (gInit) fullJoin();
+	gProfOn = enable;
+	return ALISGPU_OK;
+}
 
 extern "C" int alisgpu__prof_start(void)
 {
@@ -120,6 +153,7 @@ extern "C" int alisgpu_profile_read(int kind, double *ms, unsigned long long *la
 extern "C" int alisgpu_synchronize(void)
 {
 	if (!gInit) return ALISGPU_OK;
+	fullJoin();
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	unsigned int e = 0;
 	ALIS_CUDA(cudaMemcpy(&e, gErrWord, sizeof e, cudaMemcpyDeviceToHost));
@@ -221,6 +255,7 @@ static void freeObjects(alisgpu_world *w)
 
 extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 {
+	fullJoin();
 	if (!w) return ALISGPU_OK;
 	cudaStreamSynchronize(gStream);
 	for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
@@ -244,6 +279,7 @@ extern "C" size_t alisgpu_world_bytes(const alisgpu_world *w) { return w ? w->by
 
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
+	fullJoin();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_reset: null world");
 	size_t n = w->L.elems() * sizeof(float);
 	for (int m = 0; m <= w->g.complexField; m++) for (int c = 0; c < 3; c++) {
@@ -279,6 +315,7 @@ static int upload1D(alisgpu_world *w, float **dst, const float *src, int n)
 
 extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *const dtd[3], const float *const cpml[9])
 {
+	fullJoin();
 	if (!w || grid < 0 || grid > 1 || !dtd) return alisgpu__fail(ALISGPU_EINVAL, "set_line_tables: bad argument");
 	int len[3] = { w->g.iMAX - w->g.iMIN + 1, w->g.jMAX - w->g.jMIN + 1, w->g.kMAX - w->g.kMIN + 1 };
 	int rc;
@@ -302,6 +339,7 @@ static int uploadBoxToLayout(alisgpu_world *w, float *dev, const float *host, in
 
 extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *cy, const float *cz)
 {
+	fullJoin();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "set_eps: null world");
 	const alisgpu_geometry &g = w->g;
 	const float *src[3] = { cx, cy, cz };
@@ -321,6 +359,7 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 
 extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *objs)
 {
+	fullJoin();
 	if (!w || n < 0 || (n && !objs)) return alisgpu__fail(ALISGPU_EINVAL, "set_dispersive: bad argument");
 	cudaStreamSynchronize(gStream);
 	freeObjects(w);
@@ -379,6 +418,7 @@ static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
 
 extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
 {
+	fullJoin();
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_download: bad argument");
 	const Layout &L = w->L;
@@ -390,6 +430,7 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 
 extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
 {
+	fullJoin();
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_upload: bad argument");
 	const Layout &L = w->L;
@@ -401,6 +442,7 @@ extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp
 
 extern "C" int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host)
 {
+	fullJoin();
 	if (!w || !host || n < 0 || n >= (int)w->objs.size() || m < 0 || m > w->g.complexField || comp < 0 || comp > 2)
 		return alisgpu__fail(ALISGPU_EINVAL, "current_download: bad argument");
 	DevObj &o = w->objs[n];
@@ -1021,6 +1063,11 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	}
 	if (w->L.elems() >= (1ull << 31))
 		return alisgpu__fail(ALISGPU_ERANGE, "half_step: %zu elements per field exceed 32-bit indexing", w->L.elems());
+	// an auxiliary world runs on the side stream (not while timing kernels
+	// one by one); any other world first waits for the auxiliary step of
+	// the other field, whose fields its TFSF corrections read
+	const bool side = s->concurrent && !gProfOn;
+	if (!side && gAuxRec[1 - field]) ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvAuxDone[1 - field], 0));
 	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
 	if (cells <= ALIS_SMALL_CELLS && s->nsrc <= ALIS_MAXSRC && s->nvalues <= ALIS_MAXSRCV && s->nghost <= ALIS_SMALL_GHOSTS) {
 		static SmallStepParams S;
@@ -1045,12 +1092,32 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		if (s->nsrc) memcpy(S.src, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		if (s->nghost) memcpy(S.ghost, s->ghost, s->nghost * sizeof(alisgpu_ghost_copy));
 		if (s->nvalues) memcpy(S.v, s->values, s->nvalues * sizeof(float));
+		// on the side stream: after the parent's last step of the other
+		// field, or after everything when a join asked for that
+		cudaStream_t st = gStream;
+		if (side) {
+			st = gSide;
+			if (gSideWaitsAll) {
+				ALIS_CUDA(cudaEventRecord(gEvJoin, gStream));
+				ALIS_CUDA(cudaStreamWaitEvent(gSide, gEvJoin, 0));
+				gSideWaitsAll = 0;
+			} else if (gMainRec[1 - field]) {
+				ALIS_CUDA(cudaStreamWaitEvent(gSide, gEvMainDone[1 - field], 0));
+			}
+		}
 		int slot = alisgpu__prof_start();
-		if (field == 0) k_small_step<1><<<1, 1024, 0, gStream>>>(S);
-		else k_small_step<-1><<<1, 1024, 0, gStream>>>(S);
+		if (field == 0) k_small_step<1><<<1, 1024, 0, st>>>(S);
+		else k_small_step<-1><<<1, 1024, 0, st>>>(S);
 		alisgpu__prof_stop(slot, ALISGPU_K_STEP_AUX);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
+		if (side) {
+			ALIS_CUDA(cudaEventRecord(gEvAuxDone[field], gSide));
+			gAuxRec[field] = 1, gSideUsed = 1;
+		} else {
+			ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
+			gMainRec[field] = 1;
+		}
 		return ALISGPU_OK;
 	}
 	const int ni = g.iMAX - g.iMIN + 1;
@@ -1142,6 +1209,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			ALIS_CUDA(cudaGetLastError());
 		}
 	}
+	ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
+	gMainRec[field] = 1;
 	return ALISGPU_OK;
 }
 

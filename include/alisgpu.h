@@ -161,6 +161,9 @@ typedef struct alisgpu_half_step {
 	int nvalues;
 	int nghost;
 	const alisgpu_ghost_copy *ghost;
+	int concurrent;                             /* 1: a TFSF auxiliary world, read only by its
+	                                               parent's half steps; it may run concurrently
+	                                               with the parent's step of the same field */
 } alisgpu_half_step;
 
 /* One half step of a world: conductivity, ADE subtraction, curl with
