@@ -117,13 +117,11 @@ double c2_step_h2d_bytes(void)
 	return 4.0 * values + 16.0 * nfreqs;
 }
 
-/* bytes of the phaser accumulators read back by c2_result */
+/* bytes read back by c2_result: the flux of each of the 6 faces at every
+ * frequency (the accumulators are reduced where they live) */
 double c2_result_d2h_bytes(void)
 {
-	phaser p = P;
-	double ni = 1 + p->iMax - p->iMin, nj = 1 + p->jMax - p->jMin, nk = 1 + p->kMax - p->kMin;
-	double cells = 2 * nj * nk + 2 * ni * nk + 2 * ni * nj;
-	return cells * 4 * 8 * nfreqs;
+	return 6.0 * sizeof(float) * nfreqs;
 }
 
 long c2_cells(void) { return (long)W->iNUM * W->jNUM * W->kNUM; }

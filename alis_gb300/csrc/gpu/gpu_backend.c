@@ -41,6 +41,8 @@ typedef struct devPhaser {
 	int faceSlot[6];          /* cfield index (0..5: xMin,xMax,yMin,yMax,zMin,zMax) of each device face */
 	alisgpu_phaser *dp;
 	int hostStale;
+	int fluxStale;            /* face fluxes behind the accumulators */
+	float *flux;              /* [nfreq][6] face fluxes by cfield slot */
 	float *phE, *phH;
 	struct devPhaser *next;
 } devPhaser;
@@ -391,6 +393,8 @@ void alis_be_phaser_created(phaser P)
 	CHECK("phaser_create", alisgpu_phaser_create(dw->dw, d->nfreq, d->nface, faces, phaserRing(), k && k[0] == '1', &d->dp));
 	d->phE = calloc(2 * d->nfreq, sizeof(float));
 	d->phH = calloc(2 * d->nfreq, sizeof(float));
+	d->flux = calloc((size_t)6 * d->nfreq, sizeof(float));
+	d->fluxStale = 1;
 	d->next = phasers;
 	phasers = d;
 }
@@ -405,6 +409,7 @@ void alis_be_phaser_deleted(phaser P)
 	alisgpu_phaser_destroy(d->dp);
 	free(d->phE);
 	free(d->phH);
+	free(d->flux);
 	free(d);
 }
 
@@ -426,6 +431,31 @@ void updatePhaser(world W, phaser P)
 	}
 	CHECK("phaser_record", alisgpu_phaser_record(d->dp, d->phE, d->phH));
 	d->hostStale = 1;
+	d->fluxStale = 1;
+}
+
+/* face fluxes of every frequency of the set, reduced on the device from
+ * the accumulators, with the spacing tables of the phaser box */
+int alis_be_phaser_flux(phaser P, float face[6])
+{
+	devPhaser *d = findPhaser(P);
+	if (!d) return 0;
+	if (d->fluxStale) {
+		phaser p = d->P;
+		world W = p->W;
+		int lo[3] = { p->iMin, p->jMin, p->kMin }, hi[3] = { p->iMax, p->jMax, p->kMax };
+		const float *wE[3] = { &W->CE->dx[p->iMin], &W->CE->dy[p->jMin], &W->CE->dz[p->kMin] };
+		const float *wH[3] = { &W->CH->dx[p->iMin], &W->CH->dy[p->jMin], &W->CH->dz[p->kMin] };
+		float *out = malloc((size_t)d->nfreq * (d->nface ? d->nface : 1) * sizeof(float));
+		CHECK("phaser_face_flux", alisgpu_phaser_face_flux(d->dp, wE, wH, lo, hi, out));
+		memset(d->flux, 0, (size_t)6 * d->nfreq * sizeof(float));
+		for (int n = 0; n < d->nfreq; n++)
+			for (int f = 0; f < d->nface; f++) d->flux[n * 6 + d->faceSlot[f]] = out[n * d->nface + f];
+		free(out);
+		d->fluxStale = 0;
+	}
+	memcpy(face, d->flux + (P - d->P) * 6, 6 * sizeof(float));
+	return 1;
 }
 
 static void downloadPhaser(devPhaser *d)
@@ -455,6 +485,11 @@ void alis_be_sync_phaser(phaser P)
 {
 	devPhaser *d = findPhaser(P);
 	if (d && d->hostStale) downloadPhaser(d);
+}
+
+void alis_be_sync_phasers_of(world W)
+{
+	for (devPhaser *d = phasers; d; d = d->next) if (d->P->W == W && d->hostStale) downloadPhaser(d);
 }
 
 void alis_be_sync_all(void)

@@ -34,6 +34,8 @@ struct alisgpu_phaser {
 	std::vector<float2> hostPhase;        // phases of buffered steps
 	int *faceInfo;                        // per face: axis, box
 	int used;                             // buffered steps
+	float *fluxTab;                       // spacing tables and sums of the flux kernels
+	size_t fluxTabBytes;
 };
 
 // world layout and field pointers needed by the gather kernel
@@ -176,6 +178,7 @@ extern "C" int alisgpu_phaser_destroy(alisgpu_phaser *p)
 	if (p->acc) cudaFree(p->acc);
 	if (p->comp) cudaFree(p->comp);
 	if (p->phase) cudaFree(p->phase);
+	if (p->fluxTab) cudaFree(p->fluxTab);
 	delete p;
 	return ALISGPU_OK;
 }
@@ -255,6 +258,189 @@ extern "C" int alisgpu_phaser_zero(alisgpu_phaser *p)
 	size_t bytes = (size_t)p->nfreq * p->cells * 4 * sizeof(float2);
 	ALIS_CUDA(cudaMemsetAsync(p->acc, 0, bytes, alisgpu__stream()));
 	if (p->comp) ALIS_CUDA(cudaMemsetAsync(p->comp, 0, bytes, alisgpu__stream()));
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
+// Poynting flux of every face at every frequency (reference
+// src/phaser.c:156-219), with the reference's arithmetic in its order as
+// one OpenMP thread runs it: each face has two sums, each an outer loop
+// over one in-plane index of (spacing x inner sum), the inner sum running
+// over the other index with half-weight edge terms in double and interior
+// terms in float complex.  One thread computes one inner sum; one thread
+// per (frequency, face) then adds the outer loops in order.
+// ---------------------------------------------------------------------
+struct FluxLoop {
+	int face, oIsU, eq, hq, sign;          // outer index is the face's slow in-plane axis u
+	int o0, o1, n0, n1;                    // outer range [o0, o1], inner edges n0, n1
+	const float *wN, *wO;                  // inner (E grid) and outer (H grid) spacings, indexed by index
+	long long start;                       // first inner-sum slot of this loop
+};
+struct FluxParams {
+	int nloop;
+	FluxLoop loop[12];
+	long long perFreq;                     // inner sums per frequency
+	int nface;
+	int nv[6];                             // fast in-plane extent of each face
+	long long faceStart[6];                // first cell of each face
+	long long cells;                       // cells of all faces
+	const float2 *acc;                     // [nfreq][cells][4]
+	float *inner;                          // [nfreq][perFreq]
+	float *out;                            // [nfreq][nface]
+	int nfreq;
+};
+
+// the reference's `sum +/-= 0.5 * w * E * conjf(H)`: double complex product,
+// the float sum widened, the real part rounded back to float
+__device__ __forceinline__ float edgeTerm(float sum, int sign, float w, float2 e, float2 h)
+{
+	const double hw = 0.5 * (double)w;
+	const double ar = hw * (double)e.x, ai = hw * (double)e.y;
+	const double br = (double)h.x, bi = -(double)h.y;
+	const double re = __dsub_rn(__dmul_rn(ar, br), __dmul_rn(ai, bi));
+	return __double2float_rn(sign > 0 ? __dadd_rn((double)sum, re) : __dsub_rn((double)sum, re));
+}
+
+// `sum +/-= w * E * conjf(H)` in float complex arithmetic
+__device__ __forceinline__ float midTerm(float sum, int sign, float w, float2 e, float2 h)
+{
+	const float ar = __fmul_rn(w, e.x), ai = __fmul_rn(w, e.y);
+	const float re = __fsub_rn(__fmul_rn(ar, h.x), __fmul_rn(ai, -h.y));
+	return sign > 0 ? __fadd_rn(sum, re) : __fsub_rn(sum, re);
+}
+
+__global__ void k_phaser_flux_inner(const FluxParams P)
+{
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= P.perFreq * P.nfreq) return;
+	const int f = (int)(t / P.perFreq);
+	const long long r = t % P.perFreq;
+	int l = 0;
+	while (l + 1 < P.nloop && r >= P.loop[l + 1].start) l++;
+	const FluxLoop &L = P.loop[l];
+	const int o = L.o0 + 1 + (int)(r - L.start);   // outer index in (o0, o1]
+	const float2 *acc = P.acc + ((long long)f * P.cells + P.faceStart[L.face]) * 4;
+	const int nv = P.nv[L.face];
+	// cell (u, v) of the face at acc[((u - u0) * nv + (v - v0)) * 4 + q]
+	auto at = [&](int n) -> long long {
+		const long long u = L.oIsU ? o - L.o0 : n - L.n0;
+		const long long v = L.oIsU ? n - L.n0 : o - L.o0;
+		return (u * nv + v) * 4;
+	};
+	float sum = 0;
+	sum = edgeTerm(sum, L.sign, L.wN[L.n0], acc[at(L.n0) + L.eq], acc[at(L.n0) + L.hq]);
+	sum = edgeTerm(sum, L.sign, L.wN[L.n1], acc[at(L.n1) + L.eq], acc[at(L.n1) + L.hq]);
+	for (int n = L.n0 + 1; n < L.n1; n++)
+		sum = midTerm(sum, L.sign, L.wN[n], acc[at(n) + L.eq], acc[at(n) + L.hq]);
+	P.inner[t] = sum;
+}
+
+__global__ void k_phaser_flux_outer(const FluxParams P)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= P.nfreq * P.nface) return;
+	const int f = t / P.nface, face = t % P.nface;
+	const float *inner = P.inner + (long long)f * P.perFreq;
+	float Sum = 0, Part = 0;
+	int seen = 0;
+	for (int l = 0; l < P.nloop; l++) {
+		const FluxLoop &L = P.loop[l];
+		if (L.face != face) continue;
+		float acc = 0;
+		for (int o = L.o0 + 1; o <= L.o1; o++) acc = __fadd_rn(acc, __fmul_rn(L.wO[o], inner[L.start + (o - L.o0 - 1)]));
+		if (seen++ == 0) Sum = acc; else Part = acc;
+	}
+	P.out[t] = __fadd_rn(Sum, Part);
+}
+
+extern "C" int alisgpu_phaser_face_flux(alisgpu_phaser *p, const float *const wE[3], const float *const wH[3],
+                                        const int lo[3], const int hi[3], float *out)
+{
+	if (!p || !wE || !wH || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "phaser_face_flux: bad argument");
+	int rc = alisgpu_phaser_flush(p);
+	if (rc) return rc;
+	if (!p->nface || !p->nfreq) return ALISGPU_OK;
+	cudaStream_t st = alisgpu__stream();
+	int len[3];
+	size_t tabFloats = 0;
+	for (int a = 0; a < 3; a++) {
+		if (hi[a] < lo[a]) return alisgpu__fail(ALISGPU_EINVAL, "phaser_face_flux: empty box");
+		len[a] = 1 + hi[a] - lo[a];
+		tabFloats += 2 * (size_t)len[a];
+	}
+	FluxParams P;
+	memset(&P, 0, sizeof P);
+	P.nface = p->nface, P.nfreq = p->nfreq, P.cells = p->cells, P.acc = p->acc;
+	// inner-sum slots
+	long long per = 0;
+	for (int q = 0; q < p->nface; q++) {
+		const alisgpu_face &fc = p->faces[q];
+		for (int a = 0; a < 3; a++) {
+			const int b0 = a == 0 ? fc.i0 : a == 1 ? fc.j0 : fc.k0, b1 = a == 0 ? fc.i1 : a == 1 ? fc.j1 : fc.k1;
+			if (b0 < lo[a] || b1 > hi[a]) return alisgpu__fail(ALISGPU_EINVAL, "phaser_face_flux: face outside the table box");
+		}
+		const int ua = fc.axis == 0 ? 1 : 0, va = fc.axis == 2 ? 1 : 2;
+		const int u0 = ua == 0 ? fc.i0 : fc.j0, u1 = ua == 0 ? fc.i1 : fc.j1;
+		const int v0 = va == 1 ? fc.j0 : fc.k0, v1 = va == 1 ? fc.j1 : fc.k1;
+		P.nv[q] = 1 + v1 - v0;
+		P.faceStart[q] = p->faceStart[q];
+		// (outer axis is u, E comp, H comp, sign) of the two loops: x face
+		// (u=j, v=k) L1 j-outer Ey Hz +, L2 k-outer Ez Hy -; y face (u=i,
+		// v=k) L1 k-outer Ez Hx +, L2 i-outer Ex Hz -; z face (u=i, v=j) L1
+		// i-outer Ex Hy +, L2 j-outer Ey Hx -.  Components per cell: E1 E2 H1 H2.
+		const int oIsU[2] = { fc.axis == 1 ? 0 : 1, fc.axis == 1 ? 1 : 0 };
+		for (int l = 0; l < 2; l++) {
+			FluxLoop &L = P.loop[P.nloop++];
+			L.face = q, L.oIsU = oIsU[l];
+			L.eq = l == 0 ? 0 : 1, L.hq = l == 0 ? 3 : 2, L.sign = l == 0 ? 1 : -1;
+			L.o0 = L.oIsU ? u0 : v0, L.o1 = L.oIsU ? u1 : v1;
+			L.n0 = L.oIsU ? v0 : u0, L.n1 = L.oIsU ? v1 : u1;
+			L.start = per;
+			per += L.o1 - L.o0;
+		}
+	}
+	P.perFreq = per;
+	// device tables: wE[3], wH[3] (each over [lo, hi] of its axis), then the inner sums and the output
+	size_t innerFloats = (size_t)per * p->nfreq, outFloats = (size_t)p->nfreq * p->nface;
+	size_t bytes = (tabFloats + innerFloats + outFloats) * sizeof(float);
+	if (bytes > p->fluxTabBytes) {
+		ALIS_CUDA(cudaStreamSynchronize(st));
+		if (p->fluxTab) cudaFree(p->fluxTab);
+		p->fluxTab = 0, p->fluxTabBytes = 0;
+		ALIS_CUDA(cudaMalloc(&p->fluxTab, bytes));
+		p->fluxTabBytes = bytes;
+	}
+	float *tab = p->fluxTab;
+	const float *dE[3], *dH[3];
+	for (int a = 0; a < 3; a++) {
+		ALIS_CUDA(cudaMemcpyAsync(tab, wE[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, st));
+		dE[a] = tab - lo[a], tab += len[a];
+		ALIS_CUDA(cudaMemcpyAsync(tab, wH[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, st));
+		dH[a] = tab - lo[a], tab += len[a];
+	}
+	P.inner = tab, tab += innerFloats;
+	P.out = tab;
+	for (int l = 0; l < P.nloop; l++) {
+		FluxLoop &L = P.loop[l];
+		const alisgpu_face &fc = p->faces[L.face];
+		const int ua = fc.axis == 0 ? 1 : 0, va = fc.axis == 2 ? 1 : 2;
+		const int oa = L.oIsU ? ua : va, na = L.oIsU ? va : ua;
+		L.wN = dE[na], L.wO = dH[oa];
+	}
+	if (per > 0) {
+		long long threads = per * p->nfreq;
+		int slot = alisgpu__prof_start();
+		k_phaser_flux_inner<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(P);
+		k_phaser_flux_outer<<<(p->nfreq * p->nface + 127) / 128, 128, 0, st>>>(P);
+		alisgpu__prof_stop(slot, ALISGPU_K_FLUX);
+		alisgpu__count_launch();
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+		ALIS_CUDA(cudaMemcpyAsync(out, P.out, outFloats * sizeof(float), cudaMemcpyDeviceToHost, st));
+	} else {
+		memset(out, 0, outFloats * sizeof(float));
+	}
+	ALIS_CUDA(cudaStreamSynchronize(st));
 	return ALISGPU_OK;
 }
 

@@ -40,6 +40,12 @@ void alis_be_phaser_deleted(phaser P);
 /* Bring host mirrors of a phaser set's accumulators up to date.
  * P may point at any element of the set. */
 void alis_be_sync_phaser(phaser P);
+/* Poynting flux of each face of phaser P (xMin, xMax, yMin, yMax, zMin,
+ * zMax; 0 for a missing face) as fluxX/fluxY/fluxZ compute it.  Returns 0
+ * when the backend leaves the reduction to the host mirrors. */
+int alis_be_phaser_flux(phaser P, float face[6]);
+/* bring the host mirrors of every phaser set on W up to date */
+void alis_be_sync_phasers_of(world W);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

@@ -224,12 +224,19 @@ float phaserPoyntingIn(phaser P) { return -phaserPoyntingOut(P); }
 
 float phaserPoyntingOut(phaser P)
 {
-	alis_be_sync_phaser(P);
-	float Sum = 0;
+	float Sum = 0, face[6];
 	world W = P->W;
-	Sum += fluxX(P, P->xMax, P->iMax) - fluxX(P, P->xMin, P->iMin);
-	Sum += fluxY(P, P->yMax, P->jMax) - fluxY(P, P->yMin, P->jMin);
-	Sum += fluxZ(P, P->zMax, P->kMax) - fluxZ(P, P->zMin, P->kMin);
+	if (alis_be_phaser_flux(P, face)) {
+		/* the same face values, reduced where the accumulators live */
+		Sum += face[1] - face[0];
+		Sum += face[3] - face[2];
+		Sum += face[5] - face[4];
+	} else {
+		alis_be_sync_phaser(P);
+		Sum += fluxX(P, P->xMax, P->iMax) - fluxX(P, P->xMin, P->iMin);
+		Sum += fluxY(P, P->yMax, P->jMax) - fluxY(P, P->yMin, P->jMin);
+		Sum += fluxZ(P, P->zMax, P->kMax) - fluxZ(P, P->zMin, P->kMin);
+	}
 	if (W->Dom.x.Min==W->Dom.x.Max) Sum /= W->CH->dx[P->iMax]+W->CH->dx[P->iMax-1];
 	if (W->Dom.y.Min==W->Dom.y.Max) Sum /= W->CH->dy[P->jMax]+W->CH->dy[P->jMax-1];
 	if (W->Dom.z.Min==W->Dom.z.Max) Sum /= W->CH->dz[P->kMax]+W->CH->dz[P->kMax-1];

@@ -485,6 +485,7 @@ void deleteCloneWorld(world W)
 void alisSyncHost(world W)
 {
 	alis_be_sync_world(W);
+	alis_be_sync_phasers_of(W);
 }
 
 

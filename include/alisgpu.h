@@ -60,7 +60,8 @@ enum {
 	ALISGPU_K_FLUSH = 5,       /* phaser DFT flush */
 	ALISGPU_K_FARFIELD = 6,    /* FP64 far-field sums */
 	ALISGPU_K_STEP_AUX = 7,    /* half steps of small (TFSF auxiliary) worlds */
-	ALISGPU_K_KINDS = 8
+	ALISGPU_K_FLUX = 8,        /* phaser face fluxes */
+	ALISGPU_K_KINDS = 9
 };
 int alisgpu_profile(int enable);
 int alisgpu_profile_read(int kind, double *ms, unsigned long long *launches);
@@ -200,6 +201,14 @@ int alisgpu_phaser_flush(alisgpu_phaser *p);
  * interleaved complex host box array over the face box. */
 int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q, float *host);
 int alisgpu_phaser_zero(alisgpu_phaser *p);
+/* Poynting flux of every face at every frequency, out[f * nface + face]:
+ * the value the reference's fluxX/fluxY/fluxZ return for that face, with
+ * their float and double arithmetic in their order as one OpenMP thread
+ * runs it (reference src/phaser.c:142-219).  wE[a] / wH[a]: the E-grid and
+ * H-grid spacings (CE->dx, CH->dx, ...) of axis a over [lo[a], hi[a]], a
+ * box that holds every face.  Flushes the ring first. */
+int alisgpu_phaser_face_flux(alisgpu_phaser *p, const float *const wE[3], const float *const wH[3],
+                             const int lo[3], const int hi[3], float *out);
 
 /* ---- near-to-far-field sums in FP64 (reference src/farfld.c:248-459) ---- */
 

@@ -552,4 +552,6 @@ void alis_be_sync_world(world W) { (void)W; }
 void alis_be_phaser_created(phaser P) { (void)P; }
 void alis_be_phaser_deleted(phaser P) { (void)P; }
 void alis_be_sync_phaser(phaser P) { (void)P; }
+int alis_be_phaser_flux(phaser P, float face[6]) { (void)P; (void)face; return 0; }
+void alis_be_sync_phasers_of(world W) { (void)W; }
 void alis_be_sync_all(void) {}

@@ -116,6 +116,7 @@ static void dumpWorld(world W, const char *tag)
 static void dumpPhasers(phaser P, const char *tag)
 {
 	char nm[64];
+	if (alisSyncHost) alisSyncHost(P->W);
 	for (int n = 0; P[n].f; n++) {
 		phaser p = P + n;
 		snprintf(nm, 64, "%s.%d.flux", tag, n); dumpScalar(nm, phaserPoyntingOut(p));
