@@ -178,7 +178,14 @@ struct alisgpu_world {
 	size_t bytes;
 	unsigned short *cls[2][3];             // per-axis cell classes of the E / H step
 	std::vector<unsigned short> clsHost[2][3];
+	// ghost copies of the last E half step, not yet applied: they only
+	// write E's upper halo, which no half step reads, so they run once
+	// before the host reads E (same bytes: each copy is a function of the
+	// current interior E)
+	std::vector<alisgpu_ghost_copy> pendingE;
 };
+
+static int applyPendingGhosts(alisgpu_world *w);
 
 static Layout makeLayout(const alisgpu_geometry *g)
 {
@@ -280,6 +287,7 @@ extern "C" size_t alisgpu_world_bytes(const alisgpu_world *w) { return w ? w->by
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
 	fullJoin();
+	if (w) w->pendingE.clear();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_reset: null world");
 	size_t n = w->L.elems() * sizeof(float);
 	for (int m = 0; m <= w->g.complexField; m++) for (int c = 0; c < 3; c++) {
@@ -419,6 +427,10 @@ static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
 extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
 {
 	fullJoin();
+	if (w) {
+		int rc = applyPendingGhosts(w);
+		if (rc) return rc;
+	}
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_download: bad argument");
 	const Layout &L = w->L;
@@ -431,6 +443,7 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
 {
 	fullJoin();
+	if (w && field == 0) w->pendingE.clear();        // the host's halo wins
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_upload: bad argument");
 	const Layout &L = w->L;
@@ -844,20 +857,20 @@ struct GhostParams {
 	float *F[2][3];
 	int complexField;
 	alisgpu_ghost_copy c[ALIS_GHOST_GROUP];
-	long long start[ALIS_GHOST_GROUP + 1];
+	int start[ALIS_GHOST_GROUP + 1];         // below 2^31 (checked on the host)
 	unsigned int *err;
 };
 
 __global__ void k_ghost(const GhostParams P)
 {
-	long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= P.start[P.n]) return;
 	int q = 0;
 	while (t >= P.start[q + 1]) q++;
 	const alisgpu_ghost_copy &g = P.c[q];
-	long long r = t - P.start[q];
-	int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
-	int kk = (int)(r % nk), jj = (int)((r / nk) % nj), ii = (int)(r / ((long long)nk * nj));
+	const int r = t - P.start[q];
+	const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
+	const int kk = r % nk, jj = (r / nk) % nj, ii = r / (nk * nj);
 	int i = g.i0 + ii, j = g.j0 + jj, k = g.k0 + kk;
 	int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
 	if (i < P.L.i0 || i >= P.L.i0 + P.L.ni || j < P.L.j0 || j >= P.L.j0 + P.L.nj || k < P.L.k0 || k >= P.L.k0 + P.L.nk ||
@@ -995,6 +1008,55 @@ extern "C" void alisgpu__forget_tfsf(const alisgpu_tfsf *s)
 {
 	for (size_t q = 0; q < gTfsfCache.size();)
 		if (gTfsfCache[q].key == s) gTfsfCache.erase(gTfsfCache.begin() + q); else q++;
+}
+
+// ghost copies in list order; consecutive copies of distinct components
+// share a launch (reference src/update.c:182-191)
+static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, int n)
+{
+	const alisgpu_geometry &g = w->g;
+	int q = 0;
+	while (q < n) {
+		GhostParams GP;
+		memset(&GP, 0, sizeof GP);
+		GP.L = w->L;
+		GP.err = gErrWord;
+		GP.complexField = g.complexField;
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			GP.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		int used = 0;
+		long long total = 0;
+		while (q < n && GP.n < ALIS_GHOST_GROUP && !(used & (1 << gl[q].comp))) {
+			const alisgpu_ghost_copy &c = gl[q];
+			used |= 1 << c.comp;
+			GP.c[GP.n] = c;
+			long long cells = (c.i1 < c.i0 || c.j1 < c.j0 || c.k1 < c.k0) ? 0 :
+				(long long)(1 + c.i1 - c.i0) * (1 + c.j1 - c.j0) * (1 + c.k1 - c.k0);
+			total += cells;
+			if (total >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "ghost copies of %lld cells exceed 32-bit indexing", total);
+			GP.start[GP.n + 1] = (int)total;
+			GP.n++;
+			q++;
+		}
+		if (total > 0) {
+			int slot = alisgpu__prof_start();
+			k_ghost<<<(unsigned)((total + 255) / 256), 256, 0, gStream>>>(GP);
+			alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
+			alisgpu__count_launch();
+			ALIS_CUDA(cudaGetLastError());
+		}
+	}
+	return ALISGPU_OK;
+}
+
+static int applyPendingGhosts(alisgpu_world *w)
+{
+	if (w->pendingE.empty()) return ALISGPU_OK;
+	int rc = runGhosts(w, 0, w->pendingE.data(), (int)w->pendingE.size());
+	w->pendingE.clear();
+	return rc;
 }
 
 extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s)
@@ -1177,37 +1239,12 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		ALIS_CUDA(cudaGetLastError());
 	}
 
-	// ghost copies: consecutive copies of distinct components share a launch
-	int q = 0;
-	while (q < s->nghost) {
-		GhostParams GP;
-		memset(&GP, 0, sizeof GP);
-		GP.L = w->L;
-		GP.err = gErrWord;
-		GP.complexField = g.complexField;
-		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
-			int mm = m <= g.complexField ? m : 0;
-			GP.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
-		}
-		int used = 0;
-		while (q < s->nghost && GP.n < ALIS_GHOST_GROUP && !(used & (1 << s->ghost[q].comp))) {
-			const alisgpu_ghost_copy &c = s->ghost[q];
-			used |= 1 << c.comp;
-			GP.c[GP.n] = c;
-			long long cells = (c.i1 < c.i0 || c.j1 < c.j0 || c.k1 < c.k0) ? 0 :
-				(long long)(1 + c.i1 - c.i0) * (1 + c.j1 - c.j0) * (1 + c.k1 - c.k0);
-			GP.start[GP.n + 1] = GP.start[GP.n] + cells;
-			GP.n++;
-			q++;
-		}
-		long long total = GP.start[GP.n];
-		if (total > 0) {
-			int slot = alisgpu__prof_start();
-			k_ghost<<<(unsigned)((total + 255) / 256), 256, 0, gStream>>>(GP);
-			alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
-			alisgpu__count_launch();
-			ALIS_CUDA(cudaGetLastError());
-		}
+	// ghost copies: E's wait for the next host read, H's run now
+	if (field == 0) {
+		w->pendingE.assign(s->ghost, s->ghost + s->nghost);
+	} else {
+		int rc = runGhosts(w, 1, s->ghost, s->nghost);
+		if (rc) return rc;
 	}
 	ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
 	gMainRec[field] = 1;
