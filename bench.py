@@ -37,7 +37,9 @@ sys.path.insert(0, ROOT)
 
 HALF = 230          # domain half size in nm: 256^3 cells with the CPML
 NFREQ = 64
-WORKLOAD = "dispersive scatterer 256^3 (gold Drude+2CP, TFSF, CPML 12, 64-f box phasers)"
+def workload(cells):
+    n = round(cells ** (1 / 3))
+    return "dispersive scatterer %d^3 (gold Drude+2CP, TFSF, CPML 12, 64-f box phasers)" % n
 
 
 def env_rank():
@@ -169,14 +171,14 @@ def reference_arm(args, rank, world):
     if rank != 0:
         return
     # bounded sample: at most 32 timed and 3 warm-up steps of the full world
-    cpu = run_cpu(HALF, min(max(args.steps, 1), 32), min(args.warmup, 3))
+    cpu = run_cpu(args.half, min(max(args.steps, 1), 32), min(args.warmup, 3))
     rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
     sample = "%d timed steps (after %d warm-up) of the full %d^3-cell world" % (cpu["steps"], min(args.warmup, 3), round(cpu["cells"] ** (1 / 3)))
     line = {
         "impl": "reference", "metric": "Gcell-updates/s", "value": rate, "unit": "Gcell/s", "n_gpus": args.gpus,
         "steps": cpu["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * cpu["seconds"] / cpu["steps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": cpu["cells"], "parallelism": "host cores (OpenMP)"},
+        "config": {"workload": workload(cpu["cells"]), "cells": cpu["cells"], "parallelism": "host cores (OpenMP)"},
         "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
                          "sample": sample},
         "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -199,7 +201,7 @@ def engine_arm(args, rank, world, local):
     eng.alisgpu_launch_count.restype = ctypes.c_ulonglong
     cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
 
-    cells = lib.c2_build(HALF, NFREQ)
+    cells = lib.c2_build(args.half, NFREQ)
     stream = ctypes.c_void_p(eng.alisgpu_stream())
     ev0, ev1 = ctypes.c_void_p(), ctypes.c_void_p()
     cudart.cudaEventCreate(ctypes.byref(ev0))
@@ -251,7 +253,7 @@ def engine_arm(args, rank, world, local):
     total_ms = sum(t for t, _ in kinds.values())
     cpu_baseline = None
     if args.cpu_steps > 0:
-        cpu = run_cpu(HALF, args.cpu_steps, 1)
+        cpu = run_cpu(args.half, args.cpu_steps, 1)
         cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
         cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
                         "sample": "%d steps of the full world after 1 warm-up step (oracle restatement, OpenMP)" % cpu["steps"]}
@@ -260,7 +262,7 @@ def engine_arm(args, rank, world, local):
         "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": dev_s * 1e3 / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
+        "config": {"workload": workload(cells), "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
                    "phaser": "64 frequencies, time-blocked ring of %s steps" % os.environ.get("ALISGPU_PHASER_RING", "64")},
         "e2e": {"value": cells * K * world / e2e_s / 1e9, "unit": "Gcell/s",
@@ -286,6 +288,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4, help="steps of the CPU baseline sample (0: skip it)")
+    ap.add_argument("--half", type=int, default=HALF, help="domain half size in nm (230: the 256^3 workload)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
