@@ -188,6 +188,8 @@ def reference_arm(args, rank, world):
 
 def engine_arm(args, rank, world, local):
     os.environ.setdefault("ALISGPU_DEVICE", str(local))
+    # the workload's phasers accumulate with compensated (Kahan) sums
+    os.environ.setdefault("ALISGPU_PHASER_KAHAN", "1")
     so = build_bench_lib()
     import alis_gb300
     eng = alis_gb300.library()
@@ -264,7 +266,9 @@ def engine_arm(args, rank, world, local):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload(cells), "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
-                   "phaser": "64 frequencies, time-blocked ring of %s steps" % os.environ.get("ALISGPU_PHASER_RING", "64")},
+                   "phaser": "64 frequencies, %s, time-blocked ring of %s steps" % (
+                       "Kahan-compensated" if os.environ.get("ALISGPU_PHASER_KAHAN") == "1" else "plain float sums",
+                       os.environ.get("ALISGPU_PHASER_RING", "64"))},
         "e2e": {"value": cells * K * world / e2e_s / 1e9, "unit": "Gcell/s",
                 "h2d_bytes_per_step": lib.c2_step_h2d_bytes(),
                 "d2h_bytes_per_step": lib.c2_result_d2h_bytes() / K},

@@ -302,10 +302,57 @@ void updateH(world W)
 
 /* --- running DFT on phaser faces (reference src/phaser.c:83-110) --- */
 
+/* FP64 accumulation (environment ALIS_ORACLE_DFT64=1): the same float
+ * fields and float phase factors, summed in double complex in shadow
+ * arrays; alis_be_sync_phasers_of rounds them into the face arrays.  The
+ * GPU's compensated (Kahan) accumulation is judged against it. */
+typedef struct Shadow {
+	float complex ***A;
+	int i0, j0, k0, ni, nj, nk;
+	double complex *v;
+	struct Shadow *next;
+} Shadow;
+static Shadow *shadows;
+static int dft64 = -1;
+
+static double complex *shadowOf(float complex ***A, int i0, int i1, int j0, int j1, int k0, int k1)
+{
+	for (Shadow *s = shadows; s; s = s->next) if (s->A == A) return s->v;
+	Shadow *s = calloc(1, sizeof *s);
+	s->A = A, s->i0 = i0, s->j0 = j0, s->k0 = k0, s->ni = 1 + i1 - i0, s->nj = 1 + j1 - j0, s->nk = 1 + k1 - k0;
+	s->v = calloc((size_t)(1 + i1 - i0) * s->nj * s->nk, sizeof(double complex));
+	s->next = shadows;
+	shadows = s;
+	return s->v;
+}
+
+static void dftFace64(cfield *c, float ***e1, float ***e2, float ***h1, float ***h2,
+                      float complex pE, float complex pH, int axis, int i0, int i1, int j0, int j1, int k0, int k1)
+{
+	float complex ***E1, ***E2, ***H1, ***H2;
+	if (axis == 0) E1 = c->Ey, E2 = c->Ez, H1 = c->Hy, H2 = c->Hz;
+	else if (axis == 1) E1 = c->Ez, E2 = c->Ex, H1 = c->Hz, H2 = c->Hx;
+	else E1 = c->Ex, E2 = c->Ey, H1 = c->Hx, H2 = c->Hy;
+	if (!(E1 && E2 && H1 && H2)) return;
+	double complex *s1 = shadowOf(E1, i0, i1, j0, j1, k0, k1), *s2 = shadowOf(E2, i0, i1, j0, j1, k0, k1);
+	double complex *s3 = shadowOf(H1, i0, i1, j0, j1, k0, k1), *s4 = shadowOf(H2, i0, i1, j0, j1, k0, k1);
+	int di = axis==0, dj = axis==1, dk = axis==2, nj = 1 + j1 - j0, nk = 1 + k1 - k0;
+	double complex qE = pE, qH = pH;
+	for (int i = i0; i <= i1; i++) for (int j = j0; j <= j1; j++) for (int k = k0; k <= k1; k++) {
+		size_t o = ((size_t)(i - i0) * nj + (j - j0)) * nk + (k - k0);
+		s1[o] += qE * (double)e1[i][j][k];
+		s2[o] += qE * (double)e2[i][j][k];
+		s3[o] += qH * ((double)h1[i][j][k] + (double)h1[i+di][j+dj][k+dk]) * 0.5;
+		s4[o] += qH * ((double)h2[i][j][k] + (double)h2[i+di][j+dj][k+dk]) * 0.5;
+	}
+}
+
 static void dftFace(world W, cfield *c, float ***e1, float ***e2, float ***h1, float ***h2,
                     float complex pE, float complex pH, int axis, int i0, int i1, int j0, int j1, int k0, int k1)
 {
 	if (!(c->Ex || c->Ey || c->Ez)) return;
+	if (dft64 < 0) { const char *e = getenv("ALIS_ORACLE_DFT64"); dft64 = e && e[0] == '1'; }
+	if (dft64) { dftFace64(c, e1, e2, h1, h2, pE, pH, axis, i0, i1, j0, j1, k0, k1); return; }
 	float complex ***E1, ***E2, ***H1, ***H2;
 	if (axis == 0) E1 = c->Ey, E2 = c->Ez, H1 = c->Hy, H2 = c->Hz;
 	else if (axis == 1) E1 = c->Ez, E2 = c->Ex, H1 = c->Hz, H2 = c->Hx;
@@ -553,5 +600,13 @@ void alis_be_phaser_created(phaser P) { (void)P; }
 void alis_be_phaser_deleted(phaser P) { (void)P; }
 void alis_be_sync_phaser(phaser P) { (void)P; }
 int alis_be_phaser_flux(phaser P, float face[6]) { (void)P; (void)face; return 0; }
-void alis_be_sync_phasers_of(world W) { (void)W; }
+void alis_be_sync_phasers_of(world W)
+{
+	/* FP64 mode: the double sums rounded into the face arrays */
+	(void)W;
+	for (Shadow *s = shadows; s; s = s->next)
+		for (int i = s->i0; i < s->i0 + s->ni; i++)
+			for (int j = s->j0; j < s->j0 + s->nj; j++) for (int k = s->k0; k < s->k0 + s->nk; k++)
+				s->A[i][j][k] = (float complex)s->v[((size_t)(i - s->i0) * s->nj + (j - s->j0)) * s->nk + (k - s->k0)];
+}
 void alis_be_sync_all(void) {}

@@ -40,8 +40,13 @@ def binary(against):
     elif against == "reference":
         if build.build_reference() is None:
             return None
-    if not os.path.exists(out) or os.path.getmtime(out) < max(
-            os.path.getmtime(DRIVER), os.path.getmtime(os.path.join(ROOT, "tests", "drivers", "dump.h"))):
+    deps = [DRIVER, os.path.join(ROOT, "tests", "drivers", "dump.h")]
+    lib = {"engine": os.path.join(build.LIB, "libalis_gb300.so"),
+           "oracle": os.path.join(build.ORACLE_BUILD, "liboracle_alis.a"),
+           "reference": os.path.join(build.ORACLE, "_ref", "libalis_ref.a")}[against]
+    if os.path.exists(lib):
+        deps.append(lib)
+    if not os.path.exists(out) or os.path.getmtime(out) < max(os.path.getmtime(d) for d in deps):
         build.link_program(DRIVER, out, against)
     return out
 

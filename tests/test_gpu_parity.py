@@ -56,3 +56,30 @@ def test_engine_matches_reference_fixture(scene, scale, steps):
         scale_ = max(g["l1"], 1e-30)
         assert abs(s["l1"] - g["l1"]) <= 1e-5 * scale_, (name, s["l1"], g["l1"])
     assert exact > 0
+
+
+def _rel_l1(a, b, keys):
+    num = sum(np.abs(a[k].astype(np.complex128) - b[k].astype(np.complex128)).sum() for k in keys)
+    den = sum(np.abs(b[k].astype(np.complex128)).sum() for k in keys)
+    return num / den
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale,steps", [("c1", 1, 600), ("c2", 1, 200)], ids=["c1-600", "c2-200"])
+def test_kahan_phasers_against_fp64_accumulation(scene, scale, steps):
+    """Compensated phaser accumulation (ALISGPU_PHASER_KAHAN=1) against the
+    oracle's FP64 accumulation of the same float fields and phase factors:
+    at most 1e-6 relative (L1 over every face array), never further than
+    the reference's plain float sums; fluxes within 1e-5 relative."""
+    gpu = scenes.run("engine", scene, scale, steps, env={"ALISGPU_PHASER_KAHAN": "1"})
+    plain = scenes.run("oracle", scene, scale, steps)
+    wide = scenes.run("oracle", scene, scale, steps, env={"ALIS_ORACLE_DFT64": "1"})
+    faces = [k for k in wide if k.startswith("P.") and k.count(".") == 3 and k.split(".")[3][0] in "EH"]
+    assert faces
+    err_k, err_p = _rel_l1(gpu, wide, faces), _rel_l1(plain, wide, faces)
+    print("phaser error vs FP64: kahan %.3e plain %.3e" % (err_k, err_p))
+    assert err_k <= 1e-6 and err_k <= err_p, (err_k, err_p)
+    for k in wide:
+        if k.endswith(".flux"):
+            x, y = float(gpu[k].reshape(-1)[0]), float(wide[k].reshape(-1)[0])
+            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-30), (k, x, y)
