@@ -86,6 +86,7 @@ __device__ __forceinline__ float addHalf(float a, float p)
 
 #define FLUSH_THREADS 128
 #define FLUSH_FREQ 8
+#define FLUSH_SUB 8                              // ring steps per compensated add
 
 // thread = one (face cell, component); loops over a chunk of frequencies
 template <bool KAHAN>
@@ -106,26 +107,47 @@ __global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf
 	float2 a[FLUSH_FREQ], cc[FLUSH_FREQ];
 #pragma unroll
 	for (int ff = 0; ff < FLUSH_FREQ; ff++) {
+		a[ff] = cc[ff] = make_float2(0, 0);
 		if (ff < nf) {
 			a[ff] = acc[(long long)(f0 + ff) * n4 + t];
-			cc[ff] = KAHAN ? comp[(long long)(f0 + ff) * n4 + t] : make_float2(0, 0);
+			if (KAHAN) cc[ff] = comp[(long long)(f0 + ff) * n4 + t];
 		}
 	}
-	for (int s = 0; s < steps; s++) {
-		const float x = buf[(long long)s * n4 + t];
+	if (!KAHAN) {
+		// the reference's sums, term by term in its rounding
+		for (int s = 0; s < steps; s++) {
+			const float x = buf[(long long)s * n4 + t];
 #pragma unroll
-		for (int ff = 0; ff < FLUSH_FREQ; ff++) {
-			if (ff >= nf) break;
-			const float2 p = sph[(s * FLUSH_FREQ + ff) * 2 + (isH ? 1 : 0)];
-			const float pr = p.x * x, pi = p.y * x;
-			if (!KAHAN) {
+			for (int ff = 0; ff < FLUSH_FREQ; ff++) {
+				if (ff >= nf) break;
+				const float2 p = sph[(s * FLUSH_FREQ + ff) * 2 + (isH ? 1 : 0)];
+				const float pr = p.x * x, pi = p.y * x;
 				if (isH) a[ff].x = addHalf(a[ff].x, pr), a[ff].y = addHalf(a[ff].y, pi);
 				else a[ff].x = a[ff].x + pr, a[ff].y = a[ff].y + pi;
-			} else {
-				// Kahan: y = term - c; s' = s + y; c = (s' - s) - y
-				float yr = (isH ? pr * 0.5f : pr) - cc[ff].x, yi = (isH ? pi * 0.5f : pi) - cc[ff].y;
-				float sr = a[ff].x + yr, sI = a[ff].y + yi;
-				cc[ff].x = (sr - a[ff].x) - yr, cc[ff].y = (sI - a[ff].y) - yi;
+			}
+		}
+	} else {
+		// compensated: the terms of FLUSH_SUB steps summed with fused
+		// multiply-adds, then one Kahan step (y = part - c; s' = s + y;
+		// c = (s' - s) - y) per frequency
+		for (int s0 = 0; s0 < steps; s0 += FLUSH_SUB) {
+			float2 part[FLUSH_FREQ];
+#pragma unroll
+			for (int ff = 0; ff < FLUSH_FREQ; ff++) part[ff] = make_float2(0, 0);
+			const int s1 = min(s0 + FLUSH_SUB, steps);
+			for (int s = s0; s < s1; s++) {
+				const float x = isH ? 0.5f * buf[(long long)s * n4 + t] : buf[(long long)s * n4 + t];
+#pragma unroll
+				for (int ff = 0; ff < FLUSH_FREQ; ff++) {
+					const float2 p = sph[(s * FLUSH_FREQ + ff) * 2 + (isH ? 1 : 0)];
+					part[ff].x = __fmaf_rn(p.x, x, part[ff].x), part[ff].y = __fmaf_rn(p.y, x, part[ff].y);
+				}
+			}
+#pragma unroll
+			for (int ff = 0; ff < FLUSH_FREQ; ff++) {
+				const float yr = __fsub_rn(part[ff].x, cc[ff].x), yi = __fsub_rn(part[ff].y, cc[ff].y);
+				const float sr = __fadd_rn(a[ff].x, yr), sI = __fadd_rn(a[ff].y, yi);
+				cc[ff].x = __fsub_rn(__fsub_rn(sr, a[ff].x), yr), cc[ff].y = __fsub_rn(__fsub_rn(sI, a[ff].y), yi);
 				a[ff].x = sr, a[ff].y = sI;
 			}
 		}
