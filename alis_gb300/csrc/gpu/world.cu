@@ -18,7 +18,10 @@
 #include <cstring>
 #include <cstdlib>
 #include <vector>
+#include <algorithm>
+#include <cooperative_groups.h>
 #include "common.cuh"
+namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------
 // process-wide state: device, stream, error text, launch counter
@@ -861,32 +864,71 @@ struct GhostParams {
 	unsigned int *err;
 };
 
+// one cell of ghost copy g: F = cos F' + sin G', G = cos G' - sin F'
+// (G the imaginary set of a complex field), F = cos F' otherwise
+__device__ __forceinline__ void ghostCell(const Layout &L, float *const F2[2][3], int complexField, const alisgpu_ghost_copy &g,
+                                          int r, unsigned int *err)
+{
+	const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
+	const int kk = r % nk, jj = (r / nk) % nj, ii = r / (nk * nj);
+	const int i = g.i0 + ii, j = g.j0 + jj, k = g.k0 + kk;
+	const int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
+	if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk ||
+	    si < L.i0 || si >= L.i0 + L.ni || sj < L.j0 || sj >= L.j0 + L.nj || sk < L.k0 || sk >= L.k0 + L.nk) {
+		atomicOr(err, 2u);
+		return;
+	}
+	const long long d = L.at(i, j, k), s = L.at(si, sj, sk);
+	float *F = F2[0][g.comp];
+	if (complexField) {
+		float *G = F2[1][g.comp];
+		const float f = F[s], gg = G[s];
+		F[d] = g.cosk * f + g.sink * gg;
+		G[d] = g.cosk * gg - g.sink * f;
+	} else {
+		F[d] = g.cosk * F[s];
+	}
+}
+
 __global__ void k_ghost(const GhostParams P)
 {
 	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= P.start[P.n]) return;
 	int q = 0;
 	while (t >= P.start[q + 1]) q++;
-	const alisgpu_ghost_copy &g = P.c[q];
-	const int r = t - P.start[q];
-	const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
-	const int kk = r % nk, jj = (r / nk) % nj, ii = r / (nk * nj);
-	int i = g.i0 + ii, j = g.j0 + jj, k = g.k0 + kk;
-	int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
-	if (i < P.L.i0 || i >= P.L.i0 + P.L.ni || j < P.L.j0 || j >= P.L.j0 + P.L.nj || k < P.L.k0 || k >= P.L.k0 + P.L.nk ||
-	    si < P.L.i0 || si >= P.L.i0 + P.L.ni || sj < P.L.j0 || sj >= P.L.j0 + P.L.nj || sk < P.L.k0 || sk >= P.L.k0 + P.L.nk) {
-		atomicOr(P.err, 2u);
-		return;
-	}
-	long long d = P.L.at(i, j, k), s = P.L.at(si, sj, sk);
-	float *F = P.F[0][g.comp];
-	if (P.complexField) {
-		float *G = P.F[1][g.comp];
-		float f = F[s], gg = G[s];
-		F[d] = g.cosk * f + g.sink * gg;
-		G[d] = g.cosk * gg - g.sink * f;
-	} else {
-		F[d] = g.cosk * F[s];
+	ghostCell(P.L, P.F, P.complexField, P.c[q], t - P.start[q], P.err);
+}
+
+// All ghost copies of a half step in one cooperative launch: the host
+// sorts the copies into dependency levels (a copy follows every earlier
+// copy of the same component whose boxes it reads after, writes after or
+// overwrites); copies of one level are independent and run together, and
+// a grid-wide barrier separates the levels.  The driver guarantees that
+// all blocks of a cooperative launch are resident, so the barrier ends.
+#define ALIS_GHOST_MAX 48
+struct GhostLevels {
+	Layout L;
+	float *F[2][3];
+	int complexField;
+	int n, nlev;
+	alisgpu_ghost_copy c[ALIS_GHOST_MAX];     // in level order
+	int start[ALIS_GHOST_MAX + 1];            // first cell of each copy (below 2^31)
+	int levStart[ALIS_GHOST_MAX + 1];         // first copy of each level
+	unsigned int *err;
+};
+
+__global__ void __launch_bounds__(256) k_ghost_levels(const __grid_constant__ GhostLevels P)
+{
+	cg::grid_group grid = cg::this_grid();
+	const int stride = gridDim.x * blockDim.x;
+	for (int l = 0; l < P.nlev; l++) {
+		const int q0 = P.levStart[l], q1 = P.levStart[l + 1];
+		for (int t = P.start[q0] + blockIdx.x * blockDim.x + threadIdx.x; t < P.start[q1]; t += stride) {
+			int q = q0;
+			while (t >= P.start[q + 1]) q++;
+			ghostCell(P.L, P.F, P.complexField, P.c[q], t - P.start[q], P.err);
+		}
+		if (l + 1 < P.nlev) grid.sync();
 	}
 }
 
@@ -1012,9 +1054,75 @@ extern "C" void alisgpu__forget_tfsf(const alisgpu_tfsf *s)
 
 // ghost copies in list order; consecutive copies of distinct components
 // share a launch (reference src/update.c:182-191)
+static bool boxesMeet(const int a[6], const int b[6])
+{
+	return a[0] <= b[1] && b[0] <= a[1] && a[2] <= b[3] && b[2] <= a[3] && a[4] <= b[5] && b[4] <= a[5];
+}
+
 static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, int n)
 {
 	const alisgpu_geometry &g = w->g;
+	if (n <= 0) return ALISGPU_OK;
+	if (n <= ALIS_GHOST_MAX) {
+		// dependency levels: written box W, read box R = W shifted
+		int lev[ALIS_GHOST_MAX], nlev = 0;
+		long long cells[ALIS_GHOST_MAX], total = 0;
+		for (int q = 0; q < n; q++) {
+			const alisgpu_ghost_copy &c = gl[q];
+			const int Wq[6] = { c.i0, c.i1, c.j0, c.j1, c.k0, c.k1 };
+			const int Rq[6] = { c.i0 + c.di, c.i1 + c.di, c.j0 + c.dj, c.j1 + c.dj, c.k0 + c.dk, c.k1 + c.dk };
+			cells[q] = (c.i1 < c.i0 || c.j1 < c.j0 || c.k1 < c.k0) ? 0 : (long long)(1 + c.i1 - c.i0) * (1 + c.j1 - c.j0) * (1 + c.k1 - c.k0);
+			total += cells[q];
+			lev[q] = 0;
+			for (int p = 0; p < q; p++) {
+				const alisgpu_ghost_copy &e = gl[p];
+				if (e.comp != c.comp || !cells[p] || !cells[q]) continue;
+				const int Wp[6] = { e.i0, e.i1, e.j0, e.j1, e.k0, e.k1 };
+				const int Rp[6] = { e.i0 + e.di, e.i1 + e.di, e.j0 + e.dj, e.j1 + e.dj, e.k0 + e.dk, e.k1 + e.dk };
+				if (boxesMeet(Wp, Rq) || boxesMeet(Wp, Wq) || boxesMeet(Rp, Wq)) lev[q] = std::max(lev[q], lev[p] + 1);
+			}
+			nlev = std::max(nlev, lev[q] + 1);
+		}
+		if (total >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "ghost copies of %lld cells exceed 32-bit indexing", total);
+		if (total == 0) return ALISGPU_OK;
+		static GhostLevels GL;
+		memset(&GL, 0, sizeof GL);
+		GL.L = w->L;
+		GL.err = gErrWord;
+		GL.complexField = g.complexField;
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			GL.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		int at = 0;
+		for (int l = 0; l < nlev; l++) {
+			GL.levStart[l] = GL.n;
+			for (int q = 0; q < n; q++) if (lev[q] == l) {
+				GL.c[GL.n] = gl[q];
+				GL.start[GL.n] = at;
+				at += (int)cells[q];
+				GL.n++;
+			}
+		}
+		GL.levStart[nlev] = GL.n;
+		GL.start[GL.n] = at;
+		GL.nlev = nlev;
+		static int blocksMax;
+		if (!blocksMax) {
+			int dev = 0, sms = 0, per = 0;
+			ALIS_CUDA(cudaGetDevice(&dev));
+			ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+			ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ghost_levels, 256, 0));
+			blocksMax = std::max(1, sms * std::min(per, 2));
+		}
+		const int blocks = (int)std::min<long long>((total + 255) / 256, blocksMax);
+		void *args[] = { (void *)&GL };
+		int slot = alisgpu__prof_start();
+		ALIS_CUDA(cudaLaunchCooperativeKernel((const void *)k_ghost_levels, dim3(blocks), dim3(256), args, 0, gStream));
+		alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
+		alisgpu__count_launch();
+		return ALISGPU_OK;
+	}
 	int q = 0;
 	while (q < n) {
 		GhostParams GP;
