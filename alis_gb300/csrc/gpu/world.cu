@@ -84,7 +84,10 @@ extern "C" int alisgpu_init(void)
 	int dev = env ? atoi(env) : 0;
 	ALIS_CUDA(cudaSetDevice(dev));
 	ALIS_CUDA(cudaStreamCreateWithFlags(&gStream, cudaStreamNonBlocking));
-	ALIS_CUDA(cudaStreamCreateWithFlags(&gSide, cudaStreamNonBlocking));
+	// the side stream's small blocks take the first free slots
+	int prLeast = 0, prGreatest = 0;
+	ALIS_CUDA(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
+	ALIS_CUDA(cudaStreamCreateWithPriority(&gSide, cudaStreamNonBlocking, prGreatest));
 	for (int f = 0; f < 2; f++) {
 		ALIS_CUDA(cudaEventCreateWithFlags(&gEvMainDone[f], cudaEventDisableTiming));
 		ALIS_CUDA(cudaEventCreateWithFlags(&gEvAuxDone[f], cudaEventDisableTiming));
@@ -936,7 +939,8 @@ __global__ void __launch_bounds__(256) k_ghost_levels(const __grid_constant__ Gh
 // half step -- every cell of every m, then the source patches in list
 // order, then the ghost copies one after another -- in one block, with a
 // barrier between the dependent phases.  Same per-cell code as the large
-// path; one launch instead of one per phase and ghost group.
+// path; one launch instead of one per phase and ghost group.  The block
+// is small so that it finds room beside a running large-world kernel.
 #define ALIS_SMALL_CELLS 65536
 #define ALIS_SMALL_GHOSTS 48
 struct SmallStepParams {
@@ -949,8 +953,9 @@ struct SmallStepParams {
 	float v[ALIS_MAXSRCV];
 };
 
+#define SMALL_THREADS 128
 template <int ALT>
-__global__ void __launch_bounds__(1024) k_small_step(const __grid_constant__ SmallStepParams S)
+__global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_constant__ SmallStepParams S)
 {
 	const Layout &L = S.P[0].L;
 	for (int m = 0; m < S.nm; m++) {
@@ -1113,7 +1118,7 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 			ALIS_CUDA(cudaGetDevice(&dev));
 			ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 			ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ghost_levels, 256, 0));
-			blocksMax = std::max(1, sms * std::min(per, 2));
+			blocksMax = std::max(1, sms * per);
 		}
 		const int blocks = (int)std::min<long long>((total + 255) / 256, blocksMax);
 		void *args[] = { (void *)&GL };
@@ -1276,8 +1281,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			}
 		}
 		int slot = alisgpu__prof_start();
-		if (field == 0) k_small_step<1><<<1, 1024, 0, st>>>(S);
-		else k_small_step<-1><<<1, 1024, 0, st>>>(S);
+		if (field == 0) k_small_step<1><<<1, SMALL_THREADS, 0, st>>>(S);
+		else k_small_step<-1><<<1, SMALL_THREADS, 0, st>>>(S);
 		alisgpu__prof_stop(slot, ALISGPU_K_STEP_AUX);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
