@@ -26,6 +26,9 @@ CASES = [
     # rows longer than one warp's 128 cells, with a ragged float4 at the end
     ("c2", 2, 30),
     ("c1", 3, 40),
+    # the vacuum plane-wave workload at its lateral size (128 x 128 cells,
+    # periodic), a longer run
+    ("c1", 4, 400),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
