@@ -487,6 +487,19 @@ void alis_be_sync_phaser(phaser P)
 	if (d && d->hostStale) downloadPhaser(d);
 }
 
+int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, int vHi, float *out)
+{
+	devWorld *d = findWorld(W);
+	if (!d) return 0;
+	if (d->objectsDirty) uploadObjects(d);
+	const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
+	float *dE[3] = { W->CE->dx, W->CE->dy, W->CE->dz }, *dH[3] = { W->CH->dx, W->CH->dy, W->CH->dz };
+	int lo[2] = { uLo, vLo }, hi[2] = { uHi, vHi };
+	const float *wE[2] = { &dE[ua][uLo], &dE[va][vLo] }, *wH[2] = { &dH[ua][uLo], &dH[va][vLo] };
+	CHECK("plane_flux", alisgpu_plane_flux(d->dw, axis, pos, lo, hi, wE, wH, out));
+	return 1;
+}
+
 void alis_be_sync_phasers_of(world W)
 {
 	for (devPhaser *d = phasers; d; d = d->next) if (d->P->W == W && d->hostStale) downloadPhaser(d);

@@ -189,6 +189,8 @@ struct alisgpu_world {
 	// before the host reads E (same bytes: each copy is a function of the
 	// current interior E)
 	std::vector<alisgpu_ghost_copy> pendingE;
+	float *planeTab;                       // spacing tables and result of the plane-flux kernel
+	size_t planeTabFloats;
 };
 
 static int applyPendingGhosts(alisgpu_world *w);
@@ -276,6 +278,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 		if (w->H[m][c]) cudaFree(w->H[m][c]);
 	}
 	for (int c = 0; c < 3; c++) if (w->C[c]) cudaFree(w->C[c]);
+	if (w->planeTab) cudaFree(w->planeTab);
 	for (int grid = 0; grid < 2; grid++) {
 		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) cudaFree(w->dtd[grid][c]);
 		for (int c = 0; c < 9; c++) if (w->cp[grid][c]) cudaFree(w->cp[grid][c]);
@@ -1361,6 +1364,129 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	}
 	ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
 	gMainRec[field] = 1;
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
+// Instantaneous Poynting flux through an axis-normal plane (reference
+// src/output.c:233-356) with the reference's arithmetic in its order as
+// one OpenMP thread runs it: two sums, each an outer loop over one
+// in-plane index of (H-grid spacing x inner sum), the inner sum over the
+// other index with half-weight edge terms in double and float interior
+// terms; H is averaged across the plane.  One block: its threads compute
+// the inner sums, one thread adds the outer loops in order.
+// ---------------------------------------------------------------------
+struct PlaneParams {
+	Layout L;
+	const float *E[3], *H[3];
+	int axis, pos;
+	int lo[2], hi[2];                          // in-plane axes u < v
+	const float *wE[2], *wH[2];                // spacings over [lo, hi], indexed by index
+	float *out;
+};
+
+__global__ void __launch_bounds__(256) k_plane_flux(const PlaneParams P)
+{
+	extern __shared__ float inner[];
+	const int a = P.axis;
+	const int n1 = P.hi[a == 1 ? 1 : 0] - P.lo[a == 1 ? 1 : 0];   // outer count of the first loop
+	for (int l = 0; l < 2; l++) {
+		// x plane (u=j, v=k): Ey (Hz) over k for each j, then -Ez (Hy) over j for each k;
+		// y plane (u=i, v=k): Ez (Hx) over i for each k, then -Ex (Hz) over k for each i;
+		// z plane (u=i, v=j): Ex (Hy) over j for each i, then -Ey (Hx) over i for each j
+		const int oAx = (a == 1) == (l == 0) ? 1 : 0;               // index of the outer in-plane axis
+		const int nAx = 1 - oAx;
+		const int ec = a == 0 ? (l == 0 ? 1 : 2) : a == 1 ? (l == 0 ? 2 : 0) : (l == 0 ? 0 : 1);
+		const int hc = a == 0 ? (l == 0 ? 2 : 1) : a == 1 ? (l == 0 ? 0 : 2) : (l == 0 ? 1 : 0);
+		const int o0 = P.lo[oAx], o1 = P.hi[oAx], m0 = P.lo[nAx], m1 = P.hi[nAx];
+		const float *wN = P.wE[nAx];
+		const float *Ec = P.E[ec], *Hc = P.H[hc];
+		const long long dn = a == 0 ? P.L.si : a == 1 ? P.L.sj : 1;  // H across the plane
+		for (int t = threadIdx.x; t < o1 - o0; t += blockDim.x) {
+			const int o = o0 + 1 + t;
+			auto cell = [&](int n) -> long long {
+				const int u = oAx == 0 ? o : n, v = oAx == 0 ? n : o;
+				return a == 0 ? P.L.at(P.pos, u, v) : a == 1 ? P.L.at(u, P.pos, v) : P.L.at(u, v, P.pos);
+			};
+			float sum = 0;
+			for (int e = 0; e < 2; e++) {
+				const int n = e ? m1 : m0;
+				const long long c = cell(n);
+				const double hw = 0.5 * (double)wN[n];
+				const double term = __dmul_rn(hw * (double)Ec[c], (double)__fadd_rn(Hc[c], Hc[c + dn]));
+				sum = __double2float_rn(l == 0 ? __dadd_rn((double)sum, term) : __dsub_rn((double)sum, term));
+			}
+			for (int n = m0 + 1; n < m1; n++) {
+				const long long c = cell(n);
+				const float term = __fmul_rn(__fmul_rn(wN[n], Ec[c]), __fadd_rn(Hc[c], Hc[c + dn]));
+				sum = l == 0 ? __fadd_rn(sum, term) : __fsub_rn(sum, term);
+			}
+			inner[(l == 0 ? 0 : n1) + t] = sum;
+		}
+	}
+	__syncthreads();
+	if (threadIdx.x) return;
+	float Sum = 0, Part = 0;
+	for (int l = 0; l < 2; l++) {
+		const int oAx = (a == 1) == (l == 0) ? 1 : 0;
+		const int o0 = P.lo[oAx], o1 = P.hi[oAx];
+		const float *wO = P.wH[oAx];
+		float acc = 0;
+		for (int o = o0 + 1; o <= o1; o++) acc = __fadd_rn(acc, __fmul_rn(wO[o], inner[(l == 0 ? 0 : n1) + (o - o0 - 1)]));
+		if (l == 0) Sum = acc; else Part = acc;
+	}
+	P.out[0] = __fadd_rn(Sum, Part);
+}
+
+extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2],
+                                  const float *const wE[2], const float *const wH[2], float *out)
+{
+	if (!w || axis < 0 || axis > 2 || !lo || !hi || !wE || !wH || !out) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: bad argument");
+	const alisgpu_geometry &g = w->g;
+	const int MINs[3] = { g.iMIN, g.jMIN, g.kMIN }, MAXs[3] = { g.iMAX, g.jMAX, g.kMAX };
+	const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
+	if (pos < MINs[axis] - 1 || pos > MAXs[axis] || lo[0] < MINs[ua] - 1 || hi[0] > MAXs[ua] + 1 || lo[1] < MINs[va] - 1 ||
+	    hi[1] > MAXs[va] + 1 || hi[0] < lo[0] || hi[1] < lo[1])
+		return alisgpu__fail(ALISGPU_ERANGE, "plane_flux: plane or range outside the world");
+	// E's upper halo is written by the deferred ghost copies
+	if (pos > MAXs[axis] - 1 || hi[0] > MAXs[ua] || hi[1] > MAXs[va]) {
+		int rc = applyPendingGhosts(w);
+		if (rc) return rc;
+	}
+	const int len[2] = { 1 + hi[0] - lo[0], 1 + hi[1] - lo[1] };
+	const size_t floats = 2 * (size_t)(len[0] + len[1]) + 1;
+	if (floats > w->planeTabFloats) {
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+		if (w->planeTab) cudaFree(w->planeTab);
+		w->planeTab = 0, w->planeTabFloats = 0;
+		ALIS_CUDA(cudaMalloc(&w->planeTab, floats * sizeof(float)));
+		w->planeTabFloats = floats;
+	}
+	PlaneParams P;
+	memset(&P, 0, sizeof P);
+	P.L = w->L;
+	for (int c = 0; c < 3; c++) P.E[c] = w->E[0][c], P.H[c] = w->H[0][c];
+	P.axis = axis, P.pos = pos;
+	float *t = w->planeTab;
+	for (int q = 0; q < 2; q++) {
+		P.lo[q] = lo[q], P.hi[q] = hi[q];
+		ALIS_CUDA(cudaMemcpyAsync(t, wE[q], len[q] * sizeof(float), cudaMemcpyHostToDevice, gStream));
+		P.wE[q] = t - lo[q], t += len[q];
+		ALIS_CUDA(cudaMemcpyAsync(t, wH[q], len[q] * sizeof(float), cudaMemcpyHostToDevice, gStream));
+		P.wH[q] = t - lo[q], t += len[q];
+	}
+	P.out = t;
+	const int n1 = axis == 1 ? hi[1] - lo[1] : hi[0] - lo[0];
+	const int n2 = axis == 1 ? hi[0] - lo[0] : hi[1] - lo[1];
+	const size_t smem = (size_t)(n1 + n2 + 1) * sizeof(float);
+	if (smem > 48 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "plane_flux: plane of %d + %d rows too large", n1, n2);
+	int slot = alisgpu__prof_start();
+	k_plane_flux<<<1, 256, smem, gStream>>>(P);
+	alisgpu__prof_stop(slot, ALISGPU_K_FLUX);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	ALIS_CUDA(cudaMemcpyAsync(out, P.out, sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	return ALISGPU_OK;
 }
 

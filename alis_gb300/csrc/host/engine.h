@@ -46,6 +46,11 @@ void alis_be_sync_phaser(phaser P);
 int alis_be_phaser_flux(phaser P, float face[6]);
 /* bring the host mirrors of every phaser set on W up to date */
 void alis_be_sync_phasers_of(world W);
+/* The plane sum of poyntingX/Y/Z (before their scale factors) at plane
+ * index pos of axis, over in-plane index ranges [uLo, uHi] x [vLo, vHi]
+ * of the two other axes in increasing order.  Returns 0 when the backend
+ * leaves it to the host mirrors. */
+int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, int vHi, float *out);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

@@ -213,12 +213,13 @@ static void span(int (*toIdx)(world, float), world W, float lo, float hi, int mi
 
 float (poyntingX)(world W, float x, float yMin, float yMax, float zMin, float zMax, ...)
 {
-	alis_be_sync_world(W);
 	float Sum = 0, Part = 0;
 	int i = W->xtoi(W, x<0 && W->xMinSur==SYM ? -x : x), jMin, jMax, kMin, kMax;
 	span(W->ytoj, W, yMin, yMax, W->jMin, W->jMax, &jMin, &jMax);
 	span(W->ztok, W, zMin, zMax, W->kMin, W->kMax, &kMin, &kMax);
 	vfield *E = W->E, *H = W->H;
+	if (alis_be_plane_flux(W, 0, i, jMin, jMax, kMin, kMax, &Sum)) goto scale;
+	alis_be_sync_world(W);
 	for (int j = jMin+1; j <= jMax; j++) {
 		float sum = 0;
 		sum += 0.5 * W->CE->dz[kMin] * E->y[i][j][kMin] * (H->z[i][j][kMin] + H->z[i+1][j][kMin]);
@@ -234,6 +235,7 @@ float (poyntingX)(world W, float x, float yMin, float yMax, float zMin, float zM
 		Part += W->CH->dz[k] * sum;
 	}
 	Sum += Part;
+scale:
 	if (yMin==yMax || W->Dom.y.Min==W->Dom.y.Max) Sum /= W->CH->dy[jMax]+W->CH->dy[jMax-1];
 	if (zMin==zMax || W->Dom.z.Min==W->Dom.z.Max) Sum /= W->CH->dz[kMax]+W->CH->dz[kMax-1];
 	if (W->yMinSur==SYM) Sum *= 2;
@@ -243,12 +245,13 @@ float (poyntingX)(world W, float x, float yMin, float yMax, float zMin, float zM
 
 float (poyntingY)(world W, float y, float xMin, float xMax, float zMin, float zMax, ...)
 {
-	alis_be_sync_world(W);
 	float Sum = 0, Part = 0;
 	int j = W->ytoj(W, y<0 && W->yMinSur==SYM ? -y : y), iMin, iMax, kMin, kMax;
 	span(W->xtoi, W, xMin, xMax, W->iMin, W->iMax, &iMin, &iMax);
 	span(W->ztok, W, zMin, zMax, W->kMin, W->kMax, &kMin, &kMax);
 	vfield *E = W->E, *H = W->H;
+	if (alis_be_plane_flux(W, 1, j, iMin, iMax, kMin, kMax, &Sum)) goto scale;
+	alis_be_sync_world(W);
 	for (int k = kMin+1; k <= kMax; k++) {
 		float sum = 0;
 		sum += 0.5 * W->CE->dx[iMin] * E->z[iMin][j][k] * (H->x[iMin][j][k] + H->x[iMin][j+1][k]);
@@ -264,6 +267,7 @@ float (poyntingY)(world W, float y, float xMin, float xMax, float zMin, float zM
 		Part += W->CH->dx[i] * sum;
 	}
 	Sum += Part;
+scale:
 	if (xMin==xMax || W->Dom.x.Min==W->Dom.x.Max) Sum /= W->CH->dx[iMax]+W->CH->dx[iMax-1];
 	if (zMin==zMax || W->Dom.z.Min==W->Dom.z.Max) Sum /= W->CH->dz[kMax]+W->CH->dz[kMax-1];
 	if (W->xMinSur==SYM) Sum *= 2;
@@ -273,12 +277,13 @@ float (poyntingY)(world W, float y, float xMin, float xMax, float zMin, float zM
 
 float (poyntingZ)(world W, float z, float xMin, float xMax, float yMin, float yMax, ...)
 {
-	alis_be_sync_world(W);
 	float Sum = 0, Part = 0;
 	int k = W->ztok(W, z<0 && W->zMinSur==SYM ? -z : z), iMin, iMax, jMin, jMax;
 	span(W->xtoi, W, xMin, xMax, W->iMin, W->iMax, &iMin, &iMax);
 	span(W->ytoj, W, yMin, yMax, W->jMin, W->jMax, &jMin, &jMax);
 	vfield *E = W->E, *H = W->H;
+	if (alis_be_plane_flux(W, 2, k, iMin, iMax, jMin, jMax, &Sum)) goto scale;
+	alis_be_sync_world(W);
 	for (int i = iMin+1; i <= iMax; i++) {
 		float sum = 0;
 		sum += 0.5 * W->CE->dy[jMin] * E->x[i][jMin][k] * (H->y[i][jMin][k] + H->y[i][jMin][k+1]);
@@ -294,6 +299,7 @@ float (poyntingZ)(world W, float z, float xMin, float xMax, float yMin, float yM
 		Part += W->CH->dy[j] * sum;
 	}
 	Sum += Part;
+scale:
 	if (xMin==xMax || W->Dom.x.Min==W->Dom.x.Max) Sum /= W->CH->dx[iMax]+W->CH->dx[iMax-1];
 	if (yMin==yMax || W->Dom.y.Min==W->Dom.y.Max) Sum /= W->CH->dy[jMax]+W->CH->dy[jMax-1];
 	if (W->xMinSur==SYM) Sum *= 2;

@@ -173,6 +173,15 @@ typedef struct alisgpu_half_step {
  * reference order.  Replaces reference src/update.c:275-341. */
 int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s);
 
+/* Instantaneous Poynting flux through the plane index pos of axis (0 x,
+ * 1 y, 2 z) over the in-plane index box [lo[q], hi[q]] of its two other
+ * axes in increasing order: the sum poyntingX/Y/Z form before their
+ * scale factors, with their float and double arithmetic in their order as
+ * one OpenMP thread runs it (reference src/output.c:233-356).  wE[q] /
+ * wH[q]: E-grid and H-grid spacings of in-plane axis q over [lo[q], hi[q]]. */
+int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2],
+                       const float *const wE[2], const float *const wH[2], float *out);
+
 /* ---- phasers (reference src/phaser.c:21-110) ---- */
 
 typedef struct alisgpu_phaser alisgpu_phaser;

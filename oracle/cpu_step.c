@@ -600,6 +600,11 @@ void alis_be_phaser_created(phaser P) { (void)P; }
 void alis_be_phaser_deleted(phaser P) { (void)P; }
 void alis_be_sync_phaser(phaser P) { (void)P; }
 int alis_be_phaser_flux(phaser P, float face[6]) { (void)P; (void)face; return 0; }
+int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, int vHi, float *out)
+{
+	(void)W, (void)axis, (void)pos, (void)uLo, (void)uHi, (void)vLo, (void)vHi, (void)out;
+	return 0;
+}
 void alis_be_sync_phasers_of(world W)
 {
 	/* FP64 mode: the double sums rounded into the face arrays */

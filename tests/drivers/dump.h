@@ -62,6 +62,34 @@ static void dumpCScalar(const char *name, float complex v)
 }
 
 /* material maps, fields, ADE currents of a world */
+/* instantaneous Poynting fluxes through planes of W: whole planes, a
+ * sub-rectangle and a zero-width strip per axis, and a closed box */
+static void dumpPoynting(world W, const char *tag)
+{
+	char nm[64];
+	float lo[3] = { W->xMin, W->yMin, W->zMin }, hi[3] = { W->xMax, W->yMax, W->zMax };
+	int sym[3] = { W->xMinSur == SYM, W->yMinSur == SYM, W->zMinSur == SYM };
+	float at[3][2], a0[3], a1[3];
+	/* a symmetry plane at 0: ranges on the stored half only (the
+	 * reference mirrors plane positions, not range ends) */
+	for (int a = 0; a < 3; a++) if (sym[a] && lo[a] < 0) lo[a] = 0;
+	for (int a = 0; a < 3; a++) {
+		at[a][0] = lo[a] + 0.5f * (hi[a] - lo[a]);
+		at[a][1] = lo[a] + 0.2f * (hi[a] - lo[a]);
+		a0[a] = lo[a] + 0.15f * (hi[a] - lo[a]), a1[a] = hi[a] - 0.3f * (hi[a] - lo[a]);
+	}
+	for (int p = 0; p < 2; p++) {
+		snprintf(nm, 64, "%s.x%d", tag, p); dumpScalar(nm, poyntingX(W, at[0][p]));
+		snprintf(nm, 64, "%s.y%d", tag, p); dumpScalar(nm, poyntingY(W, at[1][p]));
+		snprintf(nm, 64, "%s.z%d", tag, p); dumpScalar(nm, poyntingZ(W, at[2][p]));
+		snprintf(nm, 64, "%s.xs%d", tag, p); dumpScalar(nm, poyntingX(W, at[0][p], a0[1], a1[1], a0[2], a1[2]));
+		snprintf(nm, 64, "%s.ys%d", tag, p); dumpScalar(nm, poyntingY(W, at[1][p], a0[0], a1[0], a0[2], a1[2]));
+		snprintf(nm, 64, "%s.zs%d", tag, p); dumpScalar(nm, poyntingZ(W, at[2][p], a0[0], a1[0], a0[1], a1[1]));
+		snprintf(nm, 64, "%s.zl%d", tag, p); dumpScalar(nm, poyntingZ(W, at[2][p], a0[0], a0[0], a0[1], a1[1]));
+	}
+	snprintf(nm, 64, "%s.out", tag); dumpScalar(nm, poyntingOut(W, a0[0], a1[0], a0[1], a1[1], a0[2], a1[2]));
+}
+
 static void dumpWorld(world W, const char *tag)
 {
 	char nm[64];
@@ -110,6 +138,7 @@ static void dumpWorld(world W, const char *tag)
 		}
 	}
 	snprintf(nm, 64, "%s.t", tag); dumpScalar(nm, W->t);
+	if (!strcmp(tag, "W")) dumpPoynting(W, "S");
 }
 
 /* accumulated DFT faces of every frequency of a phaser set, plus its flux */
