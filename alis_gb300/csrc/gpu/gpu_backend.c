@@ -213,10 +213,55 @@ static void downloadWorld(devWorld *d)
 	d->hostStale = 0;
 }
 
+static world heldWorld;
+
+void alis_be_hold_sync(world W) { heldWorld = W; }
+
 void alis_be_sync_world(world W)
 {
+	if (W == heldWorld) return;
 	devWorld *d = findWorld(W);
 	if (d && d->hostStale) downloadWorld(d);
+}
+
+/* index box of the cells a field function at (i, j, k) reads: +-2, and
+ * across a symmetry plane the mirrored cells as well */
+static void nearRange(int c, int sym, int lo0, int hi0, int *a, int *b)
+{
+	int lo = c - 2, hi = c + 2;
+	if (sym && lo < 0) hi = MAX(hi, 3 - lo);
+	*a = MAX(lo, lo0), *b = MIN(hi, hi0);
+}
+
+int alis_be_sync_near(world W, int i, int j, int k)
+{
+	devWorld *d = findWorld(W);
+	if (!d) return 0;
+	if (!d->hostStale) return 1;
+	int i0, i1, j0, j1, k0, k1;
+	nearRange(i, W->xMinSur==SYM, W->iMIN-1, W->iMAX+1, &i0, &i1);
+	nearRange(j, W->yMinSur==SYM, W->jMIN-1, W->jMAX+1, &j0, &j1);
+	nearRange(k, W->zMinSur==SYM, W->kMIN-1, W->kMAX+1, &k0, &k1);
+	if (i1 < i0 || j1 < j0 || k1 < k0) return 0;
+	coeffs *C = W->CE;
+	for (int n = 0; n < C->N; n++)
+		if (C->iMin[n] <= i1 && i0 <= C->iMax[n] && C->jMin[n] <= j1 && j0 <= C->jMax[n] && C->kMin[n] <= k1 && k0 <= C->kMax[n])
+			return 0;
+	int ni = 1 + i1 - i0, nj = 1 + j1 - j0, nk = 1 + k1 - k0, nm = 1 + W->complexField;
+	size_t cells = (size_t)ni * nj * nk;
+	float *buf = malloc(cells * 6 * nm * sizeof(float));
+	CHECK("field_box_download", alisgpu_field_box_download(d->dw, i0, i1, j0, j1, k0, k1, buf));
+	for (int f = 0; f < 2; f++) for (int m = 0; m < nm; m++) {
+		vfield *V = f ? &W->H[m] : &W->E[m];
+		float ***A[3] = { V->x, V->y, V->z };
+		for (int c = 0; c < 3; c++) {
+			const float *src = buf + ((size_t)(f * nm + m) * 3 + c) * cells;
+			for (int a = 0; a < ni; a++) for (int b = 0; b < nj; b++)
+				memcpy(&A[c][i0+a][j0+b][k0], src + ((size_t)a * nj + b) * nk, nk * sizeof(float));
+		}
+	}
+	free(buf);
+	return 1;
 }
 
 /* ---- half steps ---- */

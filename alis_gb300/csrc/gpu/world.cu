@@ -1490,6 +1490,67 @@ extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int
 	return ALISGPU_OK;
 }
 
+// ---------------------------------------------------------------------
+// E and H over a small index box, for observers that read a few cells
+// (get): one gather launch and one copy instead of whole arrays
+// ---------------------------------------------------------------------
+struct BoxGatherParams {
+	Layout L;
+	const float *F[2][2][3];                   // [E/H][m][comp]
+	int nm;
+	int i0, j0, k0, ni, nj, nk;
+	float *out;                                // [E/H][m][comp][ni][nj][nk]
+};
+
+__global__ void k_box_gather(const BoxGatherParams P)
+{
+	const int cells = P.ni * P.nj * P.nk;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= cells * 6 * P.nm) return;
+	const int r = t % cells, fc = t / cells;           // fc = (field * nm + m) * 3 + comp
+	const int comp = fc % 3, m = (fc / 3) % P.nm, f = fc / (3 * P.nm);
+	const int k = P.k0 + r % P.nk, j = P.j0 + (r / P.nk) % P.nj, i = P.i0 + r / (P.nk * P.nj);
+	P.out[t] = P.F[f][m][comp][P.L.at(i, j, k)];
+}
+
+extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1, int k0, int k1, float *host)
+{
+	if (!w || !host || i1 < i0 || j1 < j0 || k1 < k0) return alisgpu__fail(ALISGPU_EINVAL, "field_box_download: bad argument");
+	const Layout &L = w->L;
+	if (i0 < L.i0 || i1 >= L.i0 + L.ni || j0 < L.j0 || j1 >= L.j0 + L.nj || k0 < L.k0 || k1 >= L.k0 + L.nk)
+		return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box outside the halo'd grid");
+	const alisgpu_geometry &g = w->g;
+	// E's upper halo is written by the deferred ghost copies
+	if (i1 > g.iMAX || j1 > g.jMAX || k1 > g.kMAX) {
+		int rc = applyPendingGhosts(w);
+		if (rc) return rc;
+	}
+	BoxGatherParams P;
+	memset(&P, 0, sizeof P);
+	P.L = L;
+	P.nm = 1 + g.complexField;
+	for (int m = 0; m < P.nm; m++) for (int c = 0; c < 3; c++) P.F[0][m][c] = w->E[m][c], P.F[1][m][c] = w->H[m][c];
+	P.i0 = i0, P.j0 = j0, P.k0 = k0, P.ni = 1 + i1 - i0, P.nj = 1 + j1 - j0, P.nk = 1 + k1 - k0;
+	const size_t n = (size_t)P.ni * P.nj * P.nk * 6 * P.nm;
+	if (n > (1u << 20)) return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box of %zu values too large", n);
+	if (n > w->planeTabFloats) {
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+		if (w->planeTab) cudaFree(w->planeTab);
+		w->planeTab = 0, w->planeTabFloats = 0;
+		ALIS_CUDA(cudaMalloc(&w->planeTab, n * sizeof(float)));
+		w->planeTabFloats = n;
+	}
+	P.out = w->planeTab;
+	int slot = alisgpu__prof_start();
+	k_box_gather<<<(unsigned)((n + 255) / 256), 256, 0, gStream>>>(P);
+	alisgpu__prof_stop(slot, ALISGPU_K_GATHER);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	ALIS_CUDA(cudaMemcpyAsync(host, P.out, n * sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
 // field pointers of set m for the phaser gather kernel
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L)
 {

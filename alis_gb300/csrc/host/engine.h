@@ -51,6 +51,13 @@ void alis_be_sync_phasers_of(world W);
  * of the two other axes in increasing order.  Returns 0 when the backend
  * leaves it to the host mirrors. */
 int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, int vHi, float *out);
+/* Bring the host mirrors of E and H up to date around cell (i, j, k) --
+ * the cells a field function evaluated there reads -- and hold further
+ * syncs of W until alis_be_hold_sync(0).  Returns 0 when only a full sync
+ * will do (e.g. a dispersive object nearby, whose currents the function
+ * may read). */
+int alis_be_sync_near(world W, int i, int j, int k);
+void alis_be_hold_sync(world W);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

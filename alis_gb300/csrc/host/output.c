@@ -153,8 +153,16 @@ void (writeSpectrum)(world W, int N, float LMin, float LMax, char *format, ...)
 
 float get(world W, field F, float x, float y, float z)
 {
+	int i = W->xtoi(W, x), j = W->ytoj(W, y), k = W->ztok(W, z);
+	if (alis_be_sync_near(W, i, j, k)) {
+		/* the host mirrors are current around the probe */
+		alis_be_hold_sync(W);
+		float v = F(W, i, j, k);
+		alis_be_hold_sync(0);
+		return v;
+	}
 	alis_be_sync_world(W);
-	return F(W, W->xtoi(W, x), W->ytoj(W, y), W->ztok(W, z));
+	return F(W, i, j, k);
 }
 
 float worldMax(world W, field F)

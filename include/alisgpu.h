@@ -116,6 +116,10 @@ int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *ob
  * field 0 = E, 1 = H; m = 0 real / 1 imaginary set; comp 0..2. */
 int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host);
 int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host);
+/* E and H over the index box [i0,i1]x[j0,j1]x[k0,k1] (inside the halo'd
+ * grid) into host[field][m][comp][i][j][k], field 0 E / 1 H, m up to the
+ * complex set: the cells an observer probe reads, without whole arrays. */
+int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1, int k0, int k1, float *host);
 /* ADE current J (isK 0) or K (isK 1) of object n, pole p, axis comp,
  * set m, as a host box array over the object's box. */
 int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host);

@@ -614,4 +614,6 @@ void alis_be_sync_phasers_of(world W)
 			for (int j = s->j0; j < s->j0 + s->nj; j++) for (int k = s->k0; k < s->k0 + s->nk; k++)
 				s->A[i][j][k] = (float complex)s->v[((size_t)(i - s->i0) * s->nj + (j - s->j0)) * s->nk + (k - s->k0)];
 }
+int alis_be_sync_near(world W, int i, int j, int k) { (void)W, (void)i, (void)j, (void)k; return 0; }
+void alis_be_hold_sync(world W) { (void)W; }
 void alis_be_sync_all(void) {}

@@ -88,6 +88,15 @@ static void dumpPoynting(world W, const char *tag)
 		snprintf(nm, 64, "%s.zl%d", tag, p); dumpScalar(nm, poyntingZ(W, at[2][p], a0[0], a0[0], a0[1], a1[1]));
 	}
 	snprintf(nm, 64, "%s.out", tag); dumpScalar(nm, poyntingOut(W, a0[0], a1[0], a0[1], a1[1], a0[2], a1[2]));
+	/* point probes (get) of several field functions at a few positions,
+	 * including the domain's lower corner (a symmetry plane, if any) */
+	field *F[8] = { Ex, Ey, Hz, Sz, EE, UE, ScEx, SoEz };
+	const char *fn[8] = { "Ex", "Ey", "Hz", "Sz", "EE", "UE", "ScEx", "SoEz" };
+	float px[3] = { at[0][0], at[0][1], lo[0] }, py[3] = { at[1][0], at[1][1], lo[1] }, pz[3] = { at[2][1], at[2][0], lo[2] };
+	for (int q = 0; q < 3; q++) for (int f = 0; f < 8; f++) {
+		if (f >= 6 && !W->S) continue;
+		snprintf(nm, 64, "%s.get.%s.%d", tag, fn[f], q); dumpScalar(nm, get(W, F[f], px[q], py[q], pz[q]));
+	}
 }
 
 static void dumpWorld(world W, const char *tag)

@@ -41,7 +41,8 @@ rank, world, _ = bench.env_rank()
 got = bench.reduce_max(float(rank + 1) * 0.5, world)
 bench.barrier(world)
 assert got == world * 0.5, got
-print("rank", rank, "max", got)
+if rank == 0:
+    print("rank", rank, "max", got, flush=True)
 dist.destroy_process_group()
 '''
 
