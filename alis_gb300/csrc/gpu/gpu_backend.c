@@ -545,6 +545,17 @@ int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, in
 	return 1;
 }
 
+int alis_be_object_absorption(world W, int n, float *out)
+{
+	devWorld *d = findWorld(W);
+	if (!d) return 0;
+	if (d->objectsDirty) uploadObjects(d);
+	const float *wE[3] = { &W->CE->dx[W->iMIN], &W->CE->dy[W->jMIN], &W->CE->dz[W->kMIN] };
+	const float *wH[3] = { &W->CH->dx[W->iMIN], &W->CH->dy[W->jMIN], &W->CH->dz[W->kMIN] };
+	CHECK("object_absorption", alisgpu_object_absorption(d->dw, n, wE, wH, out));
+	return 1;
+}
+
 void alis_be_sync_phasers_of(world W)
 {
 	for (devPhaser *d = phasers; d; d = d->next) if (d->P->W == W && d->hostStale) downloadPhaser(d);

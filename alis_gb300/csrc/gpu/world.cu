@@ -1551,6 +1551,154 @@ extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int 
 	return ALISGPU_OK;
 }
 
+// ---------------------------------------------------------------------
+// Power absorbed by dispersive object n (reference src/output.c:359-435):
+// J . E over the object's box with the reference's arithmetic in its
+// order as one OpenMP thread runs it.  The three column sums along k of
+// each (i, j) do not depend on the column's edge weights: one thread per
+// column computes them, one thread then combines the columns in the
+// reference's call order.
+// ---------------------------------------------------------------------
+struct AbsorbParams {
+	Layout L;
+	const float *E[3], *C[3];
+	DevObj o;
+	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
+	int i0, i1, j0, j1, k0, k1;               // box clipped to the world
+	const float *dxE, *dxH, *dyE, *dyH, *dzE, *dzH;   // spacings indexed by index
+	float *cols;                              // [columns][3]
+	float *out;
+};
+
+// polarisation + conduction current density / eps of axis a at a cell of the box
+__device__ __forceinline__ float objCurrent(const AbsorbParams &P, int a, int i, int j, int k, long long c)
+{
+	const DevObj &o = P.o;
+	const int b = (i - o.i0) * (int)o.si + (j - o.j0) * (int)o.sj + (k - o.k0);
+	float f = 0;
+	if (o.a[a]) f = __fadd_rn(f, __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, o.fill[a][b]), P.E[a][c]), __fadd_rn(1.0f, __fdiv_rn(1.0f, o.a[a]))));
+	for (int p = 0; p < o.NK; p++) f = __fadd_rn(f, o.J[0][p][a][b]);
+	return __fdiv_rn(f, P.C[a][c]);
+}
+
+__global__ void k_absorb_columns(const AbsorbParams P)
+{
+	const int nj = 1 + P.j1 - P.j0;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (1 + P.i1 - P.i0) * nj) return;
+	const int i = P.i0 + t / nj, j = P.j0 + t % nj;
+	float xs = 0, ys = 0, zs = 0;
+	for (int k = P.k0; k <= P.k1; k++) {
+		const long long c = P.L.at(i, j, k);
+		if (P.C[0][c] != 0) xs = __fadd_rn(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = __fadd_rn(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
+		if (P.C[2][c] != 0) zs = __fadd_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], P.E[2][c]), objCurrent(P, 2, i, j, k, c)));
+	}
+	// half weights where the box meets the world's k edges; `* 0.5` is a
+	// double product, the difference rounds back to float
+	auto halfOff = [](float s, float v) { return __double2float_rn(__dsub_rn((double)s, (double)v * 0.5)); };
+	if (P.k0 == P.kMIN) {
+		const int k = P.kMIN;
+		const long long c = P.L.at(i, j, k);
+		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
+		if (P.C[2][c] != 0) zs = __fsub_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], P.E[2][c]), objCurrent(P, 2, i, j, k, c)));
+	}
+	if (P.k1 == P.kMAX) {
+		const int k = P.kMAX;
+		const long long c = P.L.at(i, j, k);
+		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
+	}
+	P.cols[3 * t] = xs, P.cols[3 * t + 1] = ys, P.cols[3 * t + 2] = zs;
+}
+
+__device__ __forceinline__ float absorbColumn(const AbsorbParams &P, int i, int j, float x, float y, float z)
+{
+	const int t = (i - P.i0) * (1 + P.j1 - P.j0) + (j - P.j0);
+	const float xs = P.cols[3 * t], ys = P.cols[3 * t + 1], zs = P.cols[3 * t + 2];
+	float S = 0;
+	S = __fadd_rn(S, __fmul_rn(__fmul_rn(__fmul_rn(x, xs), P.dxH[i]), P.dyE[j]));
+	S = __fadd_rn(S, __fmul_rn(__fmul_rn(__fmul_rn(y, ys), P.dxE[i]), P.dyH[j]));
+	S = __fadd_rn(S, __fmul_rn(__fmul_rn(__fmul_rn(z, zs), P.dxE[i]), P.dyE[j]));
+	return S;
+}
+
+__global__ void k_absorb_total(const AbsorbParams P)
+{
+	if (threadIdx.x || blockIdx.x) return;
+	float Sum = 0;
+	for (int i = P.i0; i <= P.i1; i++) {
+		for (int j = P.j0; j <= P.j1; j++) Sum = __fadd_rn(Sum, absorbColumn(P, i, j, 1, 1, 1));
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, i, P.jMIN, -0.5f, -1, -0.5f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, i, P.jMAX, -0.5f, 0, -0.5f));
+	}
+	if (P.i0 == P.iMIN) {
+		float part = 0;
+		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, P.iMIN, j, -1, -0.5f, -0.5f));
+		Sum = __fadd_rn(Sum, part);
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMIN, P.jMIN, 0.5f, 0.5f, 0.25f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMIN, P.jMAX, 0.5f, 0.0f, 0.25f));
+	}
+	if (P.i1 == P.iMAX) {
+		float part = 0;
+		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, P.iMAX, j, 0, -0.5f, -0.5f));
+		Sum = __fadd_rn(Sum, part);
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMAX, P.jMIN, 0.0f, 0.5f, 0.25f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMAX, P.jMAX, 0.0f, 0.0f, 0.25f));
+	}
+	P.out[0] = Sum;
+}
+
+extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, const float *const wE[3], const float *const wH[3], float *out)
+{
+	if (!w || !wE || !wH || !out || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: bad argument");
+	if (!w->C[0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: world has no eps maps");
+	const alisgpu_geometry &g = w->g;
+	AbsorbParams P;
+	memset(&P, 0, sizeof P);
+	P.L = w->L;
+	for (int c = 0; c < 3; c++) P.E[c] = w->E[0][c], P.C[c] = w->C[c];
+	P.o = w->objs[n];
+	P.iMIN = g.iMIN, P.iMAX = g.iMAX, P.jMIN = g.jMIN, P.jMAX = g.jMAX, P.kMIN = g.kMIN, P.kMAX = g.kMAX;
+	P.i0 = std::max(g.iMIN, P.o.i0), P.i1 = std::min(g.iMAX, P.o.i1);
+	P.j0 = std::max(g.jMIN, P.o.j0), P.j1 = std::min(g.jMAX, P.o.j1);
+	P.k0 = std::max(g.kMIN, P.o.k0), P.k1 = std::min(g.kMAX, P.o.k1);
+	if (P.i1 < P.i0 || P.j1 < P.j0 || P.k1 < P.k0) { *out = 0; return ALISGPU_OK; }
+	const int len[3] = { 1 + g.iMAX - g.iMIN, 1 + g.jMAX - g.jMIN, 1 + g.kMAX - g.kMIN };
+	const long long cols = (long long)(1 + P.i1 - P.i0) * (1 + P.j1 - P.j0);
+	const size_t floats = 2 * (size_t)(len[0] + len[1] + len[2]) + 3 * cols + 1;
+	if (floats > w->planeTabFloats) {
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+		if (w->planeTab) cudaFree(w->planeTab);
+		w->planeTab = 0, w->planeTabFloats = 0;
+		ALIS_CUDA(cudaMalloc(&w->planeTab, floats * sizeof(float)));
+		w->planeTabFloats = floats;
+	}
+	float *t = w->planeTab;
+	const float *dE[3], *dH[3];
+	const int MINs[3] = { g.iMIN, g.jMIN, g.kMIN };
+	for (int a = 0; a < 3; a++) {
+		ALIS_CUDA(cudaMemcpyAsync(t, wE[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, gStream));
+		dE[a] = t - MINs[a], t += len[a];
+		ALIS_CUDA(cudaMemcpyAsync(t, wH[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, gStream));
+		dH[a] = t - MINs[a], t += len[a];
+	}
+	P.dxE = dE[0], P.dyE = dE[1], P.dzE = dE[2], P.dxH = dH[0], P.dyH = dH[1], P.dzH = dH[2];
+	P.cols = t, t += 3 * cols;
+	P.out = t;
+	int slot = alisgpu__prof_start();
+	k_absorb_columns<<<(unsigned)((cols + 127) / 128), 128, 0, gStream>>>(P);
+	k_absorb_total<<<1, 32, 0, gStream>>>(P);
+	alisgpu__prof_stop(slot, ALISGPU_K_FLUX);
+	alisgpu__count_launch();
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	ALIS_CUDA(cudaMemcpyAsync(out, P.out, sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
 // field pointers of set m for the phaser gather kernel
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L)
 {

@@ -58,6 +58,9 @@ int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, in
  * may read). */
 int alis_be_sync_near(world W, int i, int j, int k);
 void alis_be_hold_sync(world W);
+/* The sum objectAbsorption forms for dispersive object n before its scale
+ * factors; 0 when the backend leaves it to the host mirrors. */
+int alis_be_object_absorption(world W, int n, float *out);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

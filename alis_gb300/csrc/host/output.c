@@ -390,11 +390,12 @@ static float columnAbsorption(world W, int n, int i, int j, float x, float y, fl
  * with half weights on the grid edges */
 float objectAbsorption(world W, object O)
 {
-	alis_be_sync_world(W);
 	float Sum = 0;
 	int n = 0;
 	for (int o = 0; !sameObject(O, W->CE->O[o]); o++) if (alis_needs_currents(W->CE->M[o])) n++;
 	coeffs *C = W->CE;
+	if (alis_be_object_absorption(W, n, &Sum)) goto scale;
+	alis_be_sync_world(W);
 	int iMinJ = MAX(W->iMIN, C->iMin[n]), iMaxJ = MIN(W->iMAX, C->iMax[n]);
 	int jMinJ = MAX(W->jMIN, C->jMin[n]), jMaxJ = MIN(W->jMAX, C->jMax[n]);
 	for (int i = iMinJ; i <= iMaxJ; i++) {
@@ -418,6 +419,7 @@ float objectAbsorption(world W, object O)
 		if (jMinJ == W->jMIN) Sum += columnAbsorption(W, n, W->iMAX, W->jMIN, 0.0, 0.5, 0.25);
 		if (jMaxJ == W->jMAX) Sum += columnAbsorption(W, n, W->iMAX, W->jMAX, 0.0, 0.0, 0.25);
 	}
+scale:
 	if (W->Dom.x.Min==W->Dom.x.Max) Sum /= W->CH->dx[W->iMax]+W->CH->dx[W->iMax-1];
 	if (W->Dom.y.Min==W->Dom.y.Max) Sum /= W->CH->dy[W->jMax]+W->CH->dy[W->jMax-1];
 	if (W->Dom.z.Min==W->Dom.z.Max) Sum /= W->CH->dz[W->kMax]+W->CH->dz[W->kMax-1];

@@ -186,6 +186,14 @@ int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s);
 int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2],
                        const float *const wE[2], const float *const wH[2], float *out);
 
+/* Power absorbed by dispersive object n before its scale factors (the
+ * sum objectAbsorption forms before dividing by the 2-D widths, doubling
+ * at symmetry planes and dividing by dt), with its arithmetic in its order
+ * as one OpenMP thread runs it (reference src/output.c:359-435).  wE[a] /
+ * wH[a]: E-grid and H-grid spacings (CE->dx..., CH->dx...) of axis a over
+ * [MIN, MAX], indexed from MIN. */
+int alisgpu_object_absorption(alisgpu_world *w, int n, const float *const wE[3], const float *const wH[3], float *out);
+
 /* ---- phasers (reference src/phaser.c:21-110) ---- */
 
 typedef struct alisgpu_phaser alisgpu_phaser;

@@ -616,4 +616,5 @@ void alis_be_sync_phasers_of(world W)
 }
 int alis_be_sync_near(world W, int i, int j, int k) { (void)W, (void)i, (void)j, (void)k; return 0; }
 void alis_be_hold_sync(world W) { (void)W; }
+int alis_be_object_absorption(world W, int n, float *out) { (void)W, (void)n, (void)out; return 0; }
 void alis_be_sync_all(void) {}

@@ -91,6 +91,7 @@ static void sceneC2(int steps)
 	planewave(W, T, Ppol, 0, 0, Pulse, 600, 200);
 	phaser P = createPhasers(W, 400, 800, 400.0/7, -L+6, L-8, -L+6, L-8, -L+6, L-8);
 	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Block));
 	dumpWorld(W, "W");
 	dumpWorld(W->S->W, "A");
 	dumpPhasers(P, "P");
@@ -112,6 +113,7 @@ static void sceneDipole(int steps)
 	pointDipole(W, Hx, -20, 10, 30, Pulse, 500, 100, 0.5, 30);
 	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
 	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Bar));
 	dumpWorld(W, "W");
 	dumpPhasers(P, "P");
 	farSamples(P + 1, "F");
@@ -132,6 +134,7 @@ static void sceneBloch(int steps)
 	planewave(W, T, Ppol, 150, 0, Pulse, 550, 120);
 	phaser P = createPhasers(W, 450, 700, 125, -INF, INF, -INF, INF, -250, -250);
 	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Pillar));
 	dumpWorld(W, "W");
 	dumpWorld(W->S->W, "A");
 	dumpPhasers(P, "P");
@@ -150,6 +153,7 @@ static void sceneSym(int steps)
 	pointDipole(W, Ex, 0, 0, -20, Band, 400, 800);
 	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
 	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Sphere));
 	dumpWorld(W, "W");
 	dumpPhasers(P, "P");
 	farSamples(P + 1, "F");
