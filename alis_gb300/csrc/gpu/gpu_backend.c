@@ -190,6 +190,8 @@ static void buildTfsf(devWorld *d)
 
 /* ---- host mirrors ---- */
 
+static void downloadCurrents(devWorld *d, int n);
+
 static void downloadWorld(devWorld *d)
 {
 	world W = d->W;
@@ -200,16 +202,8 @@ static void downloadWorld(devWorld *d)
 			CHECK("field_download", alisgpu_field_download(d->dw, 0, m, c, &E[c][W->iMIN-1][W->jMIN-1][W->kMIN-1]));
 			CHECK("field_download", alisgpu_field_download(d->dw, 1, m, c, &H[c][W->iMIN-1][W->jMIN-1][W->kMIN-1]));
 		}
-		coeffs *C = W->CE;
-		for (int n = 0; n < C->N; n++) {
-			float *****J[3] = { W->E[m].Jx, W->E[m].Jy, W->E[m].Jz }, *****K[3] = { W->E[m].Kx, W->E[m].Ky, W->E[m].Kz };
-			for (int p = 0; p < C->NK[n]; p++) for (int c = 0; c < 3; c++) {
-				CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 0, &J[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
-				if (p >= C->NJ[n])
-					CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 1, &K[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
-			}
-		}
 	}
+	for (int n = 0; n < W->CE->N; n++) downloadCurrents(d, n);
 	d->hostStale = 0;
 }
 
@@ -224,31 +218,44 @@ void alis_be_sync_world(world W)
 	if (d && d->hostStale) downloadWorld(d);
 }
 
-/* index box of the cells a field function at (i, j, k) reads: +-2, and
- * across a symmetry plane the mirrored cells as well */
-static void nearRange(int c, int sym, int lo0, int hi0, int *a, int *b)
+/* index range of the cells field functions evaluated over [lo, hi] read:
+ * +-2, and across a symmetry plane the mirrored cells as well */
+static void nearRange(int lo, int hi, int sym, int lo0, int hi0, int *a, int *b)
 {
-	int lo = c - 2, hi = c + 2;
+	lo -= 2, hi += 2;
 	if (sym && lo < 0) hi = MAX(hi, 3 - lo);
 	*a = MAX(lo, lo0), *b = MIN(hi, hi0);
 }
 
-int alis_be_sync_near(world W, int i, int j, int k)
+/* currents of dispersive object n into the host mirrors */
+static void downloadCurrents(devWorld *d, int n)
+{
+	world W = d->W;
+	coeffs *C = W->CE;
+	for (int m = 0; m <= W->complexField; m++) {
+		float *****J[3] = { W->E[m].Jx, W->E[m].Jy, W->E[m].Jz }, *****K[3] = { W->E[m].Kx, W->E[m].Ky, W->E[m].Kz };
+		for (int p = 0; p < C->NK[n]; p++) for (int c = 0; c < 3; c++) {
+			CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 0, &J[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
+			if (p >= C->NJ[n])
+				CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 1, &K[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
+		}
+	}
+}
+
+int alis_be_sync_box(world W, int bi0, int bi1, int bj0, int bj1, int bk0, int bk1)
 {
 	devWorld *d = findWorld(W);
 	if (!d) return 0;
 	if (!d->hostStale) return 1;
 	int i0, i1, j0, j1, k0, k1;
-	nearRange(i, W->xMinSur==SYM, W->iMIN-1, W->iMAX+1, &i0, &i1);
-	nearRange(j, W->yMinSur==SYM, W->jMIN-1, W->jMAX+1, &j0, &j1);
-	nearRange(k, W->zMinSur==SYM, W->kMIN-1, W->kMAX+1, &k0, &k1);
+	nearRange(MIN(bi0, bi1), MAX(bi0, bi1), W->xMinSur==SYM, W->iMIN-1, W->iMAX+1, &i0, &i1);
+	nearRange(MIN(bj0, bj1), MAX(bj0, bj1), W->yMinSur==SYM, W->jMIN-1, W->jMAX+1, &j0, &j1);
+	nearRange(MIN(bk0, bk1), MAX(bk0, bk1), W->zMinSur==SYM, W->kMIN-1, W->kMAX+1, &k0, &k1);
 	if (i1 < i0 || j1 < j0 || k1 < k0) return 0;
-	coeffs *C = W->CE;
-	for (int n = 0; n < C->N; n++)
-		if (C->iMin[n] <= i1 && i0 <= C->iMax[n] && C->jMin[n] <= j1 && j0 <= C->jMax[n] && C->kMin[n] <= k1 && k0 <= C->kMax[n])
-			return 0;
 	int ni = 1 + i1 - i0, nj = 1 + j1 - j0, nk = 1 + k1 - k0, nm = 1 + W->complexField;
 	size_t cells = (size_t)ni * nj * nk;
+	/* most of the world: one whole download is cheaper */
+	if (cells * 2 > (size_t)(W->iNUM + 2) * (W->jNUM + 2) * (W->kNUM + 2)) return 0;
 	float *buf = malloc(cells * 6 * nm * sizeof(float));
 	CHECK("field_box_download", alisgpu_field_box_download(d->dw, i0, i1, j0, j1, k0, k1, buf));
 	for (int f = 0; f < 2; f++) for (int m = 0; m < nm; m++) {
@@ -261,7 +268,16 @@ int alis_be_sync_near(world W, int i, int j, int k)
 		}
 	}
 	free(buf);
+	coeffs *C = W->CE;
+	for (int n = 0; n < C->N; n++)
+		if (C->iMin[n] <= i1 && i0 <= C->iMax[n] && C->jMin[n] <= j1 && j0 <= C->jMax[n] && C->kMin[n] <= k1 && k0 <= C->kMax[n])
+			downloadCurrents(d, n);
 	return 1;
+}
+
+int alis_be_sync_near(world W, int i, int j, int k)
+{
+	return alis_be_sync_box(W, i, i, j, j, k, k);
 }
 
 /* ---- half steps ---- */

@@ -1532,7 +1532,7 @@ extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int 
 	for (int m = 0; m < P.nm; m++) for (int c = 0; c < 3; c++) P.F[0][m][c] = w->E[m][c], P.F[1][m][c] = w->H[m][c];
 	P.i0 = i0, P.j0 = j0, P.k0 = k0, P.ni = 1 + i1 - i0, P.nj = 1 + j1 - j0, P.nk = 1 + k1 - k0;
 	const size_t n = (size_t)P.ni * P.nj * P.nk * 6 * P.nm;
-	if (n > (1u << 20)) return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box of %zu values too large", n);
+	if (n >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box of %zu values too large", n);
 	if (n > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
 		if (w->planeTab) cudaFree(w->planeTab);

@@ -51,12 +51,14 @@ void alis_be_sync_phasers_of(world W);
  * of the two other axes in increasing order.  Returns 0 when the backend
  * leaves it to the host mirrors. */
 int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, int vHi, float *out);
-/* Bring the host mirrors of E and H up to date around cell (i, j, k) --
- * the cells a field function evaluated there reads -- and hold further
- * syncs of W until alis_be_hold_sync(0).  Returns 0 when only a full sync
- * will do (e.g. a dispersive object nearby, whose currents the function
- * may read). */
+/* Bring the host mirrors of E and H (and the currents of dispersive
+ * objects nearby) up to date around cell (i, j, k) -- the cells a field
+ * function evaluated there reads; alis_be_hold_sync(W) then makes further
+ * syncs of W no-ops until alis_be_hold_sync(0).  Returns 0 when only a
+ * full sync will do. */
 int alis_be_sync_near(world W, int i, int j, int k);
+/* the same for field functions evaluated over an index box (slices) */
+int alis_be_sync_box(world W, int i0, int i1, int j0, int j1, int k0, int k1);
 void alis_be_hold_sync(world W);
 /* The sum objectAbsorption forms for dispersive object n before its scale
  * factors; 0 when the backend leaves it to the host mirrors. */

@@ -96,6 +96,23 @@ void deleteSlice(slice S)
 }
 
 
+/* bring the host mirrors up to date over the slice (the whole world when
+ * the backend cannot do it for the box) and hold further syncs of W while
+ * the field functions are evaluated; returns whether syncs are held */
+static int syncSlice(world W, slice S)
+{
+	int held = alis_be_sync_box(W, S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+	if (held) alis_be_hold_sync(W);
+	else alis_be_sync_world(W);
+	return held;
+}
+
+static void releaseSlice(int held)
+{
+	if (held) alis_be_hold_sync(0);
+}
+
+
 /* --- writers (reference src/slices.c:128-211) --- */
 
 void (h5)(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
@@ -294,10 +311,11 @@ void (sliceSnap)(world W, field F, slice S, char *f, char *s, ...)
 	sliceq *q = track(W, filename, M, &head);
 	if (N) sprintf(string, "%05ld", (q->N-skip)/step), strcat(filename, string);
 	if (q->N % step) return;
-	alis_be_sync_world(W);
+	int held = syncSlice(W, S);
 	float max = 0;
 	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
 		if (max < fabsf(S->F[i][j][k] = F(W, i, j, k))) max = fabsf(S->F[i][j][k]);
+	releaseSlice(held);
 	if (!Max) Max = max;
 	else if (Max < 0) {
 		Max = q->Max;
@@ -324,9 +342,10 @@ void (sliceTimeAvg)(world W, field F, slice S, char *f, char *s, ...)
 	sliceq *q = track(W, filename, M, &head);
 	if (N) sprintf(string, "%05ld", q->N / N), strcat(filename, string);
 	if (q->N == 1) q->F = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
-	alis_be_sync_world(W);
+	int held = syncSlice(W, S);
 	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
 		q->F[i][j][k] += F(W, i, j, k);
+	releaseSlice(held);
 	if (!N || q->N % N) return;
 	float max = 0;
 	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
@@ -359,13 +378,14 @@ void (sliceFreqDom)(world W, field F, slice S, char *f, char *s, int N, float L,
 		q->F = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
 		q->G = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
 	}
-	alis_be_sync_world(W);
+	int held = syncSlice(W, S);
 	float re = cosf(2 * PI * q->N * W->dt / L);
 	float im = sinf(2 * PI * q->N * W->dt / L);
 	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++) {
 		q->F[i][j][k] += F(W, i, j, k) * re;
 		q->G[i][j][k] += F(W, i, j, k) * im;
 	}
+	releaseSlice(held);
 	if (q->N % N) return;
 	if (Max <= 0) {
 		float max = 0;
@@ -383,10 +403,11 @@ void (sliceFreqDom)(world W, field F, slice S, char *f, char *s, int N, float L,
 
 float sliceMax(world W, field F, slice S)
 {
-	alis_be_sync_world(W);
+	int held = syncSlice(W, S);
 	float Max = 0, f;
 	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
 		if (Max < (f = fabsf(F(W, i, j, k)))) Max = f;
+	releaseSlice(held);
 	return Max;
 }
 
@@ -410,11 +431,12 @@ static float sliceSumY(world W, field F, slice S, int i)
 
 float sliceSum(world W, field F, slice S)
 {
-	alis_be_sync_world(W);
+	int held = syncSlice(W, S);
 	float Sum = 0;
 	for (int i = S->iMin+1; i < S->iMax; i++) Sum += W->CE->dx[i] * sliceSumY(W, F, S, i);
 	Sum += 0.5 * W->CE->dx[S->iMin] * sliceSumY(W, F, S, S->iMin);
 	Sum += 0.5 * W->CE->dx[S->iMax] * sliceSumY(W, F, S, S->iMax);
+	releaseSlice(held);
 	if (S->iMin==S->iMax) Sum /= W->CE->dx[S->iMin];
 	if (S->jMin==S->jMax) Sum /= W->CE->dy[S->jMin];
 	if (S->kMin==S->kMax) Sum /= W->CE->dz[S->kMin];

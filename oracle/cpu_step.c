@@ -615,6 +615,11 @@ void alis_be_sync_phasers_of(world W)
 				s->A[i][j][k] = (float complex)s->v[((size_t)(i - s->i0) * s->nj + (j - s->j0)) * s->nk + (k - s->k0)];
 }
 int alis_be_sync_near(world W, int i, int j, int k) { (void)W, (void)i, (void)j, (void)k; return 0; }
+int alis_be_sync_box(world W, int i0, int i1, int j0, int j1, int k0, int k1)
+{
+	(void)W, (void)i0, (void)i1, (void)j0, (void)j1, (void)k0, (void)k1;
+	return 0;
+}
 void alis_be_hold_sync(world W) { (void)W; }
 int alis_be_object_absorption(world W, int n, float *out) { (void)W, (void)n, (void)out; return 0; }
 void alis_be_sync_all(void) {}

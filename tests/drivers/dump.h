@@ -97,6 +97,15 @@ static void dumpPoynting(world W, const char *tag)
 		if (f >= 6 && !W->S) continue;
 		snprintf(nm, 64, "%s.get.%s.%d", tag, fn[f], q); dumpScalar(nm, get(W, F[f], px[q], py[q], pz[q]));
 	}
+	/* slice reductions: a z plane through the middle and a sub-box */
+	slice S1 = createSlice(W, lo[0], hi[0], lo[1], hi[1], at[2][0], at[2][0]);
+	slice S2 = createSlice(W, a0[0], a1[0], a0[1], a1[1], a0[2], a1[2]);
+	snprintf(nm, 64, "%s.slice.EE", tag); dumpScalar(nm, sliceSum(W, EE, S1));
+	snprintf(nm, 64, "%s.slice.Ex", tag); dumpScalar(nm, sliceMax(W, Ex, S1));
+	snprintf(nm, 64, "%s.slice.HH", tag); dumpScalar(nm, sliceSum(W, HH, S2));
+	snprintf(nm, 64, "%s.slice.Sz", tag); dumpScalar(nm, sliceMax(W, Sz, S2));
+	deleteSlice(S1);
+	deleteSlice(S2);
 }
 
 static void dumpWorld(world W, const char *tag)

@@ -77,3 +77,13 @@ def test_reference_example_compiles_and_links(engine, example):
     from alis_gb300 import build
     with tempfile.TemporaryDirectory() as d:
         build.link_program(example, os.path.join(d, "prog"), "engine")
+
+
+def test_engine_library_resolves_its_own_symbols():
+    """Every alis_* / alisgpu_* symbol the engine references is defined in it."""
+    import subprocess
+    from alis_gb300 import build
+    so = build.build_engine()
+    out = subprocess.run(["nm", "-D", "--undefined-only", so], capture_output=True, text=True).stdout
+    missing = [l.split()[-1] for l in out.splitlines() if l.split() and l.split()[-1].startswith(("alis_", "alisgpu_"))]
+    assert not missing, missing
