@@ -84,6 +84,9 @@ static void uploadLineTables(devWorld *d)
 			C->zP ? &C->zP[W->kMIN] : 0, C->zPx ? &C->zPx[W->kMIN] : 0, C->zPy ? &C->zPy[W->kMIN] : 0 };
 		CHECK("set_line_tables", alisgpu_set_line_tables(d->dw, grid, dtd, cp));
 	}
+	const float *dE[3] = { &W->CE->dx[W->iMIN], &W->CE->dy[W->jMIN], &W->CE->dz[W->kMIN] };
+	const float *dH[3] = { &W->CH->dx[W->iMIN], &W->CH->dy[W->jMIN], &W->CH->dz[W->kMIN] };
+	CHECK("set_spacing", alisgpu_set_spacing(d->dw, dE, dH));
 }
 
 void alis_be_world_created(world W)
@@ -227,19 +230,24 @@ static void nearRange(int lo, int hi, int sym, int lo0, int hi0, int *a, int *b)
 	*a = MAX(lo, lo0), *b = MIN(hi, hi0);
 }
 
-/* currents of dispersive object n into the host mirrors */
+/* currents of dispersive object n into the host mirrors (one transfer) */
 static void downloadCurrents(devWorld *d, int n)
 {
 	world W = d->W;
 	coeffs *C = W->CE;
+	size_t cells = (size_t)(1 + C->iMax[n] - C->iMin[n]) * (1 + C->jMax[n] - C->jMin[n]) * (1 + C->kMax[n] - C->kMin[n]);
+	size_t arrays = (size_t)(1 + W->complexField) * 3 * (2 * C->NK[n] - C->NJ[n]);
+	if (!cells || !arrays) return;
+	float *buf = malloc(cells * arrays * sizeof(float)), *src = buf;
+	CHECK("object_currents_download", alisgpu_object_currents_download(d->dw, n, buf));
 	for (int m = 0; m <= W->complexField; m++) {
 		float *****J[3] = { W->E[m].Jx, W->E[m].Jy, W->E[m].Jz }, *****K[3] = { W->E[m].Kx, W->E[m].Ky, W->E[m].Kz };
 		for (int p = 0; p < C->NK[n]; p++) for (int c = 0; c < 3; c++) {
-			CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 0, &J[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
-			if (p >= C->NJ[n])
-				CHECK("current_download", alisgpu_current_download(d->dw, n, m, p, c, 1, &K[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]]));
+			memcpy(&J[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]], src, cells * sizeof(float)), src += cells;
+			if (p >= C->NJ[n]) memcpy(&K[c][n][p][C->iMin[n]][C->jMin[n]][C->kMin[n]], src, cells * sizeof(float)), src += cells;
 		}
 	}
+	free(buf);
 }
 
 int alis_be_sync_box(world W, int bi0, int bi1, int bj0, int bj1, int bk0, int bk1)
@@ -553,11 +561,8 @@ int alis_be_plane_flux(world W, int axis, int pos, int uLo, int uHi, int vLo, in
 	devWorld *d = findWorld(W);
 	if (!d) return 0;
 	if (d->objectsDirty) uploadObjects(d);
-	const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
-	float *dE[3] = { W->CE->dx, W->CE->dy, W->CE->dz }, *dH[3] = { W->CH->dx, W->CH->dy, W->CH->dz };
 	int lo[2] = { uLo, vLo }, hi[2] = { uHi, vHi };
-	const float *wE[2] = { &dE[ua][uLo], &dE[va][vLo] }, *wH[2] = { &dH[ua][uLo], &dH[va][vLo] };
-	CHECK("plane_flux", alisgpu_plane_flux(d->dw, axis, pos, lo, hi, wE, wH, out));
+	CHECK("plane_flux", alisgpu_plane_flux(d->dw, axis, pos, lo, hi, out));
 	return 1;
 }
 
@@ -566,9 +571,7 @@ int alis_be_object_absorption(world W, int n, float *out)
 	devWorld *d = findWorld(W);
 	if (!d) return 0;
 	if (d->objectsDirty) uploadObjects(d);
-	const float *wE[3] = { &W->CE->dx[W->iMIN], &W->CE->dy[W->jMIN], &W->CE->dz[W->kMIN] };
-	const float *wH[3] = { &W->CH->dx[W->iMIN], &W->CH->dy[W->jMIN], &W->CH->dz[W->kMIN] };
-	CHECK("object_absorption", alisgpu_object_absorption(d->dw, n, wE, wH, out));
+	CHECK("object_absorption", alisgpu_object_absorption(d->dw, n, out));
 	return 1;
 }
 

@@ -189,8 +189,9 @@ struct alisgpu_world {
 	// before the host reads E (same bytes: each copy is a function of the
 	// current interior E)
 	std::vector<alisgpu_ghost_copy> pendingE;
-	float *planeTab;                       // spacing tables and result of the plane-flux kernel
+	float *planeTab;                       // scratch of the observer kernels
 	size_t planeTabFloats;
+	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
 };
 
 static int applyPendingGhosts(alisgpu_world *w);
@@ -279,6 +280,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 	}
 	for (int c = 0; c < 3; c++) if (w->C[c]) cudaFree(w->C[c]);
 	if (w->planeTab) cudaFree(w->planeTab);
+	for (int grid = 0; grid < 2; grid++) for (int a = 0; a < 3; a++) if (w->sp[grid][a]) cudaFree(w->sp[grid][a]);
 	for (int grid = 0; grid < 2; grid++) {
 		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) cudaFree(w->dtd[grid][c]);
 		for (int c = 0; c < 9; c++) if (w->cp[grid][c]) cudaFree(w->cp[grid][c]);
@@ -338,6 +340,19 @@ extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *
 	int rc;
 	for (int a = 0; a < 3; a++) if ((rc = upload1D(w, &w->dtd[grid][a], dtd[a], len[a]))) return rc;
 	for (int q = 0; q < 9; q++) if ((rc = upload1D(w, &w->cp[grid][q], cpml ? cpml[q] : 0, len[q / 3]))) return rc;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_set_spacing(alisgpu_world *w, const float *const dE[3], const float *const dH[3])
+{
+	fullJoin();
+	if (!w || !dE || !dH) return alisgpu__fail(ALISGPU_EINVAL, "set_spacing: bad argument");
+	const alisgpu_geometry &g = w->g;
+	int len[3] = { g.iMAX - g.iMIN + 1, g.jMAX - g.jMIN + 1, g.kMAX - g.kMIN + 1 }, rc;
+	for (int a = 0; a < 3; a++) {
+		if ((rc = upload1D(w, &w->sp[0][a], dE[a], len[a]))) return rc;
+		if ((rc = upload1D(w, &w->sp[1][a], dH[a], len[a]))) return rc;
+	}
 	return ALISGPU_OK;
 }
 
@@ -458,6 +473,48 @@ extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp
 	const Layout &L = w->L;
 	ALIS_CUDA(cudaMemcpy2DAsync(d + ALIS_KOFF, L.sj * sizeof(float), host, L.nk * sizeof(float), L.nk * sizeof(float),
 	                            (size_t)L.ni * L.nj, cudaMemcpyHostToDevice, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+// every current array of one object in one gather launch and one copy
+#define CUR_MAX (2 * ALIS_MAXPOLES * 3 * 2)
+struct CurGather { const float *src[CUR_MAX]; int count; long long cells; float *out; };
+
+__global__ void k_current_gather(const CurGather P)
+{
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= P.cells * P.count) return;
+	P.out[t] = P.src[t / P.cells][t % P.cells];
+}
+
+extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *host)
+{
+	fullJoin();
+	if (!w || !host || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_currents_download: bad argument");
+	const DevObj &o = w->objs[n];
+	CurGather P;
+	memset(&P, 0, sizeof P);
+	P.cells = (long long)(1 + o.i1 - o.i0) * o.si;
+	for (int m = 0; m <= w->g.complexField; m++)
+		for (int p = 0; p < o.NK; p++) for (int c = 0; c < 3; c++) {
+			P.src[P.count++] = o.J[m][p][c];
+			if (p >= o.NJ) P.src[P.count++] = o.K[m][p][c];
+		}
+	if (!P.count || !P.cells) return ALISGPU_OK;
+	const size_t n4 = (size_t)P.cells * P.count;
+	if (n4 > w->planeTabFloats) {
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+		if (w->planeTab) cudaFree(w->planeTab);
+		w->planeTab = 0, w->planeTabFloats = 0;
+		ALIS_CUDA(cudaMalloc(&w->planeTab, n4 * sizeof(float)));
+		w->planeTabFloats = n4;
+	}
+	P.out = w->planeTab;
+	k_current_gather<<<(unsigned)((n4 + 255) / 256), 256, 0, gStream>>>(P);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	ALIS_CUDA(cudaMemcpyAsync(host, P.out, n4 * sizeof(float), cudaMemcpyDeviceToHost, gStream));
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	return ALISGPU_OK;
 }
@@ -1385,45 +1442,71 @@ struct PlaneParams {
 	float *out;
 };
 
-__global__ void __launch_bounds__(256) k_plane_flux(const PlaneParams P)
+// One warp per inner sum: the warp stages the row's terms in shared
+// memory with coalesced loads, lane 0 then adds them in the reference's
+// order.  Rows of the first loop come first in inner[], then the second.
+#define PF_WARPS 8
+#define PF_CHUNK 256                           // row cells staged at a time
+__global__ void __launch_bounds__(32 * PF_WARPS) k_plane_rows(const PlaneParams P)
+{
+	__shared__ float se[PF_WARPS][PF_CHUNK], sh[PF_WARPS][PF_CHUNK];   // a chunk of each warp's row
+	const int a = P.axis;
+	const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+	const int n1 = P.hi[a == 1 ? 1 : 0] - P.lo[a == 1 ? 1 : 0];
+	const int n2 = P.hi[a == 1 ? 0 : 1] - P.lo[a == 1 ? 0 : 1];
+	const int row = blockIdx.x * PF_WARPS + warp;
+	if (row >= n1 + n2) return;
+	const int l = row < n1 ? 0 : 1, t = l == 0 ? row : row - n1;
+	// x plane (u=j, v=k): Ey (Hz) over k for each j, then -Ez (Hy) over j for each k;
+	// y plane (u=i, v=k): Ez (Hx) over i for each k, then -Ex (Hz) over k for each i;
+	// z plane (u=i, v=j): Ex (Hy) over j for each i, then -Ey (Hx) over i for each j
+	const int oAx = (a == 1) == (l == 0) ? 1 : 0, nAx = 1 - oAx;
+	const int ec = a == 0 ? (l == 0 ? 1 : 2) : a == 1 ? (l == 0 ? 2 : 0) : (l == 0 ? 0 : 1);
+	const int hc = a == 0 ? (l == 0 ? 2 : 1) : a == 1 ? (l == 0 ? 0 : 2) : (l == 0 ? 1 : 0);
+	const int o = P.lo[oAx] + 1 + t, m0 = P.lo[nAx], m1 = P.hi[nAx];
+	const float *wN = P.wE[nAx];
+	const float *Ec = P.E[ec], *Hc = P.H[hc];
+	const long long dn = a == 0 ? P.L.si : a == 1 ? P.L.sj : 1;  // H across the plane
+	auto cell = [&](int n) -> long long {
+		const int u = oAx == 0 ? o : n, v = oAx == 0 ? n : o;
+		return a == 0 ? P.L.at(P.pos, u, v) : a == 1 ? P.L.at(u, P.pos, v) : P.L.at(u, v, P.pos);
+	};
+	float sum = 0;
+	// edge terms: `sum +/-= 0.5 * w * E * (H + H')` in double
+	for (int e = 0; e < 2; e++) {
+		const int n = e ? m1 : m0;
+		const long long c = cell(n);
+		const double hw = 0.5 * (double)wN[n];
+		const double term = __dmul_rn(hw * (double)Ec[c], (double)__fadd_rn(Hc[c], Hc[c + dn]));
+		sum = __double2float_rn(l == 0 ? __dadd_rn((double)sum, term) : __dsub_rn((double)sum, term));
+	}
+	// interior terms in float, a chunk of the row at a time
+	for (int base = m0 + 1; base < m1; base += PF_CHUNK) {
+		const int cnt = min(PF_CHUNK, m1 - base);
+		__syncwarp();
+		for (int q = lane; q < cnt; q += 32) {
+			const long long c = cell(base + q);
+			se[warp][q] = __fmul_rn(wN[base + q], Ec[c]);
+			sh[warp][q] = __fadd_rn(Hc[c], Hc[c + dn]);
+		}
+		__syncwarp();
+		if (lane == 0)
+			for (int q = 0; q < cnt; q++) {
+				const float term = __fmul_rn(se[warp][q], sh[warp][q]);
+				sum = l == 0 ? __fadd_rn(sum, term) : __fsub_rn(sum, term);
+			}
+	}
+	if (lane == 0) P.out[1 + row] = sum;
+}
+
+// the outer loops in order: inner sums staged in shared memory first
+__global__ void __launch_bounds__(256) k_plane_total(const PlaneParams P)
 {
 	extern __shared__ float inner[];
 	const int a = P.axis;
-	const int n1 = P.hi[a == 1 ? 1 : 0] - P.lo[a == 1 ? 1 : 0];   // outer count of the first loop
-	for (int l = 0; l < 2; l++) {
-		// x plane (u=j, v=k): Ey (Hz) over k for each j, then -Ez (Hy) over j for each k;
-		// y plane (u=i, v=k): Ez (Hx) over i for each k, then -Ex (Hz) over k for each i;
-		// z plane (u=i, v=j): Ex (Hy) over j for each i, then -Ey (Hx) over i for each j
-		const int oAx = (a == 1) == (l == 0) ? 1 : 0;               // index of the outer in-plane axis
-		const int nAx = 1 - oAx;
-		const int ec = a == 0 ? (l == 0 ? 1 : 2) : a == 1 ? (l == 0 ? 2 : 0) : (l == 0 ? 0 : 1);
-		const int hc = a == 0 ? (l == 0 ? 2 : 1) : a == 1 ? (l == 0 ? 0 : 2) : (l == 0 ? 1 : 0);
-		const int o0 = P.lo[oAx], o1 = P.hi[oAx], m0 = P.lo[nAx], m1 = P.hi[nAx];
-		const float *wN = P.wE[nAx];
-		const float *Ec = P.E[ec], *Hc = P.H[hc];
-		const long long dn = a == 0 ? P.L.si : a == 1 ? P.L.sj : 1;  // H across the plane
-		for (int t = threadIdx.x; t < o1 - o0; t += blockDim.x) {
-			const int o = o0 + 1 + t;
-			auto cell = [&](int n) -> long long {
-				const int u = oAx == 0 ? o : n, v = oAx == 0 ? n : o;
-				return a == 0 ? P.L.at(P.pos, u, v) : a == 1 ? P.L.at(u, P.pos, v) : P.L.at(u, v, P.pos);
-			};
-			float sum = 0;
-			for (int e = 0; e < 2; e++) {
-				const int n = e ? m1 : m0;
-				const long long c = cell(n);
-				const double hw = 0.5 * (double)wN[n];
-				const double term = __dmul_rn(hw * (double)Ec[c], (double)__fadd_rn(Hc[c], Hc[c + dn]));
-				sum = __double2float_rn(l == 0 ? __dadd_rn((double)sum, term) : __dsub_rn((double)sum, term));
-			}
-			for (int n = m0 + 1; n < m1; n++) {
-				const long long c = cell(n);
-				const float term = __fmul_rn(__fmul_rn(wN[n], Ec[c]), __fadd_rn(Hc[c], Hc[c + dn]));
-				sum = l == 0 ? __fadd_rn(sum, term) : __fsub_rn(sum, term);
-			}
-			inner[(l == 0 ? 0 : n1) + t] = sum;
-		}
-	}
+	const int n1 = P.hi[a == 1 ? 1 : 0] - P.lo[a == 1 ? 1 : 0];
+	const int n2 = P.hi[a == 1 ? 0 : 1] - P.lo[a == 1 ? 0 : 1];
+	for (int q = threadIdx.x; q < n1 + n2; q += blockDim.x) inner[q] = P.out[1 + q];
 	__syncthreads();
 	if (threadIdx.x) return;
 	float Sum = 0, Part = 0;
@@ -1438,23 +1521,24 @@ __global__ void __launch_bounds__(256) k_plane_flux(const PlaneParams P)
 	P.out[0] = __fadd_rn(Sum, Part);
 }
 
-extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2],
-                                  const float *const wE[2], const float *const wH[2], float *out)
+extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2], float *out)
 {
-	if (!w || axis < 0 || axis > 2 || !lo || !hi || !wE || !wH || !out) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: bad argument");
+	if (!w || axis < 0 || axis > 2 || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: bad argument");
+	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: spacing tables not set");
 	const alisgpu_geometry &g = w->g;
 	const int MINs[3] = { g.iMIN, g.jMIN, g.kMIN }, MAXs[3] = { g.iMAX, g.jMAX, g.kMAX };
 	const int ua = axis == 0 ? 1 : 0, va = axis == 2 ? 1 : 2;
-	if (pos < MINs[axis] - 1 || pos > MAXs[axis] || lo[0] < MINs[ua] - 1 || hi[0] > MAXs[ua] + 1 || lo[1] < MINs[va] - 1 ||
-	    hi[1] > MAXs[va] + 1 || hi[0] < lo[0] || hi[1] < lo[1])
+	if (pos < MINs[axis] - 1 || pos > MAXs[axis] || lo[0] < MINs[ua] || hi[0] > MAXs[ua] || lo[1] < MINs[va] ||
+	    hi[1] > MAXs[va] || hi[0] < lo[0] || hi[1] < lo[1])
 		return alisgpu__fail(ALISGPU_ERANGE, "plane_flux: plane or range outside the world");
 	// E's upper halo is written by the deferred ghost copies
 	if (pos > MAXs[axis] - 1 || hi[0] > MAXs[ua] || hi[1] > MAXs[va]) {
 		int rc = applyPendingGhosts(w);
 		if (rc) return rc;
 	}
-	const int len[2] = { 1 + hi[0] - lo[0], 1 + hi[1] - lo[1] };
-	const size_t floats = 2 * (size_t)(len[0] + len[1]) + 1;
+	const int n1 = axis == 1 ? hi[1] - lo[1] : hi[0] - lo[0];
+	const int n2 = axis == 1 ? hi[0] - lo[0] : hi[1] - lo[1];
+	const size_t floats = 1 + (size_t)n1 + n2;
 	if (floats > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
 		if (w->planeTab) cudaFree(w->planeTab);
@@ -1467,21 +1551,21 @@ extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int
 	P.L = w->L;
 	for (int c = 0; c < 3; c++) P.E[c] = w->E[0][c], P.H[c] = w->H[0][c];
 	P.axis = axis, P.pos = pos;
-	float *t = w->planeTab;
+	const int axes[2] = { ua, va };
 	for (int q = 0; q < 2; q++) {
 		P.lo[q] = lo[q], P.hi[q] = hi[q];
-		ALIS_CUDA(cudaMemcpyAsync(t, wE[q], len[q] * sizeof(float), cudaMemcpyHostToDevice, gStream));
-		P.wE[q] = t - lo[q], t += len[q];
-		ALIS_CUDA(cudaMemcpyAsync(t, wH[q], len[q] * sizeof(float), cudaMemcpyHostToDevice, gStream));
-		P.wH[q] = t - lo[q], t += len[q];
+		P.wE[q] = w->sp[0][axes[q]] - MINs[axes[q]];
+		P.wH[q] = w->sp[1][axes[q]] - MINs[axes[q]];
 	}
-	P.out = t;
-	const int n1 = axis == 1 ? hi[1] - lo[1] : hi[0] - lo[0];
-	const int n2 = axis == 1 ? hi[0] - lo[0] : hi[1] - lo[1];
+	P.out = w->planeTab;
 	const size_t smem = (size_t)(n1 + n2 + 1) * sizeof(float);
 	if (smem > 48 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "plane_flux: plane of %d + %d rows too large", n1, n2);
 	int slot = alisgpu__prof_start();
-	k_plane_flux<<<1, 256, smem, gStream>>>(P);
+	if (n1 + n2 > 0) {
+		k_plane_rows<<<(n1 + n2 + PF_WARPS - 1) / PF_WARPS, 32 * PF_WARPS, 0, gStream>>>(P);
+		alisgpu__count_launch();
+	}
+	k_plane_total<<<1, 256, smem, gStream>>>(P);
 	alisgpu__prof_stop(slot, ALISGPU_K_FLUX);
 	alisgpu__count_launch();
 	ALIS_CUDA(cudaGetLastError());
@@ -1613,10 +1697,10 @@ __global__ void k_absorb_columns(const AbsorbParams P)
 	P.cols[3 * t] = xs, P.cols[3 * t + 1] = ys, P.cols[3 * t + 2] = zs;
 }
 
-__device__ __forceinline__ float absorbColumn(const AbsorbParams &P, int i, int j, float x, float y, float z)
+__device__ __forceinline__ float absorbColumn(const AbsorbParams &P, const float *cols, int i, int j, float x, float y, float z)
 {
 	const int t = (i - P.i0) * (1 + P.j1 - P.j0) + (j - P.j0);
-	const float xs = P.cols[3 * t], ys = P.cols[3 * t + 1], zs = P.cols[3 * t + 2];
+	const float xs = cols[3 * t], ys = cols[3 * t + 1], zs = cols[3 * t + 2];
 	float S = 0;
 	S = __fadd_rn(S, __fmul_rn(__fmul_rn(__fmul_rn(x, xs), P.dxH[i]), P.dyE[j]));
 	S = __fadd_rn(S, __fmul_rn(__fmul_rn(__fmul_rn(y, ys), P.dxE[i]), P.dyH[j]));
@@ -1624,35 +1708,41 @@ __device__ __forceinline__ float absorbColumn(const AbsorbParams &P, int i, int 
 	return S;
 }
 
-__global__ void k_absorb_total(const AbsorbParams P)
+__global__ void __launch_bounds__(256) k_absorb_total(const AbsorbParams P)
 {
+	// the column sums staged in shared memory, then added in order
+	extern __shared__ float cols[];
+	const int ncols = 3 * (1 + P.i1 - P.i0) * (1 + P.j1 - P.j0);
+	for (int q = threadIdx.x; q < ncols; q += blockDim.x) cols[q] = P.cols[q];
+	__syncthreads();
 	if (threadIdx.x || blockIdx.x) return;
 	float Sum = 0;
 	for (int i = P.i0; i <= P.i1; i++) {
-		for (int j = P.j0; j <= P.j1; j++) Sum = __fadd_rn(Sum, absorbColumn(P, i, j, 1, 1, 1));
-		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, i, P.jMIN, -0.5f, -1, -0.5f));
-		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, i, P.jMAX, -0.5f, 0, -0.5f));
+		for (int j = P.j0; j <= P.j1; j++) Sum = __fadd_rn(Sum, absorbColumn(P, cols, i, j, 1, 1, 1));
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, cols, i, P.jMIN, -0.5f, -1, -0.5f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, cols, i, P.jMAX, -0.5f, 0, -0.5f));
 	}
 	if (P.i0 == P.iMIN) {
 		float part = 0;
-		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, P.iMIN, j, -1, -0.5f, -0.5f));
+		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, cols, P.iMIN, j, -1, -0.5f, -0.5f));
 		Sum = __fadd_rn(Sum, part);
-		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMIN, P.jMIN, 0.5f, 0.5f, 0.25f));
-		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMIN, P.jMAX, 0.5f, 0.0f, 0.25f));
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, cols, P.iMIN, P.jMIN, 0.5f, 0.5f, 0.25f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, cols, P.iMIN, P.jMAX, 0.5f, 0.0f, 0.25f));
 	}
 	if (P.i1 == P.iMAX) {
 		float part = 0;
-		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, P.iMAX, j, 0, -0.5f, -0.5f));
+		for (int j = P.j0; j <= P.j1; j++) part = __fadd_rn(part, absorbColumn(P, cols, P.iMAX, j, 0, -0.5f, -0.5f));
 		Sum = __fadd_rn(Sum, part);
-		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMAX, P.jMIN, 0.0f, 0.5f, 0.25f));
-		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, P.iMAX, P.jMAX, 0.0f, 0.0f, 0.25f));
+		if (P.j0 == P.jMIN) Sum = __fadd_rn(Sum, absorbColumn(P, cols, P.iMAX, P.jMIN, 0.0f, 0.5f, 0.25f));
+		if (P.j1 == P.jMAX) Sum = __fadd_rn(Sum, absorbColumn(P, cols, P.iMAX, P.jMAX, 0.0f, 0.0f, 0.25f));
 	}
 	P.out[0] = Sum;
 }
 
-extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, const float *const wE[3], const float *const wH[3], float *out)
+extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 {
-	if (!w || !wE || !wH || !out || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: bad argument");
+	if (!w || !out || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: bad argument");
+	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: spacing tables not set");
 	if (!w->C[0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: world has no eps maps");
 	const alisgpu_geometry &g = w->g;
 	AbsorbParams P;
@@ -1665,9 +1755,8 @@ extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, const float *c
 	P.j0 = std::max(g.jMIN, P.o.j0), P.j1 = std::min(g.jMAX, P.o.j1);
 	P.k0 = std::max(g.kMIN, P.o.k0), P.k1 = std::min(g.kMAX, P.o.k1);
 	if (P.i1 < P.i0 || P.j1 < P.j0 || P.k1 < P.k0) { *out = 0; return ALISGPU_OK; }
-	const int len[3] = { 1 + g.iMAX - g.iMIN, 1 + g.jMAX - g.jMIN, 1 + g.kMAX - g.kMIN };
 	const long long cols = (long long)(1 + P.i1 - P.i0) * (1 + P.j1 - P.j0);
-	const size_t floats = 2 * (size_t)(len[0] + len[1] + len[2]) + 3 * cols + 1;
+	const size_t floats = 3 * cols + 1;
 	if (floats > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
 		if (w->planeTab) cudaFree(w->planeTab);
@@ -1676,20 +1765,19 @@ extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, const float *c
 		w->planeTabFloats = floats;
 	}
 	float *t = w->planeTab;
-	const float *dE[3], *dH[3];
-	const int MINs[3] = { g.iMIN, g.jMIN, g.kMIN };
-	for (int a = 0; a < 3; a++) {
-		ALIS_CUDA(cudaMemcpyAsync(t, wE[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, gStream));
-		dE[a] = t - MINs[a], t += len[a];
-		ALIS_CUDA(cudaMemcpyAsync(t, wH[a], len[a] * sizeof(float), cudaMemcpyHostToDevice, gStream));
-		dH[a] = t - MINs[a], t += len[a];
-	}
-	P.dxE = dE[0], P.dyE = dE[1], P.dzE = dE[2], P.dxH = dH[0], P.dyH = dH[1], P.dzH = dH[2];
+	P.dxE = w->sp[0][0] - g.iMIN, P.dyE = w->sp[0][1] - g.jMIN, P.dzE = w->sp[0][2] - g.kMIN;
+	P.dxH = w->sp[1][0] - g.iMIN, P.dyH = w->sp[1][1] - g.jMIN, P.dzH = w->sp[1][2] - g.kMIN;
 	P.cols = t, t += 3 * cols;
 	P.out = t;
 	int slot = alisgpu__prof_start();
 	k_absorb_columns<<<(unsigned)((cols + 127) / 128), 128, 0, gStream>>>(P);
-	k_absorb_total<<<1, 32, 0, gStream>>>(P);
+	const size_t smem = 3 * (size_t)cols * sizeof(float);
+	if (smem <= 48 * 1024) k_absorb_total<<<1, 256, smem, gStream>>>(P);
+	else {
+		ALIS_CUDA(cudaFuncSetAttribute(k_absorb_total, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+		if (smem > 200 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "object_absorption: %lld columns too many", cols);
+		k_absorb_total<<<1, 256, smem, gStream>>>(P);
+	}
 	alisgpu__prof_stop(slot, ALISGPU_K_FLUX);
 	alisgpu__count_launch();
 	alisgpu__count_launch();

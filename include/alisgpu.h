@@ -123,6 +123,10 @@ int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1,
 /* ADE current J (isK 0) or K (isK 1) of object n, pole p, axis comp,
  * set m, as a host box array over the object's box. */
 int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host);
+/* Every current of object n in one transfer: for m (up to the complex
+ * set), pole p, axis comp: J, then K for pair poles; each a box array over
+ * the object's box, back to back in host. */
+int alisgpu_object_currents_download(alisgpu_world *w, int n, float *host);
 
 /* ---- half steps (reference src/update.c:87-341) ---- */
 
@@ -177,22 +181,22 @@ typedef struct alisgpu_half_step {
  * reference order.  Replaces reference src/update.c:275-341. */
 int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s);
 
+/* Cell spacings of the E and H grids (CE->dx, CE->dy, CE->dz and CH->...)
+ * per axis over [MIN, MAX], for the observer reductions below. */
+int alisgpu_set_spacing(alisgpu_world *w, const float *const dE[3], const float *const dH[3]);
+
 /* Instantaneous Poynting flux through the plane index pos of axis (0 x,
  * 1 y, 2 z) over the in-plane index box [lo[q], hi[q]] of its two other
  * axes in increasing order: the sum poyntingX/Y/Z form before their
  * scale factors, with their float and double arithmetic in their order as
- * one OpenMP thread runs it (reference src/output.c:233-356).  wE[q] /
- * wH[q]: E-grid and H-grid spacings of in-plane axis q over [lo[q], hi[q]]. */
-int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2],
-                       const float *const wE[2], const float *const wH[2], float *out);
+ * one OpenMP thread runs it (reference src/output.c:233-356). */
+int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2], float *out);
 
 /* Power absorbed by dispersive object n before its scale factors (the
  * sum objectAbsorption forms before dividing by the 2-D widths, doubling
  * at symmetry planes and dividing by dt), with its arithmetic in its order
- * as one OpenMP thread runs it (reference src/output.c:359-435).  wE[a] /
- * wH[a]: E-grid and H-grid spacings (CE->dx..., CH->dx...) of axis a over
- * [MIN, MAX], indexed from MIN. */
-int alisgpu_object_absorption(alisgpu_world *w, int n, const float *const wE[3], const float *const wH[3], float *out);
+ * as one OpenMP thread runs it (reference src/output.c:359-435). */
+int alisgpu_object_absorption(alisgpu_world *w, int n, float *out);
 
 /* ---- phasers (reference src/phaser.c:21-110) ---- */
 
