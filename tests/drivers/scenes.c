@@ -11,6 +11,7 @@
  *
  * Scenes (scaled-down versions of the benchmark configurations):
  *   c1      vacuum plane wave, periodic x/y, CPML z, planar phasers
+ *   nug     non-uniform (graded) grid, dispersive block, dipole, CPML
  *   c2      gold block (Drude + 2 critical-point poles) in a TFSF box,
  *           CPML on all faces, box phasers, far field
  *   dipole  soft dipole, dielectric ball (12^3 supersampling) and a
@@ -203,6 +204,27 @@ static void sceneMulti(int steps)
 	dumpPhasers(P, "P");
 }
 
+/* non-uniform grid (graded cells near the centre on every axis), a
+ * Drude-Lorentz block off-centre, a dipole, CPML, box phasers */
+static void sceneNug(int steps)
+{
+	float L = 200 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {5, {20}, {1240}, {{3, 60}, {2, 80}, {4, 50}}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	object Blk = {Box, {{30, 90}, {-40, 20}, {-30, 50}}};
+	matter DL = {{2.5}, {{6.0, 0.2}, {3.5, 0.4, 1.2}}};
+	putObjects(W, DL, Blk, Air);
+	pointDipole(W, Ez, -20, 10, 0, Band, 400, 800);
+	phaser P = createPhasers(W, 400, 800, 100, -L+40, L-40, -L+40, L-40, -L+40, L-40);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Blk));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+	farSamples(P + 1, "F");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -220,6 +242,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "sym")) sceneSym(steps);
 	else if (!strcmp(s, "hbc")) sceneHBC(steps);
 	else if (!strcmp(s, "multi")) sceneMulti(steps);
+	else if (!strcmp(s, "nug")) sceneNug(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

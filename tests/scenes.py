@@ -29,6 +29,7 @@ CASES = [
     # the vacuum plane-wave workload at its lateral size (128 x 128 cells,
     # periodic), a longer run
     ("c1", 4, 400),
+    ("nug", 1, 80),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
