@@ -12,6 +12,8 @@
  * Scenes (scaled-down versions of the benchmark configurations):
  *   c1      vacuum plane wave, periodic x/y, CPML z, planar phasers
  *   nug     non-uniform (graded) grid, dispersive block, dipole, CPML
+ *   beam    focused beam over the whole domain; beamtf through a TFSF box
+ *           with a 3-D auxiliary world
  *   c2      gold block (Drude + 2 critical-point poles) in a TFSF box,
  *           CPML on all faces, box phasers, far field
  *   dipole  soft dipole, dielectric ball (12^3 supersampling) and a
@@ -225,6 +227,30 @@ static void sceneNug(int steps)
 	farSamples(P + 1, "F");
 }
 
+/* focused beams: injected directly over the whole domain (tf = 0) or
+ * through a TFSF box whose auxiliary world is a 3-D world (tf = 1) */
+static void sceneBeam(int steps, int tf)
+{
+	float L = 300 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {10, {20}, {1240}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	object Ball1 = {Ball, {{-60, 60}, {-60, 60}, {40, 160}}};
+	putObjects(W, n(1.8), Ball1, Air);
+	if (tf) {
+		dom T = {{-L+60, L-60}, {-L+60, L-60}, {-L+60, L-60}};
+		focusedBeam(W, T, Ex, 0, INF, 0, 0, Sine, 500, 3, 150);
+	} else {
+		focusedBeam(W, D, Ey, 0, INF, 0, 0, Sine, 500, 3, 150);
+	}
+	phaser P = createPhasers(W, 450, 550, 50, -L+40, L-40, -L+40, L-40, -L+40, L-40);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	if (W->S) dumpWorld(W->S->W, "A");
+	dumpPhasers(P, "P");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -243,6 +269,8 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "hbc")) sceneHBC(steps);
 	else if (!strcmp(s, "multi")) sceneMulti(steps);
 	else if (!strcmp(s, "nug")) sceneNug(steps);
+	else if (!strcmp(s, "beam")) sceneBeam(steps, 0);
+	else if (!strcmp(s, "beamtf")) sceneBeam(steps, 1);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

@@ -30,6 +30,8 @@ CASES = [
     # periodic), a longer run
     ("c1", 4, 400),
     ("nug", 1, 80),
+    ("beam", 1, 80),
+    ("beamtf", 1, 80),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
