@@ -575,6 +575,18 @@ int alis_be_object_absorption(world W, int n, float *out)
 	return 1;
 }
 
+void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt)
+{
+	devWorld *s = findWorld(WS), *p1 = findWorld(WP1), *p2 = findWorld(WP2);
+	if (!s || !p1 || !p2) { fprintf(stderr, "alis: nonlinear coupling of worlds unknown to the GPU backend\n"); exit(1); }
+	if (s->objectsDirty) uploadObjects(s);
+	/* the reference takes the tensor of C->M[n] for dispersive object n */
+	for (int n = 0; n < WS->CE->N; n++)
+		for (int m = 0; m <= WS->complexField; m++)
+			CHECK("nonlinear_twm", alisgpu_nonlinear_twm(s->dw, p1->dw, p2->dw, n, m, (const float (*)[6])WS->CE->M[n].d, Alt));
+	s->hostStale = 1;
+}
+
 void alis_be_sync_phasers_of(world W)
 {
 	for (devPhaser *d = phasers; d; d = d->next) if (d->P->W == W && d->hostStale) downloadPhaser(d);

@@ -1787,6 +1787,120 @@ extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 	return ALISGPU_OK;
 }
 
+// ---------------------------------------------------------------------
+// Second-order (chi2) coupling of a signal world to pump fields over the
+// box of dispersive object n (reference src/update.c:343-411): E_a +=
+// 2 Alt d C_a fill_a (G1_b G2_c) for the 9 terms of each axis a, with the
+// pump components averaged onto the a-grid (0.25 x a 4-cell sum, a double
+// product) where they sit elsewhere.  One launch per axis: within it a
+// cell takes its 9 terms in the reference's order, and a later axis reads
+// the finished earlier one (as the reference's term-by-term sweeps do,
+// also when the signal world is its own pump).
+// ---------------------------------------------------------------------
+struct TwmParams {
+	Layout L;
+	float *F[3];
+	const float *G1[3], *G2[3];
+	const float *C[3];
+	const float *fill[3];
+	int oi0, oj0, ok0;                     // object box origin (fill indexing)
+	long long osj, osi;
+	int i0, i1, j0, j1, k0, k1;            // coupled range
+	float coef[6];                         // 2 Alt d[a][q] per term kind
+	unsigned active;                       // d[a][q] non-zero
+};
+
+// component c of a pump field on the grid of axis a: the cell itself
+// (float) or the reference's 4-cell average (double)
+__device__ __forceinline__ double pumpAt(const float *const G[3], const Layout &L, int c, int a, int i, int j, int k, bool &isDouble)
+{
+	if (c == a) { isDouble = false; return (double)G[c][L.at(i, j, k)]; }
+	isDouble = true;
+	int o[4][3];
+	if (a == 0 && c == 1) { int t[4][3] = {{0,0,0},{-1,0,0},{0,1,0},{-1,1,0}}; memcpy(o, t, sizeof t); }
+	else if (a == 0) { int t[4][3] = {{0,0,0},{-1,0,0},{0,0,1},{-1,0,1}}; memcpy(o, t, sizeof t); }
+	else if (a == 1 && c == 2) { int t[4][3] = {{0,0,0},{0,-1,0},{0,0,1},{0,-1,1}}; memcpy(o, t, sizeof t); }
+	else if (a == 1) { int t[4][3] = {{0,0,0},{0,-1,0},{1,0,0},{1,-1,0}}; memcpy(o, t, sizeof t); }
+	else if (c == 0) { int t[4][3] = {{0,0,0},{0,0,-1},{1,0,0},{1,0,-1}}; memcpy(o, t, sizeof t); }
+	else { int t[4][3] = {{0,0,0},{0,0,-1},{0,1,0},{0,1,-1}}; memcpy(o, t, sizeof t); }
+	float sum = G[c][L.at(i + o[0][0], j + o[0][1], k + o[0][2])];
+	for (int q = 1; q < 4; q++) sum = __fadd_rn(sum, G[c][L.at(i + o[q][0], j + o[q][1], k + o[q][2])]);
+	return 0.25 * (double)sum;
+}
+
+template <int A>
+__global__ void k_twm(const TwmParams P)
+{
+	const int nj = 1 + P.j1 - P.j0, nk = 1 + P.k1 - P.k0;
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long long)(1 + P.i1 - P.i0) * nj * nk) return;
+	const int i = P.i0 + (int)(t / ((long long)nj * nk)), j = P.j0 + (int)((t / nk) % nj), k = P.k0 + (int)(t % nk);
+	const long long c = P.L.at(i, j, k);
+	const long long b = (long long)(i - P.oi0) * P.osi + (long long)(j - P.oj0) * P.osj + (k - P.ok0);
+	// the terms of axis A: (d index, G1 component, G2 component)
+	const int T[9][3] = {{0,0,0},{1,1,1},{2,2,2},{3,1,2},{3,2,1},{4,2,0},{4,0,2},{5,0,1},{5,1,0}};
+	float f = P.F[A][c];
+	const float cv = P.C[A][c], fl = P.fill[A][b];
+	// a pump that is the signal itself reads this cell's running value
+	const bool self1 = P.G1[A] == P.F[A], self2 = P.G2[A] == P.F[A];
+#pragma unroll
+	for (int q = 0; q < 9; q++) {
+		const int di = T[q][0];
+		if (!((P.active >> di) & 1u)) continue;
+		bool d1, d2;
+		double v1 = pumpAt(P.G1, P.L, T[q][1], A, i, j, k, d1);
+		double v2 = pumpAt(P.G2, P.L, T[q][2], A, i, j, k, d2);
+		if (T[q][1] == A && self1) v1 = (double)f;
+		if (T[q][2] == A && self2) v2 = (double)f;
+		const float lead = __fmul_rn(__fmul_rn(P.coef[di], cv), fl);
+		if (!d1 && !d2) f = __fadd_rn(f, __fmul_rn(lead, __fmul_rn((float)v1, (float)v2)));
+		else f = __double2float_rn(__dadd_rn((double)f, __dmul_rn((double)lead, __dmul_rn(v1, v2))));
+	}
+	P.F[A][c] = f;
+}
+
+extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
+                                     const float d[3][6], float Alt)
+{
+	fullJoin();
+	if (!ws || !wp1 || !wp2 || !d || n < 0 || n >= (int)ws->objs.size() || m < 0 || m > ws->g.complexField ||
+	    m > wp1->g.complexField || m > wp2->g.complexField)
+		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: bad argument");
+	if (!ws->C[0]) return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: signal world has no eps maps");
+	if (memcmp(&ws->L, &wp1->L, sizeof(Layout)) || memcmp(&ws->L, &wp2->L, sizeof(Layout)))
+		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: pump and signal worlds differ in grid");
+	const DevObj &o = ws->objs[n];
+	TwmParams P;
+	memset(&P, 0, sizeof P);
+	P.L = ws->L;
+	for (int c = 0; c < 3; c++) {
+		P.F[c] = ws->E[m][c], P.G1[c] = wp1->E[m][c], P.G2[c] = wp2->E[m][c];
+		P.C[c] = ws->C[c], P.fill[c] = o.fill[c];
+	}
+	P.oi0 = o.i0, P.oj0 = o.j0, P.ok0 = o.k0, P.osj = o.sj, P.osi = o.si;
+	// the reference couples [box min, box max - 1] on every axis
+	P.i0 = o.i0, P.i1 = o.i1 - 1, P.j0 = o.j0, P.j1 = o.j1 - 1, P.k0 = o.k0, P.k1 = o.k1 - 1;
+	if (P.i1 < P.i0 || P.j1 < P.j0 || P.k1 < P.k0) return ALISGPU_OK;
+	const long long cells = (long long)(1 + P.i1 - P.i0) * (1 + P.j1 - P.j0) * (1 + P.k1 - P.k0);
+	for (int a = 0; a < 3; a++) {
+		P.active = 0;
+		for (int q = 0; q < 6; q++) {
+			P.coef[q] = (2.0f * Alt) * d[a][q];
+			if (d[a][q]) P.active |= 1u << q;
+		}
+		if (!P.active) continue;
+		int slot = alisgpu__prof_start();
+		const unsigned blocks = (unsigned)((cells + 255) / 256);
+		if (a == 0) k_twm<0><<<blocks, 256, 0, gStream>>>(P);
+		else if (a == 1) k_twm<1><<<blocks, 256, 0, gStream>>>(P);
+		else k_twm<2><<<blocks, 256, 0, gStream>>>(P);
+		alisgpu__prof_stop(slot, ALISGPU_K_STEP_AUX);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	return ALISGPU_OK;
+}
+
 // field pointers of set m for the phaser gather kernel
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L)
 {

@@ -63,6 +63,9 @@ void alis_be_hold_sync(world W);
 /* The sum objectAbsorption forms for dispersive object n before its scale
  * factors; 0 when the backend leaves it to the host mirrors. */
 int alis_be_object_absorption(world W, int n, float *out);
+/* second-order coupling of WS to the pumps WP1, WP2 (reference
+ * src/update.c:343-411) */
+void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

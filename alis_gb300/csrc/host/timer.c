@@ -58,16 +58,14 @@ void (copyBoundary)(float ***F, float ***G, float cosk, float sink, int iMin, in
 
 /* chi(2) coupling between worlds (reference src/update.c:358-411) is not
  * part of the GPU engine; the entry points exist so programs link. */
+/* second-harmonic generation and three-wave mixing (reference
+ * src/update.c:386-411) */
 void nonLinearSHG(world WS, world WP, float Alt)
 {
-	(void)WS; (void)WP; (void)Alt;
-	fprintf(stderr, "alis: nonLinearSHG is not supported by this engine\n");
-	exit(1);
+	alis_be_nonlinear(WS, WP, WP, Alt);
 }
 
 void nonLinearTWM(world WS, world WP1, world WP2, float Alt)
 {
-	(void)WS; (void)WP1; (void)WP2; (void)Alt;
-	fprintf(stderr, "alis: nonLinearTWM is not supported by this engine\n");
-	exit(1);
+	alis_be_nonlinear(WS, WP1, WP2, Alt);
 }

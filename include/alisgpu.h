@@ -198,6 +198,13 @@ int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], con
  * as one OpenMP thread runs it (reference src/output.c:359-435). */
 int alisgpu_object_absorption(alisgpu_world *w, int n, float *out);
 
+/* Second-order coupling of field set m of the signal world ws to the pump
+ * fields of wp1 and wp2 (the same grid; wp1 == wp2 for second-harmonic
+ * generation, ws itself allowed) over the box of dispersive object n, with
+ * the tensor d and sign Alt (reference src/update.c:343-411). */
+int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
+                          const float d[3][6], float Alt);
+
 /* ---- phasers (reference src/phaser.c:21-110) ---- */
 
 typedef struct alisgpu_phaser alisgpu_phaser;

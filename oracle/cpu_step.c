@@ -622,4 +622,48 @@ int alis_be_sync_box(world W, int i0, int i1, int j0, int j1, int k0, int k1)
 }
 void alis_be_hold_sync(world W) { (void)W; }
 int alis_be_object_absorption(world W, int n, float *out) { (void)W, (void)n, (void)out; return 0; }
+/* --- second-order coupling (reference src/update.c:343-411) ---
+ * term by term over the box of dispersive object n (less its last plane
+ * on every axis): E_a += 2 Alt d C_a fill_a (G1 G2), the pump components
+ * averaged onto the a-grid with 0.25 x a 4-cell sum where they sit
+ * elsewhere (a double product, as the reference's 0.25 literal makes it) */
+#define PAT(G, c, i, j, k) ((G)[c][i][j][k])
+static double pumpOn(float ***G[3], int c, int a, int i, int j, int k, int *isD)
+{
+	*isD = c != a;
+	if (c == a) return PAT(G, c, i, j, k);
+	if (a == 0 && c == 1) return 0.25 * (PAT(G,1,i,j,k) + PAT(G,1,i-1,j,k) + PAT(G,1,i,j+1,k) + PAT(G,1,i-1,j+1,k));
+	if (a == 0 && c == 2) return 0.25 * (PAT(G,2,i,j,k) + PAT(G,2,i-1,j,k) + PAT(G,2,i,j,k+1) + PAT(G,2,i-1,j,k+1));
+	if (a == 1 && c == 2) return 0.25 * (PAT(G,2,i,j,k) + PAT(G,2,i,j-1,k) + PAT(G,2,i,j,k+1) + PAT(G,2,i,j-1,k+1));
+	if (a == 1 && c == 0) return 0.25 * (PAT(G,0,i,j,k) + PAT(G,0,i,j-1,k) + PAT(G,0,i+1,j,k) + PAT(G,0,i+1,j-1,k));
+	if (a == 2 && c == 0) return 0.25 * (PAT(G,0,i,j,k) + PAT(G,0,i,j,k-1) + PAT(G,0,i+1,j,k) + PAT(G,0,i+1,j,k-1));
+	return 0.25 * (PAT(G,1,i,j,k) + PAT(G,1,i,j,k-1) + PAT(G,1,i,j+1,k) + PAT(G,1,i,j+1,k-1));
+}
+
+static void couple(coeffs *C, vfield F, vfield G1, vfield G2, int n, float Alt)
+{
+	static const int T[9][3] = {{0,0,0},{1,1,1},{2,2,2},{3,1,2},{3,2,1},{4,2,0},{4,0,2},{5,0,1},{5,1,0}};
+	float ***f[3] = { F.x, F.y, F.z }, ***g1[3] = { G1.x, G1.y, G1.z }, ***g2[3] = { G2.x, G2.y, G2.z };
+	float ***cm[3] = { C->x, C->y, C->z }, ****fill[3] = { C->Jx, C->Jy, C->Jz };
+	for (int a = 0; a < 3; a++)
+		for (int q = 0; q < 9; q++) {
+			float d = C->M[n].d[a][T[q][0]];
+			if (!d) continue;
+			for (int i = C->iMin[n]; i <= C->iMax[n]-1; i++) for (int j = C->jMin[n]; j <= C->jMax[n]-1; j++)
+				for (int k = C->kMin[n]; k <= C->kMax[n]-1; k++) {
+					int d1, d2;
+					double v1 = pumpOn(g1, T[q][1], a, i, j, k, &d1), v2 = pumpOn(g2, T[q][2], a, i, j, k, &d2);
+					float lead = 2 * Alt * d * cm[a][i][j][k] * fill[a][n][i][j][k];
+					if (!d1 && !d2) f[a][i][j][k] += lead * ((float)v1 * (float)v2);
+					else f[a][i][j][k] += lead * (v1 * v2);
+				}
+		}
+}
+
+void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt)
+{
+	for (int n = 0; n < WS->CE->N; n++)
+		for (int m = 0; m <= WS->complexField; m++) couple(WS->CE, WS->E[m], WP1->E[m], WP2->E[m], n, Alt);
+}
+
 void alis_be_sync_all(void) {}

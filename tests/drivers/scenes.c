@@ -14,6 +14,8 @@
  *   nug     non-uniform (graded) grid, dispersive block, dipole, CPML
  *   beam    focused beam over the whole domain; beamtf through a TFSF box
  *           with a 3-D auxiliary world
+ *   shg     second-order coupling: second harmonic of a pump world and
+ *           three-wave mixing of a signal world with itself and the pump
  *   c2      gold block (Drude + 2 critical-point poles) in a TFSF box,
  *           CPML on all faces, box phasers, far field
  *   dipole  soft dipole, dielectric ball (12^3 supersampling) and a
@@ -251,6 +253,34 @@ static void sceneBeam(int steps, int tf)
 	dumpPhasers(P, "P");
 }
 
+/* second-order coupling: a pump world driven by a dipole, a signal world
+ * with a chi2 dispersive block, second-harmonic generation from the pump
+ * and three-wave mixing of the signal with the pump */
+static void sceneSHG(int steps)
+{
+	float L = 120 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world WP = createWorld(D, R, S, "");
+	world WS = createWorld(D, R, S, "");
+	object Blk = {Box, {{-50, 50}, {-40, 30}, {-30, 40}}};
+	matter Chi = {{4.5}, {{6.0, 0.1, 0.5}}, {{0.1, 0.2, 0, 0, 0.3, 0}, {0, 0, 0.15, 0.4, 0, 0.2}, {0.3, 0.1, 0.5, 0, 0, 0.25}}};
+	putObjects(WS, Chi, Blk, Air);
+	putObjects(WP, n(2.0), Blk, Air);
+	pointDipole(WP, Ez, -30, 10, 0, Pulse, 500, 100, 50);
+	for (int n = 1; n <= steps; n++) {
+		updateE(WP);
+		updateH(WP);
+		nonLinearSHG(WS, WP, 1);
+		nonLinearTWM(WS, WS, WP, -0.5);
+		updateE(WS);
+		updateH(WS);
+	}
+	dumpWorld(WS, "W");
+	dumpWorld(WP, "A");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -271,6 +301,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "nug")) sceneNug(steps);
 	else if (!strcmp(s, "beam")) sceneBeam(steps, 0);
 	else if (!strcmp(s, "beamtf")) sceneBeam(steps, 1);
+	else if (!strcmp(s, "shg")) sceneSHG(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

@@ -32,6 +32,7 @@ CASES = [
     ("nug", 1, 80),
     ("beam", 1, 80),
     ("beamtf", 1, 80),
+    ("shg", 1, 80),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
