@@ -16,6 +16,10 @@
  *           with a 3-D auxiliary world
  *   shg     second-order coupling: second harmonic of a pump world and
  *           three-wave mixing of a signal world with itself and the pump
+ *   spheres 20 seeded Drude-Lorentz balls in a dielectric host
+ *   unitcell periodic metasurface unit cell (TiO2-like pillar, substrate)
+ *   bowtie  Drude bowtie antenna: symmetry planes, graded grid, edge-rule
+ *           sub-pixel filling, compound shapes
  *   c2      gold block (Drude + 2 critical-point poles) in a TFSF box,
  *           CPML on all faces, box phasers, far field
  *   dipole  soft dipole, dielectric ball (12^3 supersampling) and a
@@ -281,6 +285,96 @@ static void sceneSHG(int steps)
 	dumpWorld(WP, "A");
 }
 
+/* the large-domain study in miniature: 20 seeded Drude-Lorentz balls in
+ * a dielectric host (more than 8 dispersive objects: the kernels' per-tile
+ * object lists), overlaps resolved by list order, a dipole, box phasers */
+static void sceneSpheres(int steps)
+{
+	float L = 160 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	enum { NB = 20 };
+	object O[NB + 1];
+	matter M[NB + 1];
+	lcgSeed(99);
+	for (int q = 0; q < NB; q++) {
+		/* one draw per statement: the order is fixed */
+		float r = 20 + 40 * lcgUniform();
+		float x = -L + 50 + (2 * L - 100) * lcgUniform();
+		float y = -L + 50 + (2 * L - 100) * lcgUniform();
+		float z = -L + 50 + (2 * L - 100) * lcgUniform();
+		float e = 1.5 + lcgUniform(), wp = 5 + 4 * lcgUniform(), g = 0.05 + 0.2 * lcgUniform();
+		float w0 = 3 + lcgUniform(), f0 = 0.5 + lcgUniform();
+		O[q] = (object){Ball, {{x - r, x + r}, {y - r, y + r}, {z - r, z + r}}};
+		M[q] = (matter){{e}, {{wp, g}, {w0, 0.2, f0}}};
+	}
+	O[NB] = (object){0};
+	M[NB] = n(1.5);
+	putObjectArray(W, M, O);
+	pointDipole(W, Ex, 5, -10, 15, Band, 400, 800);
+	phaser P = createPhasers(W, 400, 800, 200, -L+30, L-30, -L+30, L-30, -L+30, L-30);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, O[3]));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
+/* a metasurface unit cell of the batched sweep: periodic x/y, CPML z, a
+ * TiO2-like Lorentz pillar on a glass substrate, a normal-incidence pulse,
+ * a transmission phaser plane */
+static void sceneUnitCell(int steps)
+{
+	float a = 240 * scale;
+	dom D = {{-a/2, a/2 - 10}, {-a/2, a/2 - 10}, {-400, 400}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PBC}, {PBC}, {PML, PML}, {10}};
+	world W = createWorld(D, R, S, "");
+	object Pillar = {RodZ, {{-70, 70}, {-70, 70}, {-200, 150}}};
+	object Sub = {Box, {{-INF, INF}, {-INF, INF}, {-INF, -200}}};
+	matter TiO2 = {{5.5}, {{4.5, 0.05, 1.0}}};
+	putObjects(W, TiO2, Pillar, n(1.45), Sub, Air);
+	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {-300, 300}};
+	planewave(W, T, Ppol, 0, 0, Pulse, 600, 150);
+	phaser P = createPhasers(W, 450, 750, 100, -INF, INF, -INF, INF, 320, 320);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Pillar));
+	dumpWorld(W, "W");
+	dumpWorld(W->S->W, "A");
+	dumpPhasers(P, "P");
+}
+
+/* a Drude-metal bowtie antenna of the served mix: symmetry planes, a
+ * graded grid, the edge rule of sub-pixel filling (subN < 0), compound
+ * shapes, a substrate, a dipole in the gap */
+static void sceneBowtie(int steps)
+{
+	float g = 20, r = 20, d = 60 * scale;
+	dom D = {{160 * scale}, {120 * scale}, {-100, 100}};
+	res R = {2.5, {5}, {1240, -1}, {{3, g/2 + d}, {3, r + (d - 2*r) / sqrtf(3)}, {3, 15}}};
+	sur S = {{SYM, PML}, {SYM, PML}, {PML, PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	float s3 = sqrtf(3);
+	object Bowtie = {Combination, {3}, objects {
+		{RodZ, {{g/2, g/2 + r*2}, {-r, r}, {-15, 15}}},
+		{RodZ, {{g/2 - r*2 + d, g/2 + d}, {-r + (d - 2*r)/s3, r + (d - 2*r)/s3}, {-15, 15}}},
+		{Intersection, {2}, objects {
+			{Box, {{g/2 + r/2, g/2 + d}, {-(d - r/2)/s3, (d - r/2)/s3}, {-15, 15}}},
+			{DRodZ, {{g/2 - r, g/2 - r*2 + d*2}, {-(d - r/2)/s3, (d - r/2)/s3}, {-15, 15}}},
+		}}
+	}};
+	object Substrate = {Box, {{-INF, INF}, {-INF, INF}, {-INF, -15}}};
+	matter Ag2 = {{4.0}, {{9.0, 0.02}}};
+	putObjects(W, Ag2, Bowtie, n(1.5), Substrate, Air);
+	pointDipole(W, Ex, 0, 0, 0, Band, 400, 1000);
+	phaser P = createPhasers(W, 400, 1000, 200, -INF, INF, -INF, INF, -80, 80);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Bowtie));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -302,6 +396,9 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "beam")) sceneBeam(steps, 0);
 	else if (!strcmp(s, "beamtf")) sceneBeam(steps, 1);
 	else if (!strcmp(s, "shg")) sceneSHG(steps);
+	else if (!strcmp(s, "spheres")) sceneSpheres(steps);
+	else if (!strcmp(s, "unitcell")) sceneUnitCell(steps);
+	else if (!strcmp(s, "bowtie")) sceneBowtie(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

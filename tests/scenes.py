@@ -33,6 +33,12 @@ CASES = [
     ("beam", 1, 80),
     ("beamtf", 1, 80),
     ("shg", 1, 80),
+    # the other workloads in miniature: many dispersive objects (per-tile
+    # object lists), a periodic unit cell, a Drude bowtie with symmetry
+    # planes, a graded grid and edge-rule filling
+    ("spheres", 1, 80),
+    ("unitcell", 1, 120),
+    ("bowtie", 1, 80),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
