@@ -73,6 +73,8 @@ struct HalfStepParams {
 	float *F[3];
 	const float *G[3];
 	const float *C[3];                    // eps^-1 maps (E half step) or null
+	const unsigned char *matIdx;          // per cell index into matTab (or null): the
+	const float4 *matTab;                 // distinct (C[0], C[1], C[2]) triples
 	const float *dtd[3];                  // dt/ds tables indexed from MIN
 	const float *cp[9];                   // CPML b/c tables (xP,xPy,xPz,yP,yPz,yPx,zP,zPx,zPy)
 	int slabOn[6];                        // xMin,yMin,zMin,xMax,yMax,zMax

@@ -192,6 +192,8 @@ struct alisgpu_world {
 	float *planeTab;                       // scratch of the observer kernels
 	size_t planeTabFloats;
 	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
+	unsigned char *matIdx;                 // eps^-1 triple index per cell (few distinct triples)
+	float4 *matTab;
 };
 
 static int applyPendingGhosts(alisgpu_world *w);
@@ -280,6 +282,8 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 	}
 	for (int c = 0; c < 3; c++) if (w->C[c]) cudaFree(w->C[c]);
 	if (w->planeTab) cudaFree(w->planeTab);
+	if (w->matIdx) cudaFree(w->matIdx);
+	if (w->matTab) cudaFree(w->matTab);
 	for (int grid = 0; grid < 2; grid++) for (int a = 0; a < 3; a++) if (w->sp[grid][a]) cudaFree(w->sp[grid][a]);
 	for (int grid = 0; grid < 2; grid++) {
 		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) cudaFree(w->dtd[grid][c]);
@@ -386,6 +390,41 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 		if ((rc = uploadBoxToLayout(w, w->C[a], src[a], g.iMIN, i1, g.jMIN, j1, g.kMIN, k1))) return rc;
 	}
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	// the E half step reads (C[0], C[1], C[2]) at the cells of [MIN, MAX]^3:
+	// with at most 256 distinct triples it reads a byte per cell instead
+	if (w->matIdx) { cudaFree(w->matIdx); w->matIdx = 0; }
+	if (w->matTab) { cudaFree(w->matTab); w->matTab = 0; }
+	if (cx && cy && cz) {
+		const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
+		std::vector<unsigned char> idx(w->L.elems(), 0);
+		std::vector<float4> tab;
+		std::vector<unsigned> bits;                 // 3 words per entry
+		int last = -1;
+		bool ok = true;
+		for (int i = 0; i < ni && ok; i++) for (int j = 0; j < nj && ok; j++) for (int k = 0; k < nk; k++) {
+			const float v[3] = { cx[((size_t)i * nj + j) * nk + k], cy[((size_t)i * (nj + 1) + j) * nk + k],
+			                     cz[((size_t)i * nj + j) * (nk + 1) + k] };
+			unsigned b[3];
+			memcpy(b, v, sizeof b);
+			int q = -1;
+			if (last >= 0 && !memcmp(&bits[3 * last], b, sizeof b)) q = last;
+			for (int e = 0; q < 0 && e < (int)tab.size(); e++) if (!memcmp(&bits[3 * e], b, sizeof b)) q = e;
+			if (q < 0) {
+				if (tab.size() == 256) { ok = false; break; }
+				q = (int)tab.size();
+				tab.push_back(make_float4(v[0], v[1], v[2], 0.0f));
+				bits.insert(bits.end(), b, b + 3);
+			}
+			last = q;
+			idx[w->L.at(g.iMIN + i, g.jMIN + j, g.kMIN + k)] = (unsigned char)q;
+		}
+		if (ok) {
+			ALIS_CUDA(cudaMalloc(&w->matIdx, idx.size()));
+			ALIS_CUDA(cudaMemcpy(w->matIdx, idx.data(), idx.size(), cudaMemcpyHostToDevice));
+			ALIS_CUDA(cudaMalloc(&w->matTab, tab.size() * sizeof(float4)));
+			ALIS_CUDA(cudaMemcpy(w->matTab, tab.data(), tab.size() * sizeof(float4), cudaMemcpyHostToDevice));
+		}
+	}
 	return ALISGPU_OK;
 }
 
@@ -852,7 +891,15 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
 	const bool hasC = P.C[0] != 0;
 	float cx = 1, cy = 1, cz = 1;
-	if (hasC) cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
+	if (hasC) {
+		if (P.matIdx) {
+			// the same floats from the table of distinct triples
+			const float4 t = __ldg(P.matTab + __ldg(P.matIdx + c));
+			cx = t.x, cy = t.y, cz = t.z;
+		} else {
+			cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
+		}
+	}
 	// curl (reference src/update.c:109-118)
 	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
 	if (hasC) {
@@ -1367,6 +1414,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			P.C[c] = field == 0 ? w->C[c] : 0;
 			P.Fother[c] = w->E[m][c];
 		}
+		P.matIdx = field == 0 ? w->matIdx : 0;
+		P.matTab = field == 0 ? w->matTab : 0;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
 		int slot = alisgpu__prof_start();
 		if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
