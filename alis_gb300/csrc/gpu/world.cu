@@ -845,7 +845,9 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 	__shared__ int nlist;
 	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
 	const int j = P.jMIN + blockIdx.y * TY_ + threadIdx.y;
-	const int i = P.iMIN + blockIdx.z;
+	// E sweeps i downwards, H upwards: each starts on the planes the other
+	// touched last, which are still in L2
+	const int i = ALT == 1 ? P.iMAX - (int)blockIdx.z : P.iMIN + (int)blockIdx.z;
 	const bool manyObj = P.nobj > 8;
 	if (manyObj) {
 		// objects whose box meets this tile, in list order (one warp)
