@@ -32,7 +32,7 @@ CFLAGS = ["-std=gnu99", "-O3", "-fPIC", "-fopenmp", "-ffp-contract=off", "-w",
 HOST_SOURCES = ["world.c", "object.c", "shapes.c", "source.c", "phaser.c", "farfld.c",
                 "fields.c", "output.c", "slices.c", "timer.c"]
 # (source, exact-rounding)
-CUDA_SOURCES = [("world.cu", True), ("phaser.cu", True), ("farfield.cu", False)]
+CUDA_SOURCES = [("world.cu", True), ("phaser.cu", True), ("voxel.cu", True), ("farfield.cu", False)]
 
 
 def _cuda_home():

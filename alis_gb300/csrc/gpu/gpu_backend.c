@@ -685,3 +685,181 @@ int alis_gpu_farfield(phaser P, int nA, const tfield *T, const float *kx, const 
 	free(tab); free(Td); free(pr); free(kxd); free(kyd); free(part);
 	return rc;
 }
+
+
+/* ---- voxelization (reference src/object.c:70-121, 229-279) ----
+ * The object list becomes a node array for the device shape predicates:
+ * list objects first, members of compound shapes after their owner.  The
+ * shape is told by its function; a list holding a shape the device does
+ * not evaluate (ImportContour, user functions) stays with the host loops.
+ * The host supplies every sample coordinate through the world's own
+ * itox/jtoy/ktoz and the glibc trigonometric values of rotations.
+ * ALISGPU_VOXELIZE=host leaves every list to the host loops. */
+
+#define VOX_MAX_DEPTH 12   /* nesting the device recursion allows */
+
+typedef struct {
+	alisgpu_vox_node *node;
+	int n, cap;
+	float *pool;
+	int npool, pcap;
+} voxList;
+
+static int shapeTypeOf(shape *S)
+{
+	static shape *const known[ALISGPU_SHAPE_COUNT] = {
+		[ALISGPU_SHAPE_BOX] = Box, [ALISGPU_SHAPE_BALL] = Ball, [ALISGPU_SHAPE_DIAMOND] = Diamond,
+		[ALISGPU_SHAPE_BICONEX] = BiconeX, [ALISGPU_SHAPE_BICONEY] = BiconeY, [ALISGPU_SHAPE_BICONEZ] = BiconeZ,
+		[ALISGPU_SHAPE_RODX] = RodX, [ALISGPU_SHAPE_RODY] = RodY, [ALISGPU_SHAPE_RODZ] = RodZ,
+		[ALISGPU_SHAPE_DRODX] = DRodX, [ALISGPU_SHAPE_DRODY] = DRodY, [ALISGPU_SHAPE_DRODZ] = DRodZ,
+		[ALISGPU_SHAPE_HRODXY] = HRodXY, [ALISGPU_SHAPE_HRODYZ] = HRodYZ, [ALISGPU_SHAPE_HRODZX] = HRodZX,
+		[ALISGPU_SHAPE_HRODXZ] = HRodXZ, [ALISGPU_SHAPE_HRODYX] = HRodYX, [ALISGPU_SHAPE_HRODZY] = HRodZY,
+		[ALISGPU_SHAPE_TRANSLATION] = Translation, [ALISGPU_SHAPE_ROTATION] = Rotation,
+		[ALISGPU_SHAPE_COMBINATION] = Combination, [ALISGPU_SHAPE_INTERSECTION] = Intersection,
+		[ALISGPU_SHAPE_DIFFERENCE] = Difference, [ALISGPU_SHAPE_LATTICE] = Lattice, [ALISGPU_SHAPE_DLATTICE] = DLattice,
+		[ALISGPU_SHAPE_CLATTICEX] = CLatticeX, [ALISGPU_SHAPE_CLATTICEY] = CLatticeY, [ALISGPU_SHAPE_CLATTICEZ] = CLatticeZ,
+	};
+	for (int t = 0; t < ALISGPU_SHAPE_COUNT; t++) if (S && S == known[t]) return t;
+	return -1;
+}
+
+/* count new zeroed nodes; index of the first */
+static int voxNodes(voxList *L, int count)
+{
+	if (L->n + count > L->cap) {
+		L->cap = 2 * (L->n + count) + 16;
+		L->node = realloc(L->node, L->cap * sizeof *L->node);
+	}
+	memset(L->node + L->n, 0, count * sizeof *L->node);
+	L->n += count;
+	return L->n - count;
+}
+
+static int voxPool(voxList *L, int count)
+{
+	if (L->npool + count > L->pcap) {
+		L->pcap = 2 * (L->npool + count) + 16;
+		L->pool = realloc(L->pool, L->pcap * sizeof *L->pool);
+	}
+	L->npool += count;
+	return L->npool - count;
+}
+
+/* node id from object O and its members; 0 if the device cannot evaluate it */
+static int voxObject(voxList *L, int id, object O, int depth)
+{
+	int t = shapeTypeOf(O.S);
+	if (t < 0 || depth > VOX_MAX_DEPTH) return 0;
+	alisgpu_vox_node *x = &L->node[id];
+	x->type = t;
+	memcpy(x->f, O.f, sizeof x->f);
+	int members = 0;
+	switch (t) {
+	case ALISGPU_SHAPE_ROTATION:
+		/* the values Rotation computes (reference src/shapes.c:133-140) */
+		x->rot[0] = cosf(O.f[0][0]*PI/180.), x->rot[1] = sinf(O.f[0][0]*PI/180.);
+		x->rot[2] = cosf(O.f[0][1]*PI/180.), x->rot[3] = sinf(O.f[0][1]*PI/180.);
+		x->rot[4] = cosf(O.f[0][2]*PI/180.), x->rot[5] = sinf(O.f[0][2]*PI/180.);
+		members = 1;
+		break;
+	case ALISGPU_SHAPE_CLATTICEX: case ALISGPU_SHAPE_CLATTICEY: case ALISGPU_SHAPE_CLATTICEZ: {
+		/* the angles CLatticeX/Y/Z step through (reference src/shapes.c:193-221) */
+		int N = O.f[0][0];
+		int at = voxPool(L, N > 0 ? 2 * N : 0);
+		for (int n = 0; n < N; n++) {
+			float t = 2 * PI * n / N;
+			L->pool[at + n] = cosf(t), L->pool[at + N + n] = sinf(t);
+		}
+		L->node[id].trig = at;
+		members = 1;
+		break;
+	}
+	case ALISGPU_SHAPE_TRANSLATION: case ALISGPU_SHAPE_LATTICE: case ALISGPU_SHAPE_DLATTICE:
+		members = 1;
+		break;
+	case ALISGPU_SHAPE_COMBINATION: case ALISGPU_SHAPE_INTERSECTION: case ALISGPU_SHAPE_DIFFERENCE:
+		members = O.f[0][0];
+		if (members < 0) members = 0;
+		if (t == ALISGPU_SHAPE_DIFFERENCE && members < 1) return 0;
+		break;
+	}
+	if (!members) return 1;
+	if (!O.p) return 0;
+	int c = voxNodes(L, members);
+	L->node[id].child = c, L->node[id].nchild = members;
+	object *m = O.p;
+	for (int n = 0; n < members; n++) if (!voxObject(L, c + n, m[n], depth + 1)) return 0;
+	return 1;
+}
+
+/* sample coordinates of one axis over indices lo..hi: kinds n - 1/2, n,
+ * n + 1/2, each moved by the offsets fillFactor applies (reference
+ * src/object.c:84-121) in the slot order the device expects */
+static float *voxTable(world W, float (*itox)(world, float), int lo, int hi, int nslot)
+{
+	int subN = W->subN;
+	float h = (subN-1.0) / (subN*2.0);
+	float *tab = malloc((size_t)(1 + hi - lo) * 3 * nslot * sizeof *tab);
+	for (int n = lo; n <= hi; n++) for (int kind = 0; kind < 3; kind++) {
+		float b = kind == 0 ? n-0.5 : kind == 1 ? n : n+0.5;
+		float *s = tab + ((size_t)(n - lo) * 3 + kind) * nslot;
+		s[0] = itox(W, b);
+		s[1] = itox(W, b-0.5);
+		s[2] = itox(W, b+0.5);
+		if (nslot > 3) {
+			s[3] = itox(W, b+(-1)*h);
+			s[4] = itox(W, b+1*h);
+			for (int q = 0, di = 1-subN; di < subN; q++, di += 2) s[5+q] = itox(W, b+0.5*di/subN);
+		}
+	}
+	return tab;
+}
+
+void *alis_be_vox_begin(world W, object *O, int N)
+{
+	const char *e = getenv("ALISGPU_VOXELIZE");
+	/* the supersampling counts hits exactly up to 2^24 samples */
+	if (N <= 0 || W->subN > 256 || (e && !strcmp(e, "host"))) return NULL;
+	voxList L = { 0 };
+	voxNodes(&L, N);
+	int ok = 1;
+	for (int o = 0; o < N && ok; o++) ok = voxObject(&L, o, O[o], 0);
+	alisgpu_voxelizer *v = NULL;
+	if (ok) {
+		int nslot = W->subN >= 2 ? 5 + W->subN : 3;
+		int MIN[3] = { W->iMIN, W->jMIN, W->kMIN }, MAX[3] = { W->iMAX, W->jMAX, W->kMAX };
+		int lo[3], hi[3];
+		float (*itox[3])(world, float) = { W->itox, W->jtoy, W->ktoz };
+		float *tab[3];
+		for (int a = 0; a < 3; a++) lo[a] = MIN[a] - 1, hi[a] = MAX[a] + 2, tab[a] = voxTable(W, itox[a], lo[a], hi[a], nslot);
+		CHECK("voxelizer_create", alisgpu_voxelizer_create(L.node, L.n, L.pool, L.npool, (const float *const *)tab, lo, hi,
+		                                                   nslot, W->subN, MIN, MAX, &v));
+		for (int a = 0; a < 3; a++) free(tab[a]);
+	}
+	free(L.node);
+	free(L.pool);
+	return v;
+}
+
+int alis_be_vox_bounds(void *v, int N, int *box)
+{
+	CHECK("voxelizer_bounds", alisgpu_voxelizer_bounds(v, N, box));
+	return 1;
+}
+
+int alis_be_vox_fill(void *v, int o, const int *b, float *fx, float *fy, float *fz)
+{
+	CHECK("voxelizer_fill", alisgpu_voxelizer_fill(v, o, b[0], b[1], b[2], b[3], b[4], b[5], fx, fy, fz));
+	return 1;
+}
+
+int alis_be_vox_fill_edge(void *v, int o, int axis, int n, int u0, int u1, int v0, int v1, float *out)
+{
+	CHECK("voxelizer_fill_edge", alisgpu_voxelizer_fill_edge(v, o, axis, n, u0, u1, v0, v1, out));
+	return 1;
+}
+
+void alis_be_vox_end(void *v)
+{
+	if (v) alisgpu_voxelizer_destroy(v);
+}

@@ -66,6 +66,19 @@ int alis_be_object_absorption(world W, int n, float *out);
 /* second-order coupling of WS to the pumps WP1, WP2 (reference
  * src/update.c:343-411) */
 void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt);
+/* Voxelization of the object list O[0..N-1] on the backend (reference
+ * src/object.c:70-121, 229-279): a handle, or NULL when the host loops do
+ * it (a shape the backend does not evaluate).  With a handle: box[6 o..]
+ * = iMin, iMax, jMin, jMax, kMin, kMax of the cell centres object o owns
+ * first; the fill factors of object o at (i - 1/2, j, k), (i, j - 1/2, k),
+ * (i, j, k - 1/2) over the index box b[6], as box arrays (k fastest); and
+ * those at index n + 1/2 of axis over the plane [u0,u1] x [v0,v1] of the
+ * other two axes.  Each returns 0 when the host is to do the work. */
+void *alis_be_vox_begin(world W, object *O, int N);
+int alis_be_vox_bounds(void *v, int N, int *box);
+int alis_be_vox_fill(void *v, int o, const int *b, float *fx, float *fy, float *fz);
+int alis_be_vox_fill_edge(void *v, int o, int axis, int n, int u0, int u1, int v0, int v1, float *out);
+void alis_be_vox_end(void *v);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

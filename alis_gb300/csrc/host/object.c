@@ -138,11 +138,12 @@ static float fillFactor(world W, object *O, int o, float i, float j, float k)
 /* Index box of the cell centres owned by each object, padded by -1/+2
  * and clamped to the grid.  An object that owns no centre stops the
  * program, as in the reference. */
-static bounds *objectBounds(world W, object *O, int N)
+static bounds *objectBounds(world W, object *O, int N, void *vox)
 {
 	bounds *B;
 	MALLOC(B, 0, N);
 	for (int o = 0; o < N; o++) B[o] = (bounds){ W->iMAX, W->iMIN, W->jMAX, W->jMIN, W->kMAX, W->kMIN };
+	if (!(vox && alis_be_vox_bounds(vox, N, &B[0].iMin)))
 	#pragma omp parallel
 	{
 		bounds *b;
@@ -239,8 +240,11 @@ static void dispersiveBox(world W, coeffs *C, int n, bounds B)
 /* fill maps, conductivity factors and pole coefficients of dispersive
  * object n = list entry o; m = 1 for anisotropic matter, whose poles come
  * in x/y/z triples (reference src/object.c:290-336) */
-static void dispersiveCoeffs(world W, coeffs *C, matter *M, object *O, int n, int o, int m)
+static void dispersiveCoeffs(world W, coeffs *C, matter *M, object *O, int n, int o, int m, void *vox)
 {
+	int box[6] = { C->iMin[n], C->iMax[n], C->jMin[n], C->jMax[n], C->kMin[n], C->kMax[n] };
+	float *at[3] = { &C->Jx[n][box[0]][box[2]][box[4]], &C->Jy[n][box[0]][box[2]][box[4]], &C->Jz[n][box[0]][box[2]][box[4]] };
+	if (!(vox && alis_be_vox_fill(vox, o, box, at[0], at[1], at[2])))
 	#pragma omp parallel for schedule(guided)
 	for (int i = C->iMin[n]; i <= C->iMax[n]; i++) for (int j = C->jMin[n]; j <= C->jMax[n]; j++) for (int k = C->kMin[n]; k <= C->kMax[n]; k++) {
 		C->Jx[n][i][j][k] = fillFactor(W, O, o, i-0.5, j, k);
@@ -290,6 +294,44 @@ static void dispersiveCoeffs(world W, coeffs *C, matter *M, object *O, int n, in
  * the staggered grid where the box touches the grid edge */
 #define HARMONIC(map, i, j, k, d, fill) ((map)[i][j][k] = 1 / (1 / (map)[i][j][k] + (d) * (fill)))
 
+/* the non-dispersive branch of putObjectArray with fill factors from the
+ * backend's voxelizer; 0 when the host loops are to do it */
+static int harmonicOnDevice(world W, coeffs *C, object *O, void *vox, int o, bounds b, float cx, float cy, float cz)
+{
+	long NI = 1 + b.iMax - b.iMin, NJ = 1 + b.jMax - b.jMin, NK = 1 + b.kMax - b.kMin;
+	float *f = malloc(3 * NI * NJ * NK * sizeof *f);
+	if (!f || !alis_be_vox_fill(vox, o, &b.iMin, f, f + NI*NJ*NK, f + 2*NI*NJ*NK)) {
+		free(f);
+		return 0;
+	}
+	float *fx = f, *fy = f + NI*NJ*NK, *fz = f + 2*NI*NJ*NK;
+	#pragma omp parallel for
+	for (int i = b.iMin; i <= b.iMax; i++) for (int j = b.jMin; j <= b.jMax; j++) for (int k = b.kMin; k <= b.kMax; k++) {
+		long t = ((i - b.iMin) * NJ + (j - b.jMin)) * NK + (k - b.kMin);
+		HARMONIC(C->x, i, j, k, cx, fx[t]);
+		HARMONIC(C->y, i, j, k, cy, fy[t]);
+		HARMONIC(C->z, i, j, k, cz, fz[t]);
+	}
+	/* the far plane of the staggered grid where the box touches the edge */
+	if (b.iMax == W->iMAX) {
+		int dev = alis_be_vox_fill_edge(vox, o, 0, b.iMax, b.jMin, b.jMax, b.kMin, b.kMax, f);
+		for (int j = b.jMin; j <= b.jMax; j++) for (int k = b.kMin; k <= b.kMax; k++)
+			HARMONIC(C->x, b.iMax+1, j, k, cx, dev ? f[(j - b.jMin) * NK + (k - b.kMin)] : fillFactor(W, O, o, b.iMax+0.5, j, k));
+	}
+	if (b.jMax == W->jMAX) {
+		int dev = alis_be_vox_fill_edge(vox, o, 1, b.jMax, b.iMin, b.iMax, b.kMin, b.kMax, f);
+		for (int i = b.iMin; i <= b.iMax; i++) for (int k = b.kMin; k <= b.kMax; k++)
+			HARMONIC(C->y, i, b.jMax+1, k, cy, dev ? f[(i - b.iMin) * NK + (k - b.kMin)] : fillFactor(W, O, o, i, b.jMax+0.5, k));
+	}
+	if (b.kMax == W->kMAX) {
+		int dev = alis_be_vox_fill_edge(vox, o, 2, b.kMax, b.iMin, b.iMax, b.jMin, b.jMax, f);
+		for (int i = b.iMin; i <= b.iMax; i++) for (int j = b.jMin; j <= b.jMax; j++)
+			HARMONIC(C->z, i, j, b.kMax+1, cz, dev ? f[(i - b.iMin) * NJ + (j - b.jMin)] : fillFactor(W, O, o, i, j, b.kMax+0.5));
+	}
+	free(f);
+	return 1;
+}
+
 void putObjectArray(world W, matter *M, object *O)
 {
 	removeObjects(W);
@@ -297,7 +339,8 @@ void putObjectArray(world W, matter *M, object *O)
 	for (N = 0; O[N].S; N++) if (alis_needs_currents(M[N])) W->CE->N++;
 	printf("\rPreparing to put %d objects.\n", N);
 	W->subN = W->Res.spec.subN = W->Res.spec.subN ? W->Res.spec.subN : W->CE->N ? 1 : 12;
-	bounds *B = objectBounds(W, O, N);
+	void *vox = alis_be_vox_begin(W, O, N);
+	bounds *B = objectBounds(W, O, N, vox);
 	coeffs *C = W->CE;
 	alis_alloc_current_tables(W, W->E, C->N);
 	allocCoeffTables(W, C);
@@ -325,7 +368,7 @@ void putObjectArray(world W, matter *M, object *O)
 			}
 			if (m) C->NJ[n] /= 3, C->NK[n] /= 3;
 			dispersiveBox(W, C, n, b);
-			dispersiveCoeffs(W, C, M, O, n, o, m);
+			dispersiveCoeffs(W, C, M, O, n, o, m, vox);
 			float ****fx = C->Jx, ****fy = C->Jy, ****fz = C->Jz;
 			#pragma omp parallel for schedule(guided)
 			for (int i = b.iMin; i <= b.iMax; i++) for (int j = b.jMin; j <= b.jMax; j++) for (int k = b.kMin; k <= b.kMax; k++) {
@@ -339,6 +382,7 @@ void putObjectArray(world W, matter *M, object *O)
 				HARMONIC(C->y, i, b.jMax+1, k, cy, fy[n][i][b.jMax+1][k]);
 			if (b.kMax == W->kMAX) for (int i = b.iMin; i <= b.iMax; i++) for (int j = b.jMin; j <= b.jMax; j++)
 				HARMONIC(C->z, i, j, b.kMax+1, cz, fz[n][i][j][b.kMax+1]);
+		} else if (vox && harmonicOnDevice(W, C, O, vox, o, b, cx, cy, cz)) {
 		} else {
 			#pragma omp parallel for schedule(guided)
 			for (int i = b.iMin; i <= b.iMax; i++) for (int j = b.jMin; j <= b.jMax; j++) for (int k = b.kMin; k <= b.kMax; k++) {
@@ -355,6 +399,7 @@ void putObjectArray(world W, matter *M, object *O)
 		}
 	}
 	free(B);
+	alis_be_vox_end(vox);
 	printf("\rPutting objects: %d done.\n", N);
 	fflush(stdout);
 	alis_be_objects_changed(W);

@@ -205,6 +205,48 @@ int alisgpu_object_absorption(alisgpu_world *w, int n, float *out);
 int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
                           const float d[3][6], float Alt);
 
+/* ---- voxelization (reference src/object.c:70-121, 229-279; src/shapes.c:9-221) ----
+ * An object list as a node array: nodes 0..N-1 are the list's objects in
+ * order, compound shapes point at their members further on.  Sample
+ * coordinates come from host tables tab[a][((n - lo[a]) * 3 + kind) *
+ * nslot + slot]: index n of axis a at n - 1/2, n, n + 1/2 (kind 0, 1, 2)
+ * moved by slot 0: none, 1: -1/2, 2: +1/2, 3: -h, 4: +h, 5 + q: the q-th
+ * sub-grid offset of the fill factor (subN >= 2). */
+enum {
+	ALISGPU_SHAPE_BOX, ALISGPU_SHAPE_BALL, ALISGPU_SHAPE_DIAMOND, ALISGPU_SHAPE_BICONEX, ALISGPU_SHAPE_BICONEY,
+	ALISGPU_SHAPE_BICONEZ, ALISGPU_SHAPE_RODX, ALISGPU_SHAPE_RODY, ALISGPU_SHAPE_RODZ, ALISGPU_SHAPE_DRODX,
+	ALISGPU_SHAPE_DRODY, ALISGPU_SHAPE_DRODZ, ALISGPU_SHAPE_HRODXY, ALISGPU_SHAPE_HRODYZ, ALISGPU_SHAPE_HRODZX,
+	ALISGPU_SHAPE_HRODXZ, ALISGPU_SHAPE_HRODYX, ALISGPU_SHAPE_HRODZY, ALISGPU_SHAPE_TRANSLATION, ALISGPU_SHAPE_ROTATION,
+	ALISGPU_SHAPE_COMBINATION, ALISGPU_SHAPE_INTERSECTION, ALISGPU_SHAPE_DIFFERENCE, ALISGPU_SHAPE_LATTICE,
+	ALISGPU_SHAPE_DLATTICE, ALISGPU_SHAPE_CLATTICEX, ALISGPU_SHAPE_CLATTICEY, ALISGPU_SHAPE_CLATTICEZ,
+	ALISGPU_SHAPE_COUNT
+};
+
+typedef struct alisgpu_vox_node {
+	int type;                                   /* ALISGPU_SHAPE_* */
+	float f[3][3];                              /* the object's parameters */
+	int child, nchild;                          /* first member node and count */
+	float rot[6];                               /* rotation: cos, sin about x, y, z */
+	int trig;                                   /* rotational lattice: N cos then N sin in pool */
+} alisgpu_vox_node;
+
+typedef struct alisgpu_voxelizer alisgpu_voxelizer;
+
+int alisgpu_voxelizer_create(const alisgpu_vox_node *nodes, int nnode, const float *pool, int npool,
+                             const float *const tab[3], const int lo[3], const int hi[3], int nslot, int subN,
+                             const int MIN[3], const int MAX[3], alisgpu_voxelizer **v);
+int alisgpu_voxelizer_destroy(alisgpu_voxelizer *v);
+/* per object the index box of the cell centres it owns first:
+ * box[6 o] = iMin, iMax, jMin, jMax, kMin, kMax (min > max: none) */
+int alisgpu_voxelizer_bounds(alisgpu_voxelizer *v, int nobj, int *box);
+/* fill factors of object o at (i - 1/2, j, k), (i, j - 1/2, k), (i, j, k - 1/2)
+ * over a box, as box arrays */
+int alisgpu_voxelizer_fill(alisgpu_voxelizer *v, int o, int i0, int i1, int j0, int j1, int k0, int k1,
+                           float *fx, float *fy, float *fz);
+/* fill factors at index n + 1/2 of axis over the plane [u0,u1] x [v0,v1] of
+ * the other two axes in increasing order */
+int alisgpu_voxelizer_fill_edge(alisgpu_voxelizer *v, int o, int axis, int n, int u0, int u1, int v0, int v1, float *out);
+
 /* ---- phasers (reference src/phaser.c:21-110) ---- */
 
 typedef struct alisgpu_phaser alisgpu_phaser;

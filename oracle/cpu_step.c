@@ -622,6 +622,12 @@ int alis_be_sync_box(world W, int i0, int i1, int j0, int j1, int k0, int k1)
 }
 void alis_be_hold_sync(world W) { (void)W; }
 int alis_be_object_absorption(world W, int n, float *out) { (void)W, (void)n, (void)out; return 0; }
+void *alis_be_vox_begin(world W, object *O, int N) { (void)W, (void)O, (void)N; return NULL; }
+int alis_be_vox_bounds(void *v, int N, int *box) { (void)v, (void)N, (void)box; return 0; }
+int alis_be_vox_fill(void *v, int o, const int *b, float *fx, float *fy, float *fz) { (void)v, (void)o, (void)b, (void)fx, (void)fy, (void)fz; return 0; }
+int alis_be_vox_fill_edge(void *v, int o, int axis, int n, int u0, int u1, int v0, int v1, float *out)
+{ (void)v, (void)o, (void)axis, (void)n, (void)u0, (void)u1, (void)v0, (void)v1, (void)out; return 0; }
+void alis_be_vox_end(void *v) { (void)v; }
 /* --- second-order coupling (reference src/update.c:343-411) ---
  * term by term over the box of dispersive object n (less its last plane
  * on every axis): E_a += 2 Alt d C_a fill_a (G1 G2), the pump components

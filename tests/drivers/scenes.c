@@ -29,6 +29,10 @@
  *   sym     dipole on two symmetry planes, Drude-Lorentz sphere
  *   hbc     hexagonal-Bloch lattice slab with an iHz dipole
  *   multi   overlapping Drude-Lorentz spheres in a dielectric host
+ *   shapes  every shape of the object API, nested compounds, plain and
+ *           dispersive matter; 4^3 supersampling (shapespt: point
+ *           samples, shapesedge: the edge rule)
+ *   contour a height-map object, filled by the host loops
  */
 #include <alis.h>
 #include "dump.h"
@@ -375,6 +379,101 @@ static void sceneBowtie(int steps)
 	dumpPhasers(P, "P");
 }
 
+/* every shape of the object API in one list: basic shapes, translated,
+ * rotated, set operations, finite, doubled, infinite and rotational
+ * lattices, nested up to three deep; plain and dispersive matter,
+ * overlaps resolved by list order, sub-pixel filling by subN
+ * (supersampling, point samples or the edge rule for subN < 0) */
+static void sceneShapes(int steps, int subN)
+{
+	float L = 200 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {5, {10}, {1240, subN}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	matter Drude = {{2.0}, {{8.0, 0.05}}};
+	matter Lorentz = {{2.5}, {{4.0, 0.1, 0.8}}};
+	float zb[2] = { -130, -70 };
+#define AT(x, y) {{(x) - 28, (x) + 28}, {(y) - 28, (y) + 28}, {zb[0], zb[1]}}
+	object O[] = {
+		/* basic shapes, z in [-130, -70] */
+		{Ball, AT(-120, -120)}, {Diamond, AT(-40, -120)}, {BiconeX, AT(40, -120)}, {BiconeY, AT(120, -120)},
+		{BiconeZ, AT(-120, -40)}, {RodX, AT(-40, -40)}, {RodY, AT(40, -40)}, {RodZ, AT(120, -40)},
+		{DRodX, AT(-120, 40)}, {DRodY, AT(-40, 40)}, {DRodZ, AT(40, 40)}, {HRodXY, AT(120, 40)},
+		{HRodYZ, AT(-120, 120)}, {HRodZX, AT(-40, 120)}, {HRodXZ, AT(40, 120)}, {HRodYX, AT(120, 120)},
+		/* compound shapes, z around 0 */
+		{HRodZY, {{-150, -90}, {-150, -90}, {-30, 30}}},
+		{Translation, {{-40, -120, 0}}, objects {{Ball, {{-25, 25}, {-20, 20}, {-30, 30}}}}},
+		{Rotation, {{30, 20, 45}, {40, -120, 0}}, objects {{Box, {{-25, 25}, {-15, 15}, {-20, 20}}}}},
+		{Difference, {{2}}, objects {
+			{Box, {{95, 150}, {-150, -95}, {-25, 25}}},
+			{Ball, {{110, 140}, {-140, -110}, {-40, 40}}}}},
+		{Combination, {{3}}, objects {
+			{Box, {{-150, -110}, {-60, -20}, {-20, 20}}},
+			{RodX, {{-110, -60}, {-50, -30}, {-15, 15}}},
+			{Intersection, {{2}}, objects {
+				{Ball, {{-75, -25}, {-65, -15}, {-25, 25}}},
+				{Box, {{-60, -20}, {-80, 0}, {-10, 30}}}}}}},
+		{Translation, {{80, -40, 0}}, objects {{Lattice, {{25, 3}, {25, 2}, {0}}, objects {
+			{Ball, {{-8, 8}, {-9, 9}, {-20, 20}}}}}}},
+		{Translation, {{-80, 40, 0}}, objects {{DLattice, {{22, 3}, {22, 3}, {0}}, objects {
+			{Box, {{-6, 6}, {-6, 6}, {-25, 25}}}}}}},
+		{CLatticeZ, {{5}, {80, 40}}, objects {{RodZ, {{95, 112}, {32, 48}, {-30, 30}}}}},
+		{CLatticeX, {{6}, {120, 0}}, objects {{Ball, {{-150, -95}, {128, 146}, {-9, 9}}}}},
+		{CLatticeY, {{4}, {-40, 0}}, objects {{RodY, {{-28, -12}, {100, 150}, {12, 28}}}}},
+		{Intersection, {{2}}, objects {
+			{Box, {{20, 150}, {100, 150}, {-30, 30}}},
+			{Lattice, {{25, 0}, {0}, {0}}, objects {{RodY, {{-6, 6}, {-INF, INF}, {-20, 20}}}}}}},
+		/* a dispersive slab on top, partly under earlier objects, and a
+		 * rotated compound */
+		{Box, {{-150, 150}, {-150, 0}, {60, 110}}},
+		{Rotation, {{-20, 35, 10}, {60, 80, 90}}, objects {{Combination, {{2}}, objects {
+			{RodZ, {{-12, 12}, {-12, 12}, {-25, 25}}},
+			{Translation, {{10, 0, 0}}, objects {{Box, {{-5, 25}, {-5, 5}, {-20, 20}}}}}}}}},
+		{0},
+	};
+#undef AT
+	int N = sizeof O / sizeof *O - 1;
+	matter M[sizeof O / sizeof *O];
+	for (int o = 0; o < N; o++) M[o] = n(1.3 + 0.07 * o);
+	M[7] = Drude, M[19] = Lorentz, M[24] = Drude, M[27] = Lorentz;
+	M[N] = Air;
+	putObjectArray(W, M, O);
+	pointDipole(W, Ez, 5, -10, 0, Band, 400, 800);
+	phaser P = createPhasers(W, 400, 800, 200, -L+50, L-50, -L+50, L-50, -L+50, L-50);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
+/* a height-map object (ImportContour) in the list: filled by the host
+ * loops, as are lists holding any shape outside the object API's own */
+static float contourMap[16][16], *contourRows[16];
+
+static void sceneContour(int steps)
+{
+	float L = 160 * scale;
+	dom D = {{-L, L}, {-L, L}, {-L, L}};
+	res R = {5, {10}, {1240, 3}};
+	sur S = {{PML}, {PML}, {PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	for (int i = 0; i < 16; i++) {
+		contourRows[i] = contourMap[i];
+		for (int j = 0; j < 16; j++) contourMap[i][j] = (i - 7.5f) * (i - 7.5f) + 0.5f * (j - 7.5f) * (j - 7.5f);
+	}
+	object Hill = {Intersection, {{2}}, objects {
+		{Box, {{-INF, INF}, {-INF, INF}, {-40, 40}}},
+		{ImportContour, {{-100, 100, 16}, {-100, 100, 16}, {0, 30}}, contourRows}}};
+	object Cap = {Ball, {{-50, 50}, {-50, 50}, {20, 80}}};
+	matter Drude = {{2.0}, {{8.0, 0.05}}};
+	putObjects(W, Drude, Cap, n(2), Hill, Air);
+	pointDipole(W, Ex, 5, -10, 100, Band, 400, 800);
+	phaser P = createPhasers(W, 400, 800, 200, -L+50, L-50, -L+50, L-50, -L+50, L-50);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -399,6 +498,10 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "spheres")) sceneSpheres(steps);
 	else if (!strcmp(s, "unitcell")) sceneUnitCell(steps);
 	else if (!strcmp(s, "bowtie")) sceneBowtie(steps);
+	else if (!strcmp(s, "shapes")) sceneShapes(steps, 4);
+	else if (!strcmp(s, "shapespt")) sceneShapes(steps, 1);
+	else if (!strcmp(s, "shapesedge")) sceneShapes(steps, -1);
+	else if (!strcmp(s, "contour")) sceneContour(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

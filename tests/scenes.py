@@ -39,6 +39,12 @@ CASES = [
     ("spheres", 1, 80),
     ("unitcell", 1, 120),
     ("bowtie", 1, 80),
+    # the voxelizer: every shape of the object API with 4^3 supersampling,
+    # point samples and the edge rule; a height map filled on the host
+    ("shapes", 1, 40),
+    ("shapespt", 1, 40),
+    ("shapesedge", 1, 40),
+    ("contour", 1, 40),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
