@@ -189,6 +189,10 @@ struct alisgpu_world {
 	// before the host reads E (same bytes: each copy is a function of the
 	// current interior E)
 	std::vector<alisgpu_ghost_copy> pendingE;
+	// per field: the last ghost list seen and whether its chains qualify
+	// for the one-launch form (k_ghost_chain)
+	std::vector<alisgpu_ghost_copy> ghostSeen[2];
+	bool ghostChain[2];
 	float *planeTab;                       // scratch of the observer kernels
 	size_t planeTabFloats;
 	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
@@ -1044,6 +1048,78 @@ __global__ void __launch_bounds__(256) k_ghost_levels(const __grid_constant__ Gh
 	}
 }
 
+// All ghost copies of a half step in one plain launch.  The value a copy
+// leaves in a cell comes down a short chain: the copy reads a cell that an
+// earlier copy of the component wrote, that copy read another, and so on
+// back to a root cell that no earlier copy wrote.  One thread per cell
+// that keeps its value (no later copy of the component writes it) walks
+// its chain back to the root and applies the copies forward, in the
+// reference's order with the reference's arithmetic -- the bytes the
+// sequential copies leave.  The list qualifies when no root is a cell that
+// any copy writes (then no thread reads what another writes) and no chain
+// is deeper than ALIS_GHOST_CHAIN; the CHECK instance tests that once per
+// list, otherwise the list keeps the level-ordered cooperative launch.
+#define ALIS_GHOST_CHAIN 8
+
+__device__ __forceinline__ bool inCopy(const alisgpu_ghost_copy &c, int i, int j, int k)
+{
+	return c.i0 <= i && i <= c.i1 && c.j0 <= j && j <= c.j1 && c.k0 <= k && k <= c.k1;
+}
+
+template <bool CHECK>
+__global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ GhostLevels P, unsigned int *flag)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= P.start[P.n]) return;
+	int q = 0;
+	while (t >= P.start[q + 1]) q++;
+	const alisgpu_ghost_copy &g = P.c[q];
+	const int r = t - P.start[q];
+	const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
+	const int i = g.i0 + r / (nk * nj), j = g.j0 + (r / nk) % nj, k = g.k0 + r % nk;
+	for (int p = q + 1; p < P.n; p++) if (P.c[p].comp == g.comp && inCopy(P.c[p], i, j, k)) return;
+	const Layout &L = P.L;
+	int chain[ALIS_GHOST_CHAIN], depth = 0, cur = q, ci = i, cj = j, ck = k;
+	for (;;) {
+		if (depth == ALIS_GHOST_CHAIN) {
+			atomicOr(CHECK ? flag : P.err, CHECK ? 1u : 2u);
+			return;
+		}
+		chain[depth++] = cur;
+		const alisgpu_ghost_copy &c = P.c[cur];
+		ci += c.di, cj += c.dj, ck += c.dk;
+		int prev = -1;
+		for (int p = cur - 1; p >= 0; p--) if (P.c[p].comp == g.comp && inCopy(P.c[p], ci, cj, ck)) { prev = p; break; }
+		if (prev < 0) break;
+		cur = prev;
+	}
+	if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk ||
+	    ci < L.i0 || ci >= L.i0 + L.ni || cj < L.j0 || cj >= L.j0 + L.nj || ck < L.k0 || ck >= L.k0 + L.nk) {
+		atomicOr(P.err, 2u);
+		return;
+	}
+	if (CHECK) {
+		for (int p = 0; p < P.n; p++) if (P.c[p].comp == g.comp && inCopy(P.c[p], ci, cj, ck)) { atomicOr(flag, 2u); return; }
+		return;
+	}
+	const long long s = L.at(ci, cj, ck), d = L.at(i, j, k);
+	float *F = P.F[0][g.comp];
+	if (P.complexField) {
+		float *G = P.F[1][g.comp];
+		float f = F[s], gg = G[s];
+		for (int l = depth - 1; l >= 0; l--) {
+			const alisgpu_ghost_copy &c = P.c[chain[l]];
+			const float nf = c.cosk * f + c.sink * gg, ng = c.cosk * gg - c.sink * f;
+			f = nf, gg = ng;
+		}
+		F[d] = f, G[d] = gg;
+	} else {
+		float f = F[s];
+		for (int l = depth - 1; l >= 0; l--) f = P.c[chain[l]].cosk * f;
+		F[d] = f;
+	}
+}
+
 // Small worlds (the TFSF auxiliary columns, tiny test worlds): the whole
 // half step -- every cell of every m, then the source patches in list
 // order, then the ghost copies one after another -- in one block, with a
@@ -1207,6 +1283,39 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
 			int mm = m <= g.complexField ? m : 0;
 			GL.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		// the one-launch form, copies in the reference's order
+		std::vector<alisgpu_ghost_copy> &seen = w->ghostSeen[field];
+		const bool same = seen.size() == (size_t)n && !memcmp(seen.data(), gl, n * sizeof *gl);
+		if (!same || w->ghostChain[field]) {
+			int at = 0;
+			for (int q = 0; q < n; q++) GL.c[q] = gl[q], GL.start[q] = at, at += (int)cells[q];
+			GL.n = n, GL.start[n] = at;
+			const unsigned blocks = (unsigned)((total + 255) / 256);
+			if (!same) {
+				seen.assign(gl, gl + n);
+				unsigned int *flag = 0, h = 0;
+				ALIS_CUDA(cudaMalloc(&flag, sizeof h));
+				ALIS_CUDA(cudaMemsetAsync(flag, 0, sizeof h, gStream));
+				k_ghost_chain<true><<<blocks, 256, 0, gStream>>>(GL, flag);
+				alisgpu__count_launch();
+				ALIS_CUDA(cudaGetLastError());
+				ALIS_CUDA(cudaMemcpyAsync(&h, flag, sizeof h, cudaMemcpyDeviceToHost, gStream));
+				ALIS_CUDA(cudaStreamSynchronize(gStream));
+				cudaFree(flag);
+				w->ghostChain[field] = h == 0;
+			}
+			if (w->ghostChain[field]) {
+				int slot = alisgpu__prof_start();
+				k_ghost_chain<false><<<blocks, 256, 0, gStream>>>(GL, nullptr);
+				alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
+				alisgpu__count_launch();
+				ALIS_CUDA(cudaGetLastError());
+				return ALISGPU_OK;
+			}
+			memset(GL.c, 0, sizeof GL.c);
+			memset(GL.start, 0, sizeof GL.start);
+			GL.n = 0;
 		}
 		int at = 0;
 		for (int l = 0; l < nlev; l++) {
