@@ -50,6 +50,14 @@ typedef struct devPhaser {
 static devWorld *worlds, *lastWorld;
 static devPhaser *phasers;
 
+/* a sliceFreqDom accumulator on the device; h is 0 once its world is gone */
+typedef struct devSliceDft {
+	devWorld *d;
+	alisgpu_slice_dft *h;
+	struct devSliceDft *next;
+} devSliceDft;
+static devSliceDft *sliceDfts;
+
 static void die(const char *what, int rc)
 {
 	fprintf(stderr, "alis: %s failed (%d): %s\n", what, rc, alisgpu_last_error());
@@ -113,6 +121,8 @@ void alis_be_world_deleted(world W)
 	devWorld *d = *pp;
 	*pp = d->next;
 	if (lastWorld == d) lastWorld = 0;
+	for (devSliceDft *s = sliceDfts; s; s = s->next)
+		if (s->d == d) alisgpu_slice_dft_destroy(s->h), s->h = 0, s->d = 0;
 	for (int q = 0; q < d->ntf; q++) alisgpu__forget_tfsf(&d->tf[q]);
 	alisgpu_world_destroy(d->dw);
 	free(d);
@@ -862,4 +872,70 @@ int alis_be_vox_fill_edge(void *v, int o, int axis, int n, int u0, int u1, int v
 void alis_be_vox_end(void *v)
 {
 	if (v) alisgpu_voxelizer_destroy(v);
+}
+
+
+/* ---- sliceFreqDom's running DFT (reference src/slices.c:326-356) ----
+ * Field functions that sample E or H (src/fields.c:130-291) run on the
+ * device; the others (currents, incident and scattered fields) stay with
+ * the host loop over the synced box. */
+
+static int sampleOf(field *F, int *fld, int *m, int *comp, int *avg, int sgn[3])
+{
+	static const struct { field *F; int fld, m, comp, avg, s[3]; } tab[] = {
+		{ rawEx, 0, 0, 0, 0, { 1, -1, -1 } }, { rawEy, 0, 0, 1, 0, { -1, 1, -1 } }, { rawEz, 0, 0, 2, 0, { -1, -1, 1 } },
+		{ rawHx, 1, 0, 0, 0, { -1, 1, 1 } }, { rawHy, 1, 0, 1, 0, { 1, -1, 1 } }, { rawHz, 1, 0, 2, 0, { 1, 1, -1 } },
+		{ Ex, 0, 0, 0, 1, { 1, -1, -1 } }, { Ey, 0, 0, 1, 1, { -1, 1, -1 } }, { Ez, 0, 0, 2, 1, { -1, -1, 1 } },
+		{ iEx, 0, 1, 0, 1, { 1, -1, -1 } }, { iEy, 0, 1, 1, 1, { -1, 1, -1 } }, { iEz, 0, 1, 2, 1, { -1, -1, 1 } },
+		{ Hx, 1, 0, 0, 1, { -1, 1, 1 } }, { Hy, 1, 0, 1, 1, { 1, -1, 1 } }, { Hz, 1, 0, 2, 1, { 1, 1, -1 } },
+		{ iHx, 1, 1, 0, 1, { -1, 1, 1 } }, { iHy, 1, 1, 1, 1, { 1, -1, 1 } }, { iHz, 1, 1, 2, 1, { 1, 1, -1 } },
+	};
+	for (int n = 0; n < (int)(sizeof tab / sizeof *tab); n++) if (tab[n].F == F) {
+		*fld = tab[n].fld, *m = tab[n].m, *comp = tab[n].comp, *avg = tab[n].avg;
+		for (int a = 0; a < 3; a++) sgn[a] = tab[n].s[a];
+		return 1;
+	}
+	return 0;
+}
+
+void *alis_be_slice_dft_begin(world W, const int box[6])
+{
+	devWorld *d = findWorld(W);
+	if (!d) return NULL;
+	alisgpu_slice_dft *h = NULL;
+	CHECK("slice_dft_create", alisgpu_slice_dft_create(d->dw, box, &h));
+	devSliceDft *s = calloc(1, sizeof *s);
+	s->d = d, s->h = h, s->next = sliceDfts, sliceDfts = s;
+	return s;
+}
+
+int alis_be_slice_dft_add(void *v, world W, field *F, float re, float im)
+{
+	devSliceDft *s = v;
+	int fld, m, comp, avg, sgn[3];
+	if (!s || !s->h || s->d->W != W || !sampleOf(F, &fld, &m, &comp, &avg, sgn)) return 0;
+	/* the mirror parities the field functions apply: sign times the Bloch cosine */
+	int sym[3] = { W->xMinSur == SYM, W->yMinSur == SYM, W->zMinSur == SYM };
+	float par[3] = { sgn[0] * W->coskx, sgn[1] * W->cosky, sgn[2] * W->coskz };
+	CHECK("slice_dft_add", alisgpu_slice_dft_add(s->h, fld, m, comp, avg, sym, par, re, im));
+	return 1;
+}
+
+int alis_be_slice_dft_read(void *v, float *F, float *G)
+{
+	devSliceDft *s = v;
+	if (!s || !s->h) return 0;
+	CHECK("slice_dft_download", alisgpu_slice_dft_download(s->h, F, G));
+	return 1;
+}
+
+void alis_be_slice_dft_end(void *v)
+{
+	devSliceDft *s = v;
+	if (!s) return;
+	devSliceDft **pp = &sliceDfts;
+	while (*pp && *pp != s) pp = &(*pp)->next;
+	if (*pp) *pp = s->next;
+	if (s->h) alisgpu_slice_dft_destroy(s->h);
+	free(s);
 }

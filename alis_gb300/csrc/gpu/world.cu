@@ -1796,6 +1796,147 @@ extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int 
 }
 
 // ---------------------------------------------------------------------
+// Running DFT of sliceFreqDom (reference src/slices.c:326-356) over a box:
+// F += f(i,j,k) * re, G += f(i,j,k) * im with f one of the E/H samples of
+// the field functions (reference src/fields.c:130-291): a raw component,
+// E averaged over its two samples, H over its four, with the mirror
+// parities of symmetry planes, in their float arithmetic.  The sums stay
+// on the device until the slice is written.
+// ---------------------------------------------------------------------
+struct alisgpu_slice_dft {
+	alisgpu_world *w;
+	int i0, i1, j0, j1, k0, k1;
+	float *acc;                                // F then G, box arrays (k fastest)
+};
+
+struct SliceDftParams {
+	Layout L;
+	const float *F;                            // the sampled component (E or H, m)
+	int kind;                                  // 0 raw, 1 E pair, 2 H quad; -1: zero (imaginary part of a real field)
+	int d1, d2;                                // offsets of the second (and third) sample
+	float base;                                // 1, 0.5, 0.25
+	int sym[3];
+	float par[3];
+	int i0, j0, k0, ni, nj, nk;
+	float re, im;
+	float *acc;
+};
+
+__global__ void k_slice_dft(const SliceDftParams P)
+{
+	const int cells = P.ni * P.nj * P.nk;
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= cells) return;
+	int k = P.k0 + t % P.nk, j = P.j0 + (t / P.nk) % P.nj, i = P.i0 + t / (P.nk * P.nj);
+	float v = 0;
+	if (P.kind >= 0) {
+		float p = P.base;
+		if (P.sym[0] && i < 0) i = -i, p *= P.par[0];
+		if (P.sym[1] && j < 0) j = -j, p *= P.par[1];
+		if (P.sym[2] && k < 0) k = -k, p *= P.par[2];
+		const long long c = P.L.at(i, j, k);
+		if (P.kind == 0) v = p * P.F[c];
+		else if (P.kind == 1) v = p * (P.F[c] + P.F[c + P.d1]);
+		else v = p * (P.F[c] + P.F[c + P.d1] + P.F[c + P.d2] + P.F[c + P.d1 + P.d2]);
+	}
+	P.acc[t] += v * P.re;
+	P.acc[t + cells] += v * P.im;
+}
+
+extern "C" int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alisgpu_slice_dft **out)
+{
+	if (!w || !box || !out || box[1] < box[0] || box[3] < box[2] || box[5] < box[4])
+		return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_create: bad argument");
+	const size_t cells = (size_t)(1 + box[1] - box[0]) * (1 + box[3] - box[2]) * (1 + box[5] - box[4]);
+	if (2 * cells >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "slice_dft_create: box of %zu cells too large", cells);
+	alisgpu_slice_dft *d = new alisgpu_slice_dft();
+	d->w = w;
+	d->i0 = box[0], d->i1 = box[1], d->j0 = box[2], d->j1 = box[3], d->k0 = box[4], d->k1 = box[5];
+	cudaError_t e = cudaMalloc(&d->acc, 2 * cells * sizeof(float));
+	if (e == cudaSuccess) e = cudaMemsetAsync(d->acc, 0, 2 * cells * sizeof(float), gStream);
+	if (e != cudaSuccess) {
+		cudaFree(d->acc);
+		delete d;
+		return alisgpu__check(e, "slice_dft_create");
+	}
+	*out = d;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int comp, int avg, const int sym[3], const float par[3],
+                                     float re, float im)
+{
+	if (!d || field < 0 || field > 1 || m < 0 || m > 1 || comp < 0 || comp > 2 || avg < 0 || avg > 1 || !sym || !par)
+		return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_add: bad argument");
+	alisgpu_world *w = d->w;
+	const alisgpu_geometry &g = w->g;
+	const Layout &L = w->L;
+	SliceDftParams P;
+	memset(&P, 0, sizeof P);
+	P.L = L;
+	// the indices read, after mirroring, and one cell beyond: inside the halo'd grid
+	const int lo[3] = { d->i0, d->j0, d->k0 }, hi[3] = { d->i1, d->j1, d->k1 };
+	const int L0[3] = { L.i0, L.j0, L.k0 }, LN[3] = { L.ni, L.nj, L.nk };
+	for (int a = 0; a < 3; a++) {
+		P.sym[a] = sym[a] != 0, P.par[a] = par[a];
+		int mn = lo[a], mx = hi[a];
+		if (P.sym[a] && lo[a] < 0) {
+			if (hi[a] < 0) mn = -hi[a], mx = -lo[a];
+			else mn = 0, mx = std::max(hi[a], -lo[a]);
+		}
+		if (mn < L0[a] || mx + 1 >= L0[a] + LN[a]) return alisgpu__fail(ALISGPU_ERANGE, "slice_dft_add: box outside the grid");
+	}
+	if (m > g.complexField) {
+		P.kind = -1;
+	} else {
+		P.F = field == 0 ? w->E[m][comp] : w->H[m][comp];
+		const long long st[3] = { L.si, L.sj, 1 };
+		if (!avg) P.kind = 0, P.base = 1.0f;
+		else if (field == 0) P.kind = 1, P.base = 0.5f, P.d1 = (int)st[comp];
+		else {
+			// H: the two axes other than its own, in the reference's order
+			const int a1 = comp == 0 ? 1 : comp == 1 ? 2 : 0, a2 = comp == 0 ? 2 : comp == 1 ? 0 : 1;
+			P.kind = 2, P.base = 0.25f, P.d1 = (int)st[a1], P.d2 = (int)st[a2];
+		}
+	}
+	// E's upper halo (written by the deferred ghost copies) is read at the box's upper edge
+	if (field == 0 && P.kind >= 0 && (d->i1 >= g.iMAX || d->j1 >= g.jMAX || d->k1 >= g.kMAX || P.sym[0] || P.sym[1] || P.sym[2])) {
+		int rc = applyPendingGhosts(w);
+		if (rc) return rc;
+	}
+	P.i0 = d->i0, P.j0 = d->j0, P.k0 = d->k0;
+	P.ni = 1 + d->i1 - d->i0, P.nj = 1 + d->j1 - d->j0, P.nk = 1 + d->k1 - d->k0;
+	P.re = re, P.im = im;
+	P.acc = d->acc;
+	const int cells = P.ni * P.nj * P.nk;
+	int slot = alisgpu__prof_start();
+	k_slice_dft<<<(unsigned)((cells + 255) / 256), 256, 0, gStream>>>(P);
+	alisgpu__prof_stop(slot, ALISGPU_K_GATHER);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_slice_dft_download(alisgpu_slice_dft *d, float *F, float *G)
+{
+	if (!d || !F || !G) return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_download: bad argument");
+	const size_t cells = (size_t)(1 + d->i1 - d->i0) * (1 + d->j1 - d->j0) * (1 + d->k1 - d->k0);
+	ALIS_CUDA(cudaMemcpyAsync(F, d->acc, cells * sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaMemcpyAsync(G, d->acc + cells, cells * sizeof(float), cudaMemcpyDeviceToHost, gStream));
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_slice_dft_destroy(alisgpu_slice_dft *d)
+{
+	if (!d) return ALISGPU_OK;
+	cudaStreamSynchronize(gStream);
+	cudaFree(d->acc);
+	delete d;
+	return ALISGPU_OK;
+}
+
+// ---------------------------------------------------------------------
 // Power absorbed by dispersive object n (reference src/output.c:359-435):
 // J . E over the object's box with the reference's arithmetic in its
 // order as one OpenMP thread runs it.  The three column sums along k of

@@ -66,6 +66,15 @@ int alis_be_object_absorption(world W, int n, float *out);
 /* second-order coupling of WS to the pumps WP1, WP2 (reference
  * src/update.c:343-411) */
 void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt);
+/* The running DFT of sliceFreqDom over the index box b[6] kept by the
+ * backend (reference src/slices.c:326-356): a handle or NULL.  add: one
+ * call's F += f * re, G += f * im; 0 when the backend does not evaluate
+ * field function f (the host loop then takes over after read).  read:
+ * the sums as box arrays (k fastest); 0 when there are none. */
+void *alis_be_slice_dft_begin(world W, const int b[6]);
+int alis_be_slice_dft_add(void *h, world W, field *f, float re, float im);
+int alis_be_slice_dft_read(void *h, float *F, float *G);
+void alis_be_slice_dft_end(void *h);
 /* Voxelization of the object list O[0..N-1] on the backend (reference
  * src/object.c:70-121, 229-279): a handle, or NULL when the host loops do
  * it (a shape the backend does not evaluate).  With a handle: box[6 o..]

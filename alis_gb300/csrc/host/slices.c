@@ -259,6 +259,7 @@ typedef struct sliceq {
 	char *name;
 	float max, Max, ***F, ***G;
 	long N;
+	void *dev;                /* sliceFreqDom: the sums kept by the backend */
 	struct sliceq *next;
 } sliceq;
 
@@ -374,19 +375,28 @@ void (sliceFreqDom)(world W, field F, slice S, char *f, char *s, int N, float L,
 	va_end(ap);
 	expandName(filename, f, s);
 	sliceq *q = track(W, filename, M, &head);
+	int box[6] = { S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax };
+	float *F0 = 0, *G0 = 0;
 	if (q->N == 1) {
 		q->F = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
 		q->G = makeField(S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+		q->dev = alis_be_slice_dft_begin(W, box);
 	}
-	int held = syncSlice(W, S);
+	F0 = &q->F[S->iMin][S->jMin][S->kMin], G0 = &q->G[S->iMin][S->jMin][S->kMin];
 	float re = cosf(2 * PI * q->N * W->dt / L);
 	float im = sinf(2 * PI * q->N * W->dt / L);
-	for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++) {
-		q->F[i][j][k] += F(W, i, j, k) * re;
-		q->G[i][j][k] += F(W, i, j, k) * im;
+	if (!(q->dev && alis_be_slice_dft_add(q->dev, W, F, re, im))) {
+		/* a field function the backend does not evaluate: the sums so far come to the host */
+		if (q->dev) alis_be_slice_dft_read(q->dev, F0, G0), alis_be_slice_dft_end(q->dev), q->dev = 0;
+		int held = syncSlice(W, S);
+		for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++) {
+			q->F[i][j][k] += F(W, i, j, k) * re;
+			q->G[i][j][k] += F(W, i, j, k) * im;
+		}
+		releaseSlice(held);
 	}
-	releaseSlice(held);
 	if (q->N % N) return;
+	if (q->dev) alis_be_slice_dft_read(q->dev, F0, G0);
 	if (Max <= 0) {
 		float max = 0;
 		for (int i = S->iMin; i <= S->iMax; i++) for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)

@@ -205,6 +205,23 @@ int alisgpu_object_absorption(alisgpu_world *w, int n, float *out);
 int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
                           const float d[3][6], float Alt);
 
+/* ---- frequency-domain slices (reference src/slices.c:326-356) ----
+ * The running DFT sliceFreqDom keeps over a slice box: per call
+ * F += f * re, G += f * im for every cell, f the sample of a field
+ * function of src/fields.c:130-291 -- component comp of E (field 0) or H
+ * (field 1), real (m 0) or imaginary (m 1) set, raw (avg 0) or averaged
+ * (avg 1: E over its two samples along its axis, H over its four around
+ * the cell's centre line) -- mirrored on the symmetry planes of the axes
+ * with sym[a] != 0 with parity par[a] (the reference's sign times the
+ * Bloch cosine).  The sums stay on the device until downloaded as box
+ * arrays (k fastest), F then G. */
+typedef struct alisgpu_slice_dft alisgpu_slice_dft;
+int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alisgpu_slice_dft **d);
+int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int comp, int avg, const int sym[3], const float par[3],
+                          float re, float im);
+int alisgpu_slice_dft_download(alisgpu_slice_dft *d, float *F, float *G);
+int alisgpu_slice_dft_destroy(alisgpu_slice_dft *d);
+
 /* ---- voxelization (reference src/object.c:70-121, 229-279; src/shapes.c:9-221) ----
  * An object list as a node array: nodes 0..N-1 are the list's objects in
  * order, compound shapes point at their members further on.  Sample

@@ -66,13 +66,63 @@ static void farSamples(phaser P, const char *tag)
 	}
 }
 
+/* called after every step of run() when set: per-step observers */
+static void (*perStep)(world W, int n, int steps);
+
 static void run(world W, phaser P, int steps)
 {
 	for (int n = 1; n <= steps; n++) {
 		updateE(W);
 		updateH(W);
 		if (P) updatePhaser(W, P);
+		if (perStep) perStep(W, n, steps);
 	}
+}
+
+/* a slice writer that dumps frames 1 and 4 (phase 0 and 90 degrees) of
+ * each sliceFreqDom output and the scale it was given */
+static void dumpFrames(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
+{
+	(void)W, (void)F, (void)cmap;
+	size_t n = strlen(filename);
+	if (n < 2 || (strcmp(filename + n - 2, "01") && strcmp(filename + n - 2, "04"))) return;
+	static int count;
+	char nm[160];
+	snprintf(nm, sizeof nm, "FD.%s.%d", filename, count);
+	dumpField(nm, S->F, S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+	snprintf(nm, sizeof nm, "FD.%s.%d.max", filename, count++);
+	dumpScalar(nm, Max);
+}
+
+/* frequency-domain slices: E/H samples the device accumulates, and
+ * currents and incident/scattered fields the host loop does */
+static slice fdA, fdB;
+
+static void fdSym(world W, int n, int steps)
+{
+	(void)n;
+	sliceFreqDom(W, Ex, fdA, steps / 2, 600, dumpFrames, "a%%");
+	sliceFreqDom(W, Hz, fdA, steps / 2, 550, dumpFrames, "a%%");
+	sliceFreqDom(W, rawEy, fdB, steps / 2, 600, dumpFrames, "b%%");
+	sliceFreqDom(W, Jx, fdA, steps / 2, 600, dumpFrames, "a%%");
+}
+
+static void fdBloch(world W, int n, int steps)
+{
+	(void)n;
+	sliceFreqDom(W, Ex, fdA, steps / 2, 550, dumpFrames, "a%%");
+	sliceFreqDom(W, iEx, fdA, steps / 2, 550, dumpFrames, "a%%");
+	sliceFreqDom(W, iHy, fdB, steps / 2, 550, dumpFrames, "b%%");
+	sliceFreqDom(W, rawHz, fdB, steps / 2, 500, dumpFrames, "b%%");
+}
+
+static void fdC2(world W, int n, int steps)
+{
+	(void)n;
+	sliceFreqDom(W, Ez, fdA, steps / 2, 600, dumpFrames, "a%%");
+	sliceFreqDom(W, Hy, fdB, steps / 2, 600, dumpFrames, "b%%");
+	sliceFreqDom(W, ScEx, fdA, steps / 2, 600, dumpFrames, "a%%");
+	sliceFreqDom(W, Jx, fdB, steps / 2, 600, dumpFrames, "b%%");
 }
 
 static void sceneC1(int steps)
@@ -103,6 +153,9 @@ static void sceneC2(int steps)
 	putObjects(W, seededGold(1234), Block, Air);
 	planewave(W, T, Ppol, 0, 0, Pulse, 600, 200);
 	phaser P = createPhasers(W, 400, 800, 400.0/7, -L+6, L-8, -L+6, L-8, -L+6, L-8);
+	fdA = createSlice(W, -INF, INF, 0, 0, -INF, INF);
+	fdB = createSlice(W, -30, 30, -20, 20, L-12, L-12);
+	perStep = fdC2;
 	run(W, P, steps);
 	dumpScalar("S.abs", objectAbsorption(W, Block));
 	dumpWorld(W, "W");
@@ -146,6 +199,9 @@ static void sceneBloch(int steps)
 	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {-200, 250}};
 	planewave(W, T, Ppol, 150, 0, Pulse, 550, 120);
 	phaser P = createPhasers(W, 450, 700, 125, -INF, INF, -INF, INF, -250, -250);
+	fdA = createSlice(W, -INF, INF, 0, 0, -INF, INF);
+	fdB = createSlice(W, -INF, INF, -INF, INF, 150, 150);
+	perStep = fdBloch;
 	run(W, P, steps);
 	dumpScalar("S.abs", objectAbsorption(W, Pillar));
 	dumpWorld(W, "W");
@@ -165,6 +221,10 @@ static void sceneSym(int steps)
 	putObjects(W, DL, Sphere, Air);
 	pointDipole(W, Ex, 0, 0, -20, Band, 400, 800);
 	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
+	/* slices reaching across the symmetry planes (mirrored samples) */
+	fdA = createSlice(W, -60, 60, -60, 60, 40, 40);
+	fdB = createSlice(W, -70, 70, 10, 10, -20, -20);
+	perStep = fdSym;
 	run(W, P, steps);
 	dumpScalar("S.abs", objectAbsorption(W, Sphere));
 	dumpWorld(W, "W");
