@@ -32,6 +32,12 @@ struct alisgpu_phaser {
 	float2 *comp;                         // Kahan compensation (or null)
 	float2 *phase;                        // [ring][nfreq][2] (E, H)
 	std::vector<float2> hostPhase;        // phases of buffered steps
+	// pinned staging of the phases, two in turn, so that their upload is
+	// asynchronous (a pageable copy may wait for the stream to drain)
+	float2 *pinned[2];
+	cudaEvent_t pinnedFree[2];
+	size_t pinnedCap;
+	int pinnedNext;
 	int *faceInfo;                        // per face: axis, box
 	int used;                             // buffered steps
 	float *fluxTab;                       // spacing tables and sums of the flux kernels
@@ -201,6 +207,7 @@ extern "C" int alisgpu_phaser_destroy(alisgpu_phaser *p)
 	if (p->comp) cudaFree(p->comp);
 	if (p->phase) cudaFree(p->phase);
 	if (p->fluxTab) cudaFree(p->fluxTab);
+	for (int b = 0; b < 2; b++) if (p->pinned[b]) cudaFreeHost(p->pinned[b]), cudaEventDestroy(p->pinnedFree[b]);
 	delete p;
 	return ALISGPU_OK;
 }
@@ -210,7 +217,28 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_flush: null phaser");
 	if (!p->used || !p->cells) { p->used = 0; p->hostPhase.clear(); return ALISGPU_OK; }
 	cudaStream_t st = alisgpu__stream();
-	ALIS_CUDA(cudaMemcpyAsync(p->phase, p->hostPhase.data(), p->hostPhase.size() * sizeof(float2), cudaMemcpyHostToDevice, st));
+	const size_t nph = p->hostPhase.size();
+	if (nph > p->pinnedCap) {
+		for (int b = 0; b < 2; b++) {
+			if (p->pinned[b]) {
+				ALIS_CUDA(cudaEventSynchronize(p->pinnedFree[b]));
+				ALIS_CUDA(cudaFreeHost(p->pinned[b]));
+				p->pinned[b] = 0;
+			} else {
+				ALIS_CUDA(cudaEventCreateWithFlags(&p->pinnedFree[b], cudaEventDisableTiming));
+				ALIS_CUDA(cudaEventRecord(p->pinnedFree[b], st));
+			}
+			ALIS_CUDA(cudaMallocHost(&p->pinned[b], nph * sizeof(float2)));
+		}
+		p->pinnedCap = nph;
+	}
+	// the buffer's last upload (two flushes back) has left it
+	const int b = p->pinnedNext;
+	p->pinnedNext ^= 1;
+	ALIS_CUDA(cudaEventSynchronize(p->pinnedFree[b]));
+	memcpy(p->pinned[b], p->hostPhase.data(), nph * sizeof(float2));
+	ALIS_CUDA(cudaMemcpyAsync(p->phase, p->pinned[b], nph * sizeof(float2), cudaMemcpyHostToDevice, st));
+	ALIS_CUDA(cudaEventRecord(p->pinnedFree[b], st));
 	long long n4 = p->cells * 4;
 	dim3 grid((unsigned)((n4 + FLUSH_THREADS - 1) / FLUSH_THREADS), (p->nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ);
 	size_t smem = (size_t)p->used * FLUSH_FREQ * 2 * sizeof(float2);

@@ -1022,6 +1022,7 @@ __global__ void k_ghost(const GhostParams P)
 // a grid-wide barrier separates the levels.  The driver guarantees that
 // all blocks of a cooperative launch are resident, so the barrier ends.
 #define ALIS_GHOST_MAX 48
+#define ALIS_GHOST_NEAR 6
 struct GhostLevels {
 	Layout L;
 	float *F[2][3];
@@ -1031,6 +1032,12 @@ struct GhostLevels {
 	int start[ALIS_GHOST_MAX + 1];            // first cell of each copy (below 2^31)
 	int levStart[ALIS_GHOST_MAX + 1];         // first copy of each level
 	unsigned int *err;
+	// one-launch form: per copy the copies of its component that can matter
+	// to its cells -- later copies whose boxes meet its write box, earlier
+	// copies whose boxes meet its read box (ALIS_GHOST_NEAR at most, else
+	// -1: test every copy)
+	signed char nLater[ALIS_GHOST_MAX], nEarlier[ALIS_GHOST_MAX];
+	unsigned char later[ALIS_GHOST_MAX][ALIS_GHOST_NEAR], earlier[ALIS_GHOST_MAX][ALIS_GHOST_NEAR];
 };
 
 __global__ void __launch_bounds__(256) k_ghost_levels(const __grid_constant__ GhostLevels P)
@@ -1077,7 +1084,12 @@ __global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ Gho
 	const int r = t - P.start[q];
 	const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0;
 	const int i = g.i0 + r / (nk * nj), j = g.j0 + (r / nk) % nj, k = g.k0 + r % nk;
-	for (int p = q + 1; p < P.n; p++) if (P.c[p].comp == g.comp && inCopy(P.c[p], i, j, k)) return;
+	// kept by a later copy?  (the candidates are in increasing order)
+	if (P.nLater[q] < 0) {
+		for (int p = q + 1; p < P.n; p++) if (P.c[p].comp == g.comp && inCopy(P.c[p], i, j, k)) return;
+	} else {
+		for (int n = 0; n < P.nLater[q]; n++) if (inCopy(P.c[P.later[q][n]], i, j, k)) return;
+	}
 	const Layout &L = P.L;
 	int chain[ALIS_GHOST_CHAIN], depth = 0, cur = q, ci = i, cj = j, ck = k;
 	for (;;) {
@@ -1088,8 +1100,13 @@ __global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ Gho
 		chain[depth++] = cur;
 		const alisgpu_ghost_copy &c = P.c[cur];
 		ci += c.di, cj += c.dj, ck += c.dk;
+		// the last earlier copy that wrote the cell read (candidates in decreasing order)
 		int prev = -1;
-		for (int p = cur - 1; p >= 0; p--) if (P.c[p].comp == g.comp && inCopy(P.c[p], ci, cj, ck)) { prev = p; break; }
+		if (P.nEarlier[cur] < 0) {
+			for (int p = cur - 1; p >= 0; p--) if (P.c[p].comp == g.comp && inCopy(P.c[p], ci, cj, ck)) { prev = p; break; }
+		} else {
+			for (int n = 0; n < P.nEarlier[cur]; n++) if (inCopy(P.c[P.earlier[cur][n]], ci, cj, ck)) { prev = P.earlier[cur][n]; break; }
+		}
 		if (prev < 0) break;
 		cur = prev;
 	}
@@ -1291,6 +1308,29 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 			int at = 0;
 			for (int q = 0; q < n; q++) GL.c[q] = gl[q], GL.start[q] = at, at += (int)cells[q];
 			GL.n = n, GL.start[n] = at;
+			// candidate lists: copies of the component whose boxes meet the
+			// write box (later) or the read box (earlier, nearest first)
+			for (int q = 0; q < n; q++) {
+				const alisgpu_ghost_copy &c = gl[q];
+				const int Wq[6] = { c.i0, c.i1, c.j0, c.j1, c.k0, c.k1 };
+				const int Rq[6] = { c.i0 + c.di, c.i1 + c.di, c.j0 + c.dj, c.j1 + c.dj, c.k0 + c.dk, c.k1 + c.dk };
+				int nl = 0, ne = 0;
+				for (int p = q + 1; p < n; p++) {
+					const alisgpu_ghost_copy &e = gl[p];
+					const int Wp[6] = { e.i0, e.i1, e.j0, e.j1, e.k0, e.k1 };
+					if (e.comp != c.comp || !cells[p] || !boxesMeet(Wp, Wq)) continue;
+					if (nl >= 0 && nl < ALIS_GHOST_NEAR) GL.later[q][nl++] = (unsigned char)p;
+					else nl = -1;
+				}
+				for (int p = q - 1; p >= 0; p--) {
+					const alisgpu_ghost_copy &e = gl[p];
+					const int Wp[6] = { e.i0, e.i1, e.j0, e.j1, e.k0, e.k1 };
+					if (e.comp != c.comp || !cells[p] || !boxesMeet(Wp, Rq)) continue;
+					if (ne >= 0 && ne < ALIS_GHOST_NEAR) GL.earlier[q][ne++] = (unsigned char)p;
+					else ne = -1;
+				}
+				GL.nLater[q] = (signed char)nl, GL.nEarlier[q] = (signed char)ne;
+			}
 			const unsigned blocks = (unsigned)((total + 255) / 256);
 			if (!same) {
 				seen.assign(gl, gl + n);
