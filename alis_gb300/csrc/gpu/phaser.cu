@@ -55,6 +55,8 @@ struct GatherParams {
 };
 
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L);
+extern "C" cudaStream_t alisgpu__gather_begin(alisgpu_world *w, const int (*box)[6], int n);
+extern "C" int alisgpu__gather_end(alisgpu_world *w, cudaStream_t st);
 
 __global__ void k_phaser_gather(const GatherParams P)
 {
@@ -273,11 +275,22 @@ extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, con
 			memcpy(G.box[f], b, sizeof b);
 		}
 		G.out = p->buf + (size_t)p->used * p->cells * 4;
+		// H is read on each face and one cell beyond it along the face axis
+		int reads[6][6];
+		for (int f = 0; f < p->nface; f++) {
+			const alisgpu_face &a = p->faces[f];
+			int b[6] = { a.i0, a.i1, a.j0, a.j1, a.k0, a.k1 };
+			b[2 * a.axis + 1]++;
+			memcpy(reads[f], b, sizeof b);
+		}
+		cudaStream_t st = alisgpu__gather_begin(p->w, reads, p->nface);
 		int slot = alisgpu__prof_start();
-		k_phaser_gather<<<(unsigned)((p->cells + 255) / 256), 256, 0, alisgpu__stream()>>>(G);
+		k_phaser_gather<<<(unsigned)((p->cells + 255) / 256), 256, 0, st>>>(G);
 		alisgpu__prof_stop(slot, ALISGPU_K_GATHER);
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
+		int rc2 = alisgpu__gather_end(p->w, st);
+		if (rc2) return rc2;
 	}
 	for (int f = 0; f < p->nfreq; f++) {
 		p->hostPhase.push_back(make_float2(phaseE[2 * f], phaseE[2 * f + 1]));

@@ -57,6 +57,11 @@ extern "C" int alisgpu__check(cudaError_t e, const char *what)
 // issued before it.
 static cudaStream_t gSide;
 static cudaEvent_t gEvMainDone[2], gEvAuxDone[2], gEvJoin;
+// phaser gathers that run beside the H ghost copies (a second side stream)
+static cudaStream_t gGather;
+static cudaEvent_t gEvGatherDone;
+// operations that change world data, enqueued so far (launches and uploads)
+static unsigned long long gOps;
 static int gMainRec[2], gAuxRec[2], gSideUsed, gSideWaitsAll = 1;
 
 static void fullJoin(void)
@@ -69,7 +74,7 @@ static void fullJoin(void)
 }
 
 extern "C" const char *alisgpu_last_error(void) { return gErr; }
-extern "C" void alisgpu__count_launch(void) { gLaunches++; }
+extern "C" void alisgpu__count_launch(void) { gLaunches++, gOps++; }
 extern "C" unsigned long long alisgpu_launch_count(void) { return gLaunches; }
 extern "C" cudaStream_t alisgpu__stream(void) { return gStream; }
 extern "C" void *alisgpu_stream(void) { return (void *)gStream; }
@@ -93,6 +98,8 @@ extern "C" int alisgpu_init(void)
 		ALIS_CUDA(cudaEventCreateWithFlags(&gEvAuxDone[f], cudaEventDisableTiming));
 	}
 	ALIS_CUDA(cudaEventCreateWithFlags(&gEvJoin, cudaEventDisableTiming));
+	ALIS_CUDA(cudaStreamCreateWithFlags(&gGather, cudaStreamNonBlocking));
+	ALIS_CUDA(cudaEventCreateWithFlags(&gEvGatherDone, cudaEventDisableTiming));
 	ALIS_CUDA(cudaMalloc(&gErrWord, sizeof(unsigned int)));
 	ALIS_CUDA(cudaMemset(gErrWord, 0, sizeof(unsigned int)));
 	gInit = 1;
@@ -193,6 +200,13 @@ struct alisgpu_world {
 	// for the one-launch form (k_ghost_chain)
 	std::vector<alisgpu_ghost_copy> ghostSeen[2];
 	bool ghostChain[2];
+	// the last H half step: its ghost copies, an event after its cell
+	// updates, and the operation count after its ghost launch (a phaser
+	// gather that follows directly may run beside the ghost copies)
+	std::vector<alisgpu_ghost_copy> hGhosts;
+	cudaEvent_t evHCells;
+	unsigned long long hOps;
+	bool hRecorded;
 	float *planeTab;                       // scratch of the observer kernels
 	size_t planeTabFloats;
 	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
@@ -297,6 +311,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 	}
 	freeObjects(w);
 	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) cudaFree(w->cls[f][a]);
+	if (w->evHCells) cudaEventDestroy(w->evHCells);
 	delete w;
 	return ALISGPU_OK;
 }
@@ -305,6 +320,7 @@ extern "C" size_t alisgpu_world_bytes(const alisgpu_world *w) { return w ? w->by
 
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
+	gOps++;
 	fullJoin();
 	if (w) w->pendingE.clear();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_reset: null world");
@@ -509,6 +525,7 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 
 extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
 {
+	gOps++;
 	fullJoin();
 	if (w && field == 0) w->pendingE.clear();        // the host's halo wins
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
@@ -820,14 +837,6 @@ __device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int
 	stepCell<ALT>(P, i, j, k, list, nIter);
 }
 
-// Fused half step of a large world, one thread per cell, one i plane per
-// block of TX x TY threads.  Tiers by the cell's class bits: plain cells
-// take the curl only; CPML cells and cells on TFSF k face planes add
-// their face updates, all inline; cells on TFSF i or j face planes (whole
-// blocks or warps) and dispersive cells go to hardCell.  Index
-// arithmetic is 32-bit (at most 2^31 elements per array, checked on the
-// host).  Worlds with more than 8 objects add a per-block list of the
-// objects that meet the tile.
 #define TX 32
 // launch shapes, measured on the 256^3 dispersive world: 32x4 threads,
 // 16 blocks per SM (32 registers) for both fields; -D overrides for tuning
@@ -841,13 +850,87 @@ __device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int
 #endif
 #define STEP_TY(ALT) ((ALT) == 1 ? ALIS_E_TY : ALIS_H_TY)
 #define STEP_MINB(ALT) ((ALT) == 1 ? ALIS_E_MINB : ALIS_H_MINB)
+// The lean tiers for NC cells k, k + TX, ... of one row, all in range and
+// none of them hard: the loads of every cell first, then the updates, so
+// the cells' memory round trips overlap and share their index arithmetic.
+template <int ALT, int NC>
+__device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j, int k, unsigned bi, unsigned bj, const unsigned *bk)
+{
+	const int sj = (int)P.L.sj, si = (int)P.L.si;
+	const int c0 = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	float gx0[NC], gy0[NC], gz0[NC], gyk[NC], gxk[NC], gzj[NC], gxj[NC], gzi[NC], gyi[NC];
+	float fx[NC], fy[NC], fz[NC], cx[NC], cy[NC], cz[NC], dz[NC];
+	const bool hasC = P.C[0] != 0;
+#pragma unroll
+	for (int q = 0; q < NC; q++) {
+		const int c = c0 + q * TX;
+		gx0[q] = __ldg(Gx + c), gy0[q] = __ldg(Gy + c), gz0[q] = __ldg(Gz + c);
+		gyk[q] = __ldg(Gy + c + ALT), gxk[q] = __ldg(Gx + c + ALT);
+		gzj[q] = __ldg(Gz + c + ALT * sj), gxj[q] = __ldg(Gx + c + ALT * sj);
+		gzi[q] = __ldg(Gz + c + ALT * si), gyi[q] = __ldg(Gy + c + ALT * si);
+		fx[q] = P.F[0][c], fy[q] = P.F[1][c], fz[q] = P.F[2][c];
+		dz[q] = __ldg(P.dtd[2] + (k + q * TX - P.kMIN));
+		cx[q] = 1, cy[q] = 1, cz[q] = 1;
+		if (hasC) {
+			if (P.matIdx) {
+				// the same floats from the table of distinct triples
+				const float4 t = __ldg(P.matTab + __ldg(P.matIdx + c));
+				cx[q] = t.x, cy[q] = t.y, cz[q] = t.z;
+			} else {
+				cx[q] = __ldg(P.C[0] + c), cy[q] = __ldg(P.C[1] + c), cz[q] = __ldg(P.C[2] + c);
+			}
+		}
+	}
+	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN));
+#pragma unroll
+	for (int q = 0; q < NC; q++) {
+		const int kq = k + q * TX, c = c0 + q * TX;
+		// curl (reference src/update.c:109-118)
+		if (hasC) {
+			fx[q] += (dz[q] * (gy0[q] - gyk[q]) + dy * (gzj[q] - gz0[q])) * cx[q];
+			fy[q] += (dx * (gz0[q] - gzi[q]) + dz[q] * (gxk[q] - gx0[q])) * cy[q];
+			fz[q] += (dy * (gx0[q] - gxj[q]) + dx * (gyi[q] - gy0[q])) * cz[q];
+		} else {
+			fx[q] += (dz[q] * (gy0[q] - gyk[q]) + dy * (gzj[q] - gz0[q]));
+			fy[q] += (dx * (gz0[q] - gzi[q]) + dz[q] * (gxk[q] - gx0[q]));
+			fz[q] += (dy * (gx0[q] - gxj[q]) + dx * (gyi[q] - gy0[q]));
+		}
+		// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
+		if ((bi | bj | bk[q]) & (CLS_PML_LO | CLS_PML_HI)) {
+#define PML_ARGS P, i, j, kq, fx[q], fy[q], fz[q], gx0[q], gy0[q], gz0[q], gyk[q], gxk[q], gzj[q], gxj[q], gzi[q], gyi[q], hasC, cx[q], cy[q], cz[q]
+			if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
+			if (bj & CLS_PML_LO) pmlFace<1>(PML_ARGS);
+			if (bk[q] & CLS_PML_LO) pmlFace<2>(PML_ARGS);
+			if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
+			if (bj & CLS_PML_HI) pmlFace<4>(PML_ARGS);
+			if (bk[q] & CLS_PML_HI) pmlFace<5>(PML_ARGS);
+#undef PML_ARGS
+		}
+		// TFSF k face planes (cells on an i or j face plane are hard)
+		if (bk[q] & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, kq, fx[q], fy[q], fz[q], hasC, cx[q], cy[q], cz[q]);
+		P.F[0][c] = fx[q], P.F[1][c] = fy[q], P.F[2][c] = fz[q];
+	}
+}
+
+// Fused half step of a large world, one thread per ALIS_KPT cells of a
+// row (k, k + TX, ...), one i plane per block of TX x TY threads.  Tiers
+// by the cell's class bits: plain cells take the curl only; CPML cells
+// and cells on TFSF k face planes add their face updates, all inline;
+// cells on TFSF i or j face planes (whole blocks or warps) and dispersive
+// cells go to hardCell.  Index arithmetic is 32-bit (at most 2^31
+// elements per array, checked on the host).  Worlds with more than 8
+// objects add a per-block list of the objects that meet the tile.
+#ifndef ALIS_KPT
+#define ALIS_KPT 1
+#endif
 template <int ALT>
 __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
-	constexpr int TY_ = STEP_TY(ALT);
+	constexpr int TY_ = STEP_TY(ALT), KW = TX * ALIS_KPT;
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	const int k = P.kMIN + blockIdx.x * TX + threadIdx.x;
+	const int k = P.kMIN + blockIdx.x * KW + threadIdx.x;
 	const int j = P.jMIN + blockIdx.y * TY_ + threadIdx.y;
 	// E sweeps i downwards, H upwards: each starts on the planes the other
 	// touched last, which are still in L2
@@ -857,7 +940,7 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 		// objects whose box meets this tile, in list order (one warp)
 		if (threadIdx.y == 0) {
 			const int tj0 = P.jMIN + blockIdx.y * TY_, tj1 = min(tj0 + TY_ - 1, P.jMAX);
-			const int tk0 = P.kMIN + blockIdx.x * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
+			const int tk0 = P.kMIN + blockIdx.x * KW, tk1 = min(tk0 + KW - 1, P.kMAX);
 			int cnt = 0;
 			for (int base = 0; base < P.nobj; base += 32) {
 				int n = base + threadIdx.x;
@@ -878,59 +961,31 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 		__syncthreads();
 	}
 	if (k > P.kMAX || j > P.jMAX) return;
-	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
-	if (((bi | bj) & CLS_TFSF) || (bi & bj & bk & 0x1FFu)) {
-		// object loops: the tile's list, or all objects filtered by class bits
-		const int *list = 0;
-		int nIter = P.nobj;
-		if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
-		hardCell<ALT>(P, i, j, k, list, nIter);
+	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN));
+	unsigned bk[ALIS_KPT];
+	bool lean = !((bi | bj) & CLS_TFSF);
+#pragma unroll
+	for (int q = 0; q < ALIS_KPT; q++) {
+		const int kq = k + q * TX;
+		bk[q] = kq <= P.kMAX ? __ldg(P.cls[2] + (kq - P.kMIN)) : 0u;
+		if (kq > P.kMAX || (bi & bj & bk[q] & 0x1FFu)) lean = false;
+	}
+	if (lean) {
+		leanCells<ALT, ALIS_KPT>(P, i, j, k, bi, bj, bk);
 		return;
 	}
-	const int sj = (int)P.L.sj, si = (int)P.L.si;
-	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
-	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
-	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
-	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
-	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
-	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
-	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
-	const bool hasC = P.C[0] != 0;
-	float cx = 1, cy = 1, cz = 1;
-	if (hasC) {
-		if (P.matIdx) {
-			// the same floats from the table of distinct triples
-			const float4 t = __ldg(P.matTab + __ldg(P.matIdx + c));
-			cx = t.x, cy = t.y, cz = t.z;
-		} else {
-			cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
-		}
+	// one cell at a time: hard cells run the full sequence out of line
+	// (object loops: the tile's list, or all objects filtered by class bits)
+	const int *list = 0;
+	int nIter = P.nobj;
+	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
+#pragma unroll
+	for (int q = 0; q < ALIS_KPT; q++) {
+		const int kq = k + q * TX;
+		if (kq > P.kMAX) break;
+		if (((bi | bj) & CLS_TFSF) || (bi & bj & bk[q] & 0x1FFu)) hardCell<ALT>(P, i, j, kq, list, nIter);
+		else leanCells<ALT, 1>(P, i, j, kq, bi, bj, bk + q);
 	}
-	// curl (reference src/update.c:109-118)
-	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
-	if (hasC) {
-		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
-		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
-		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
-	} else {
-		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
-		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
-		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
-	}
-	// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
-	if ((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI)) {
-#define PML_ARGS P, i, j, k, fx, fy, fz, gx0, gy0, gz0, gyk, gxk, gzj, gxj, gzi, gyi, hasC, cx, cy, cz
-		if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
-		if (bj & CLS_PML_LO) pmlFace<1>(PML_ARGS);
-		if (bk & CLS_PML_LO) pmlFace<2>(PML_ARGS);
-		if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
-		if (bj & CLS_PML_HI) pmlFace<4>(PML_ARGS);
-		if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
-#undef PML_ARGS
-	}
-	// TFSF k face planes (cells on an i or j face plane went to hardCell)
-	if (bk & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
-	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1556,7 +1611,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	const int ni = g.iMAX - g.iMIN + 1;
 	const int ty = STEP_TY(field == 0 ? 1 : -1);
 	dim3 block(TX, ty, 1);
-	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + ty) / ty, ni);
+	dim3 grid((g.kMAX - g.kMIN + TX * ALIS_KPT) / (TX * ALIS_KPT), (g.jMAX - g.jMIN + ty) / ty, ni);
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -1615,9 +1670,14 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	// ghost copies: E's wait for the next host read, H's run now
 	if (field == 0) {
 		w->pendingE.assign(s->ghost, s->ghost + s->nghost);
+		w->hRecorded = false;
 	} else {
+		if (!w->evHCells) ALIS_CUDA(cudaEventCreateWithFlags(&w->evHCells, cudaEventDisableTiming));
+		ALIS_CUDA(cudaEventRecord(w->evHCells, gStream));
+		w->hGhosts.assign(s->ghost, s->ghost + s->nghost);
 		int rc = runGhosts(w, 1, s->ghost, s->nghost);
 		if (rc) return rc;
+		w->hOps = gOps, w->hRecorded = true;
 	}
 	ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
 	gMainRec[field] = 1;
@@ -2243,6 +2303,33 @@ extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1
 }
 
 // field pointers of set m for the phaser gather kernel
+// The stream of a phaser gather on world w that reads H over the boxes
+// box[n] (i0, i1, j0, j1, k0, k1, each already widened by the cells the
+// gather reads): the side stream, after w's last H cell updates, when
+// nothing has changed world data since that half step's ghost launch and
+// none of its ghost copies writes H there -- the gather then runs beside
+// the ghost copies; else the main stream.  gatherEnd joins the streams.
+extern "C" cudaStream_t alisgpu__gather_begin(alisgpu_world *w, const int (*box)[6], int n)
+{
+	if (gProfOn || !w || !w->hRecorded || gOps != w->hOps) return gStream;
+	for (const alisgpu_ghost_copy &c : w->hGhosts) {
+		const int W[6] = { c.i0, c.i1, c.j0, c.j1, c.k0, c.k1 };
+		for (int q = 0; q < n; q++) if (boxesMeet(W, box[q])) return gStream;
+	}
+	if (cudaStreamWaitEvent(gGather, w->evHCells, 0) != cudaSuccess) return gStream;
+	return gGather;
+}
+
+extern "C" int alisgpu__gather_end(alisgpu_world *w, cudaStream_t st)
+{
+	if (st == gStream) return ALISGPU_OK;
+	ALIS_CUDA(cudaEventRecord(gEvGatherDone, gGather));
+	ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvGatherDone, 0));
+	// a gather changes no world data: a further phaser may also run beside
+	w->hOps = gOps;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L)
 {
 	if (!w || m < 0 || m > w->g.complexField) return alisgpu__fail(ALISGPU_EINVAL, "world_fields: bad argument");
