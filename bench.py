@@ -11,10 +11,11 @@ value     cells x steps / device time of K steps (CUDA events on the
           engine stream; fields resident in HBM; the 1.5 GB per step of
           field traffic exceeds the 129 MB L2, so no L2 flush is needed)
 e2e       the same through the public API timed on the host: K steps plus
-          the read-back of the phaser accumulators and the flux result
+          the flux result (face fluxes reduced on the device, read back)
 roofline  the fused half-step kernel: algorithmic bytes per step (84 B per
           cell, +32 B per CPML slab, ADE terms) over the mean E + H launch
-          time, against the measured HBM copy bandwidth
+          time, against the measured HBM copy bandwidth (frac) and the
+          nominal 8 TB/s (frac_nominal)
 cpu_baseline  the oracle restatement of the reference loops on the host
           cores (OpenMP), bounded sample of the same world
 --impl reference  times that CPU implementation alone as the reference arm.
@@ -170,8 +171,9 @@ def barrier(world):
 def reference_arm(args, rank, world):
     if rank != 0:
         return
-    # bounded sample: at most 32 timed and 3 warm-up steps of the full world
-    cpu = run_cpu(args.half, min(max(args.steps, 1), 32), min(args.warmup, 3))
+    # bounded sample: at most 256 timed steps (about 10 s on 16 cores) and 3
+    # warm-up steps of the full world
+    cpu = run_cpu(args.half, min(max(args.steps, 1), 256), min(args.warmup, 3))
     rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
     sample = "%d timed steps (after %d warm-up) of the full %d^3-cell world" % (cpu["steps"], min(args.warmup, 3), round(cpu["cells"] ** (1 / 3)))
     line = {
@@ -273,6 +275,7 @@ def engine_arm(args, rank, world, local):
                 "h2d_bytes_per_step": lib.c2_step_h2d_bytes(),
                 "d2h_bytes_per_step": lib.c2_result_d2h_bytes() / K},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "frac_nominal": achieved / 8000.0,
                      "peak_source": pk_kind, "traffic": traffic,
                      "kernel": "k_half_step (E + H launches, mean per launch pair)",
                      "algorithmic_bytes_per_step": step_bytes, "launch_pair_ms": pair_ms},
@@ -288,10 +291,10 @@ def engine_arm(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=256)
+    ap.add_argument("--steps", type=int, default=1024)
     ap.add_argument("--warmup", type=int, default=64)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--cpu-steps", type=int, default=4, help="steps of the CPU baseline sample (0: skip it)")
+    ap.add_argument("--cpu-steps", type=int, default=256, help="steps of the CPU baseline sample, about 10 s on 16 cores (0: skip it)")
     ap.add_argument("--half", type=int, default=HALF, help="domain half size in nm (230: the 256^3 workload)")
     args = ap.parse_args()
     if args.warmup < 3:
