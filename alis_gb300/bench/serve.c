@@ -1,0 +1,291 @@
+/*
+ * serve.c -- a request loop over the ALiS API: many simulations resident
+ * on one GPU at once, admitted by device footprint as requests arrive and
+ * stepped in turn, each world on streams of its own so that their steps
+ * overlap on the device.
+ *
+ *   serve <mode> <requests> <rate/s> <seed> <small|large> [slots] [budget GB]
+ *
+ * mode served:     Poisson arrivals at <rate>; a request is admitted when
+ *                  a slot is free and its footprint fits the budget; the
+ *                  admitted worlds advance CHUNK steps each in turn.
+ * mode sequential: the same requests one after another, each run to its
+ *                  end alone on the default streams (the plain path).
+ * mode alone <id>: request <id> by itself (its result, for comparison).
+ *
+ * The mix follows the served-stream workload in miniature: half vacuum
+ * with a dielectric ball, three tenths a Drude bowtie antenna with a gap
+ * of 5-30 nm, a fifth photonic-crystal slab k-point runs (Bloch-periodic,
+ * complex fields, several k-points per request); 1-3 dipoles with Band or
+ * Pulse waveforms; grid and step counts drawn per request.  Each request
+ * reports the outgoing flux of its phaser box summed over frequencies
+ * (and k-points) as its result.
+ *
+ * Output: one line per finished request "R id kind cells steps latency_ms
+ * result(hex)", then one JSON line with throughput and latency percentiles.
+ */
+#include <alis.h>
+#include <time.h>
+#include <stdint.h>
+#include <unistd.h>
+
+#define MAXREQ 4096
+#define MAXK 16
+#define CHUNK 32
+
+static double now(void)
+{
+	struct timespec t;
+	clock_gettime(CLOCK_MONOTONIC, &t);
+	return t.tv_sec + 1e-9 * t.tv_nsec;
+}
+
+static unsigned long long rng;
+static double uniform(void)
+{
+	rng = rng * 6364136223846793005ULL + 1442695040888963407ULL;
+	return (double)(rng >> 11) / 9007199254740992.0;
+}
+
+typedef struct {
+	int kind, half, steps, nk, ndip, gap;
+	float dip[3][3];
+	int wave[3];
+	double arrival;
+	/* while running */
+	world W[MAXK];
+	phaser P[MAXK];
+	int done;
+	long cells;
+	double start, finish;
+	double result;
+} request;
+
+static request R[MAXREQ];
+static int small = 1;
+/* host wall time spent setting requests up, stepping them, finishing them */
+static double tSetup, tStep, tFinish;
+
+/* draw request q (the draw order is fixed, so every mode sees the same stream) */
+static void drawRequest(int q, double *t, double rate)
+{
+	request *r = &R[q];
+	double u = uniform();
+	r->kind = u < 0.5 ? 0 : u < 0.8 ? 1 : 2;
+	int lo = small ? 14 : 40, hi = small ? 24 : 96;                /* half size in cells */
+	r->half = lo + (int)((hi - lo + 1) * uniform());
+	int slo = small ? 120 : 1000, shi = small ? 240 : 2000;
+	r->steps = slo + (int)((shi - slo + 1) * uniform());
+	r->nk = r->kind == 2 ? (small ? 2 : 8) + (int)((small ? 2 : 9) * uniform()) : 1;
+	r->ndip = 1 + (int)(3 * uniform());
+	r->gap = 5 + (int)(26 * uniform());
+	for (int d = 0; d < 3; d++) {
+		for (int a = 0; a < 3; a++) r->dip[d][a] = (float)(20 * (uniform() - 0.5));
+		r->wave[d] = uniform() < 0.5;
+	}
+	*t += -log(1 - uniform()) / rate;
+	r->arrival = *t;
+}
+
+/* the worlds of request q, set up through the public API */
+static void setupRequest(int q, int streams)
+{
+	double t0 = now();
+	request *r = &R[q];
+	float L = 10.0f * r->half;
+	r->cells = 0;
+	for (int k = 0; k < r->nk; k++) {
+		world W;
+		if (r->kind == 0) {
+			dom D = {{-L, L - 10}, {-L, L - 10}, {-L, L - 10}};
+			res Re = {5, {10}, {1240}};
+			sur S = {{PML}, {PML}, {PML}, {8}};
+			W = createWorld(D, Re, S, "");
+			object Ball1 = {Ball, {{-0.4f * L, 0.3f * L}, {-0.3f * L, 0.3f * L}, {-0.2f * L, 0.4f * L}}};
+			putObjects(W, n(1.5), Ball1, Air);
+		} else if (r->kind == 1) {
+			float g = r->gap, a = 0.25f * L, s3 = sqrtf(3);
+			dom D = {{-L, L - 10}, {-L, L - 10}, {-L, L - 10}};
+			res Re = {5, {10}, {1240}};
+			sur S = {{PML}, {PML}, {PML}, {8}};
+			W = createWorld(D, Re, S, "");
+			object Bowtie = {Combination, {{2}}, objects {
+				{Intersection, {{2}}, objects {
+					{Box, {{g / 2, g / 2 + 2 * a}, {-2 * a / s3, 2 * a / s3}, {-15, 15}}},
+					{DRodZ, {{g / 2 - 2 * a, g / 2 + 2 * a}, {-2 * a / s3, 2 * a / s3}, {-15, 15}}}}},
+				{Intersection, {{2}}, objects {
+					{Box, {{-g / 2 - 2 * a, -g / 2}, {-2 * a / s3, 2 * a / s3}, {-15, 15}}},
+					{DRodZ, {{-g / 2 - 2 * a, -g / 2 + 2 * a}, {-2 * a / s3, 2 * a / s3}, {-15, 15}}}}}}};
+			matter Ag = {{4.0}, {{9.0, 0.02}}};
+			putObjects(W, Ag, Bowtie, Air);
+		} else {
+			/* k-point k of a path through the Brillouin zone */
+			float kk = 0.1f + 2.8f * k / r->nk, kx, ky;
+			if (kk < 1) kx = 0, ky = kk;
+			else if (kk < 2) kx = kk - 1, ky = 1;
+			else kx = 3 - kk, ky = 3 - kk;
+			float a = 2 * L;
+			dom D = {{-L, L - 10}, {-L, L - 10}, {-L, L - 10}};
+			res Re = {5, {10}, {1240}};
+			sur S = {{BBC, a * 3 / kx}, {BBC, a * 3 / ky}, {PML}, {8}};
+			W = createWorld(D, Re, S, "");
+			object Slab = {Difference, {{2}}, objects {
+				{Box, {{-INF, INF}, {-INF, INF}, {-0.2f * L, 0.2f * L}}},
+				{RodZ, {{-0.4f * L, 0.4f * L}, {-0.4f * L, 0.4f * L}, {-INF, INF}}}}};
+			putObjects(W, n(3.5), Slab, Air);
+		}
+		for (int d = 0; d < r->ndip; d++)
+			pointDipole(W, d == 0 ? Ez : d == 1 ? Hx : Ey, r->dip[d][0], r->dip[d][1], r->dip[d][2],
+			            r->wave[d] ? Band : Pulse, 500, r->wave[d] ? 800 : 100);
+		/* the phaser box 10 nm inside the CPML */
+		float b = L - 90;
+		phaser P = createPhasers(W, 500, 800, 100, -b, b, -b, b, -b, b);
+		if (streams) alisWorldStreams(W);
+		r->W[k] = W, r->P[k] = P;
+		r->cells += (long)W->iNUM * W->jNUM * W->kNUM;
+	}
+	r->done = 0;
+	tSetup += now() - t0;
+}
+
+/* device bytes of request q: fields (complex: twice), eps^-1, CPML psi
+ * slabs, phaser accumulators and ring -- an estimate from the grid */
+static double footprint(int q)
+{
+	request *r = &R[q];
+	double n = 2 * r->half + 2;
+	double cells = n * n * n, face = n * n;
+	double per = (r->kind == 2 ? 2 : 1) * 6 * 4.0 + 12 + 0.5 * 16;
+	return r->nk * (cells * per + 6 * face * 4 * 8 * 4 * 2 + 6 * face * 16 * 64);
+}
+
+static void stepRequest(int q, int n)
+{
+	double t0 = now();
+	request *r = &R[q];
+	for (int s = 0; s < n && r->done < r->steps; s++, r->done++)
+		for (int k = 0; k < r->nk; k++) {
+			updateE(r->W[k]);
+			updateH(r->W[k]);
+			updatePhaser(r->W[k], r->P[k]);
+		}
+	tStep += now() - t0;
+}
+
+static void finishRequest(int q)
+{
+	double t0 = now();
+	request *r = &R[q];
+	double sum = 0;
+	for (int k = 0; k < r->nk; k++) {
+		for (int f = 0; r->P[k][f].f; f++) sum += phaserPoyntingOut(r->P[k] + f);
+		deletePhaser(r->P[k]);
+		deleteWorld(r->W[k]);
+	}
+	r->result = sum;
+	r->finish = now();
+	tFinish += r->finish - t0;
+}
+
+static int cmpd(const void *a, const void *b)
+{
+	double x = *(const double *)a, y = *(const double *)b;
+	return x < y ? -1 : x > y;
+}
+
+int main(int argc, char **argv)
+{
+	if (argc < 6) {
+		fprintf(stderr, "usage: %s served|sequential|alone requests rate seed small|large [slots|id] [budget GB]\n", argv[0]);
+		return 2;
+	}
+	const char *mode = argv[1];
+	int nreq = atoi(argv[2]);
+	double rate = atof(argv[3]);
+	rng = strtoull(argv[4], 0, 10);
+	small = strcmp(argv[5], "large") != 0;
+	int slots = argc > 6 ? atoi(argv[6]) : 16;
+	double budget = (argc > 7 ? atof(argv[7]) : 64) * 1e9;
+	if (nreq < 1 || nreq > MAXREQ) return 2;
+	double t = 0;
+	for (int q = 0; q < nreq; q++) drawRequest(q, &t, rate);
+	/* silence the library's progress lines */
+	fflush(stdout);
+	int saved = dup(1);
+	freopen("/dev/null", "w", stdout);
+
+	double t0 = now(), cellSteps = 0;
+	int finished = 0;
+	if (!strcmp(mode, "alone")) {
+		int q = slots;
+		setupRequest(q, 0);
+		R[q].start = now();
+		stepRequest(q, R[q].steps);
+		finishRequest(q);
+		cellSteps = (double)R[q].cells * R[q].steps;
+		R[q].arrival = 0, R[q].finish -= t0;
+		finished = 1;
+		nreq = q + 1;
+		for (int p = 0; p < q; p++) R[p].finish = -1;
+	} else if (!strcmp(mode, "sequential")) {
+		for (int q = 0; q < nreq; q++) {
+			setupRequest(q, 0);
+			stepRequest(q, R[q].steps);
+			finishRequest(q);
+			R[q].finish -= t0;
+			R[q].arrival = 0;
+			cellSteps += (double)R[q].cells * R[q].steps;
+			finished++;
+		}
+	} else {
+		int active[MAXREQ], nact = 0, next = 0;
+		double used = 0;
+		while (finished < nreq) {
+			double tn = now() - t0;
+			/* admit the arrived requests that fit, in arrival order */
+			while (next < nreq && R[next].arrival <= tn && nact < slots && (nact == 0 || used + footprint(next) <= budget)) {
+				setupRequest(next, 1);
+				used += footprint(next);
+				active[nact++] = next++;
+			}
+			if (!nact) {
+				/* idle until the next arrival */
+				while (now() - t0 < R[next].arrival) ;
+				continue;
+			}
+			for (int a = 0; a < nact; a++) stepRequest(active[a], CHUNK);
+			for (int a = 0; a < nact; a++) {
+				int q = active[a];
+				if (R[q].done < R[q].steps) continue;
+				finishRequest(q);
+				R[q].finish -= t0;
+				used -= footprint(q);
+				cellSteps += (double)R[q].cells * R[q].steps;
+				finished++;
+				active[a--] = active[--nact];
+			}
+		}
+	}
+	double wall = now() - t0;
+
+	fflush(stdout);
+	dup2(saved, 1);
+	double lat[MAXREQ];
+	int nl = 0;
+	for (int q = 0; q < nreq; q++) {
+		if (R[q].finish < 0) continue;
+		double l = R[q].finish - R[q].arrival;
+		lat[nl++] = l;
+		union { double d; uint64_t u; } v = { R[q].result };
+		printf("R %d %d %ld %d %.3f %016llx\n", q, R[q].kind, R[q].cells, R[q].steps, 1e3 * l, (unsigned long long)v.u);
+	}
+	qsort(lat, nl, sizeof *lat, cmpd);
+	double p50 = lat[(nl - 1) / 2], p99 = lat[(int)(0.99 * (nl - 1))];
+	printf("{\"mode\": \"%s\", \"requests\": %d, \"offered_per_s\": %g, \"seed\": %s, \"mix\": \"%s\", \"slots\": %d, "
+	       "\"budget_gb\": %g, \"wall_s\": %.4f, \"cell_updates\": %.6g, \"gcell_per_s\": %.4f, "
+	       "\"latency_ms\": {\"p50\": %.3f, \"p99\": %.3f, \"max\": %.3f}, \"achieved_per_s\": %.3f, "
+	       "\"host_s\": {\"setup\": %.4f, \"step\": %.4f, \"finish\": %.4f}}\n",
+	       mode, finished, rate, argv[4], small ? "small" : "large", slots, budget / 1e9, wall, cellSteps,
+	       cellSteps / wall / 1e9, 1e3 * p50, 1e3 * p99, 1e3 * lat[nl - 1], finished / wall, tSetup, tStep, tFinish);
+	return 0;
+}

@@ -105,3 +105,16 @@ extern "C" cudaStream_t alisgpu__stream(void);
 extern "C" int alisgpu__fail(int code, const char *fmt, ...);
 extern "C" int alisgpu__check(cudaError_t e, const char *what);
 #define ALIS_CUDA(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return alisgpu__check(e_, #call); } while (0)
+
+// Device memory of worlds, phasers and their scratch comes from the
+// stream-ordered pool on the main stream of the world's group: freeing a
+// world that finished does not wait for the work of every other world.
+template <class T>
+static inline cudaError_t alisgpu__mallocAsync(T **p, size_t bytes)
+{
+	return cudaMallocAsync((void **)p, bytes, alisgpu__stream());
+}
+static inline cudaError_t alisgpu__freeAsync(void *p)
+{
+	return p ? cudaFreeAsync(p, alisgpu__stream()) : cudaSuccess;
+}

@@ -19,6 +19,7 @@
 
 extern "C" const float2 *alisgpu__phaser_acc(alisgpu_phaser *p, int f, int face, long long *cells);
 extern "C" int alisgpu__phaser_nface(alisgpu_phaser *p);
+extern "C" void alisgpu__bind_phaser(alisgpu_phaser *p);
 extern "C" const alisgpu_face *alisgpu__phaser_face(alisgpu_phaser *p, int face);
 
 struct FFFace {
@@ -218,6 +219,7 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 {
 	if (!p || !g || nA < 0 || !T || !present || !kx || !ky || !out) return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums: bad argument");
 	if (!nA) return ALISGPU_OK;
+	alisgpu__bind_phaser(p);
 	cudaStream_t st = alisgpu__stream();
 	FFParams P;
 	memset(&P, 0, sizeof P);
@@ -238,7 +240,7 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 	std::vector<void *> tmp;
 	auto up = [&](const void *src, size_t bytes) -> void * {
 		void *d = 0;
-		if (cudaMalloc(&d, bytes) != cudaSuccess) return 0;
+		if (alisgpu__mallocAsync(&d, bytes) != cudaSuccess) return 0;
 		cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, st);
 		tmp.push_back(d);
 		return d;
@@ -260,7 +262,7 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 	P.kx = (const double *)up(kx, nA * sizeof(double));
 	P.ky = (const double *)up(ky, nA * sizeof(double));
 	double2 *part = 0;
-	ALIS_CUDA(cudaMalloc(&part, (size_t)nA * 6 * sizeof(double2)));
+	ALIS_CUDA(alisgpu__mallocAsync(&part, (size_t)nA * 6 * sizeof(double2)));
 	tmp.push_back(part);
 	ALIS_CUDA(cudaMemsetAsync(part, 0, (size_t)nA * 6 * sizeof(double2), st));
 	P.part = part;
@@ -279,7 +281,7 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 	std::vector<double2> h((size_t)nA * 6);
 	ALIS_CUDA(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
 	ALIS_CUDA(cudaStreamSynchronize(st));
-	for (void *q : tmp) cudaFree(q);
+	for (void *q : tmp) alisgpu__freeAsync(q);
 	// faces in device order are min/max per axis as the host listed them;
 	// the host gives the sign per face through out[] layout: out[a*12 + 2*face]
 	for (int a = 0; a < nA; a++) for (int q = 0; q < 6; q++) {
@@ -332,6 +334,7 @@ extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alis
 	if (off > (size_t)ALISGPU_FF_STATIC_BYTES)
 		return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: %d directions need %zu bytes of scratch, the static buffer holds %u; "
 		                     "split the batch", nA, off, (unsigned)ALISGPU_FF_STATIC_BYTES);
+	alisgpu__bind_phaser(p);
 	cudaStream_t st = alisgpu__stream();
 	unsigned char *base = ffStaticBase[dev];
 	FFParams P;

@@ -27,6 +27,7 @@ void alisgpu__forget_tfsf(const alisgpu_tfsf *s);
 typedef struct devWorld {
 	world W;
 	alisgpu_world *dw;
+	int ownStreams;           /* W (and its auxiliary worlds) on streams of their own */
 	int objectsDirty;         /* eps maps / dispersive objects need upload */
 	int hostStale;            /* device ahead of the host mirrors */
 	int ntf;
@@ -398,10 +399,29 @@ static int ghostList(world W, int field, alisgpu_ghost_copy *g)
 	return n;
 }
 
+/* the auxiliary worlds of a world with streams of its own share them */
+static void shareStreams(devWorld *d)
+{
+	for (tfsf S = d->W->S; S; S = S->S) {
+		devWorld *a = findWorld(S->W);
+		if (a) CHECK("world_share_streams", alisgpu_world_share_streams(a->dw, d->dw));
+	}
+}
+
+void alis_be_world_streams(world W)
+{
+	devWorld *d = findWorld(W);
+	if (!d) return;
+	CHECK("world_own_streams", alisgpu_world_own_streams(d->dw));
+	d->ownStreams = 1;
+	shareStreams(d);
+}
+
 static void halfStep(world W, int field)
 {
 	devWorld *d = findWorld(W);
 	if (!d) { fprintf(stderr, "alis: world unknown to the GPU backend\n"); exit(1); }
+	if (d->ownStreams) shareStreams(d);
 	if (d->objectsDirty) uploadObjects(d);
 	alisgpu_ghost_copy g[MAX_GHOST];
 	alisgpu_half_step s;

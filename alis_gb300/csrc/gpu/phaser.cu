@@ -56,6 +56,7 @@ struct GatherParams {
 
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L);
 extern "C" cudaStream_t alisgpu__gather_begin(alisgpu_world *w, const int (*box)[6], int n);
+extern "C" void alisgpu__bind(alisgpu_world *w);
 extern "C" int alisgpu__gather_end(alisgpu_world *w, cudaStream_t st);
 
 __global__ void k_phaser_gather(const GatherParams P)
@@ -171,6 +172,7 @@ __global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf
 
 extern "C" int alisgpu_phaser_create(alisgpu_world *w, int nfreq, int nface, const alisgpu_face *faces, int ring, int kahan, alisgpu_phaser **out)
 {
+	alisgpu__bind(w);
 	if (!w || nfreq <= 0 || nface < 0 || nface > 6 || (nface && !faces) || !out || ring <= 0)
 		return alisgpu__fail(ALISGPU_EINVAL, "phaser_create: bad argument");
 	alisgpu_phaser *p = new alisgpu_phaser();
@@ -186,36 +188,60 @@ extern "C" int alisgpu_phaser_create(alisgpu_world *w, int nfreq, int nface, con
 	long long n4 = p->cells * 4;
 	cudaStream_t st = alisgpu__stream();
 	if (p->cells) {
-		ALIS_CUDA(cudaMalloc(&p->buf, (size_t)ring * n4 * sizeof(float)));
-		ALIS_CUDA(cudaMalloc(&p->acc, (size_t)nfreq * n4 * sizeof(float2)));
+		ALIS_CUDA(alisgpu__mallocAsync(&p->buf, (size_t)ring * n4 * sizeof(float)));
+		ALIS_CUDA(alisgpu__mallocAsync(&p->acc, (size_t)nfreq * n4 * sizeof(float2)));
 		ALIS_CUDA(cudaMemsetAsync(p->acc, 0, (size_t)nfreq * n4 * sizeof(float2), st));
 		if (kahan) {
-			ALIS_CUDA(cudaMalloc(&p->comp, (size_t)nfreq * n4 * sizeof(float2)));
+			ALIS_CUDA(alisgpu__mallocAsync(&p->comp, (size_t)nfreq * n4 * sizeof(float2)));
 			ALIS_CUDA(cudaMemsetAsync(p->comp, 0, (size_t)nfreq * n4 * sizeof(float2), st));
 		}
 	}
-	ALIS_CUDA(cudaMalloc(&p->phase, (size_t)ring * nfreq * 2 * sizeof(float2)));
+	ALIS_CUDA(alisgpu__mallocAsync(&p->phase, (size_t)ring * nfreq * 2 * sizeof(float2)));
 	p->used = 0;
 	*out = p;
 	return ALISGPU_OK;
 }
 
+// Pinned staging buffers outlive their phasers: freeing pinned memory
+// waits for the whole device, which a served loop of many worlds avoids.
+static std::vector<std::pair<float2 *, size_t>> gPinnedSpare;
+
+static float2 *pinnedTake(size_t n)
+{
+	for (size_t q = 0; q < gPinnedSpare.size(); q++)
+		if (gPinnedSpare[q].second >= n) {
+			float2 *b = gPinnedSpare[q].first;
+			gPinnedSpare.erase(gPinnedSpare.begin() + q);
+			return b;
+		}
+	float2 *b = 0;
+	return cudaMallocHost(&b, n * sizeof(float2)) == cudaSuccess ? b : 0;
+}
+
+static void pinnedRelease(float2 *b, size_t n)
+{
+	if (b) gPinnedSpare.push_back(std::make_pair(b, n));
+}
+
 extern "C" int alisgpu_phaser_destroy(alisgpu_phaser *p)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p) return ALISGPU_OK;
 	cudaStreamSynchronize(alisgpu__stream());
-	if (p->buf) cudaFree(p->buf);
-	if (p->acc) cudaFree(p->acc);
-	if (p->comp) cudaFree(p->comp);
-	if (p->phase) cudaFree(p->phase);
-	if (p->fluxTab) cudaFree(p->fluxTab);
-	for (int b = 0; b < 2; b++) if (p->pinned[b]) cudaFreeHost(p->pinned[b]), cudaEventDestroy(p->pinnedFree[b]);
+	if (p->buf) alisgpu__freeAsync(p->buf);
+	if (p->acc) alisgpu__freeAsync(p->acc);
+	if (p->comp) alisgpu__freeAsync(p->comp);
+	if (p->phase) alisgpu__freeAsync(p->phase);
+	if (p->fluxTab) alisgpu__freeAsync(p->fluxTab);
+	for (int b = 0; b < 2; b++)
+		if (p->pinned[b]) cudaEventSynchronize(p->pinnedFree[b]), pinnedRelease(p->pinned[b], p->pinnedCap), cudaEventDestroy(p->pinnedFree[b]);
 	delete p;
 	return ALISGPU_OK;
 }
 
 extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_flush: null phaser");
 	if (!p->used || !p->cells) { p->used = 0; p->hostPhase.clear(); return ALISGPU_OK; }
 	cudaStream_t st = alisgpu__stream();
@@ -224,13 +250,14 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 		for (int b = 0; b < 2; b++) {
 			if (p->pinned[b]) {
 				ALIS_CUDA(cudaEventSynchronize(p->pinnedFree[b]));
-				ALIS_CUDA(cudaFreeHost(p->pinned[b]));
+				pinnedRelease(p->pinned[b], p->pinnedCap);
 				p->pinned[b] = 0;
 			} else {
 				ALIS_CUDA(cudaEventCreateWithFlags(&p->pinnedFree[b], cudaEventDisableTiming));
 				ALIS_CUDA(cudaEventRecord(p->pinnedFree[b], st));
 			}
-			ALIS_CUDA(cudaMallocHost(&p->pinned[b], nph * sizeof(float2)));
+			p->pinned[b] = pinnedTake(nph);
+			if (!p->pinned[b]) return alisgpu__fail(ALISGPU_ENOMEM, "phaser_flush: no pinned host memory");
 		}
 		p->pinnedCap = nph;
 	}
@@ -257,6 +284,7 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 
 extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, const float *phaseH)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p || !phaseE || !phaseH) return alisgpu__fail(ALISGPU_EINVAL, "phaser_record: bad argument");
 	if (p->used == p->ring) {
 		int rc = alisgpu_phaser_flush(p);
@@ -302,6 +330,7 @@ extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, con
 
 extern "C" int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q, float *host)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p || !host || f < 0 || f >= p->nfreq || face < 0 || face >= p->nface || q < 0 || q > 3)
 		return alisgpu__fail(ALISGPU_EINVAL, "phaser_download: bad argument");
 	long long n = p->faceStart[face + 1] - p->faceStart[face];
@@ -314,6 +343,7 @@ extern "C" int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q
 
 extern "C" int alisgpu_phaser_zero(alisgpu_phaser *p)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_zero: null phaser");
 	p->used = 0;
 	p->hostPhase.clear();
@@ -419,6 +449,7 @@ __global__ void k_phaser_flux_outer(const FluxParams P)
 extern "C" int alisgpu_phaser_face_flux(alisgpu_phaser *p, const float *const wE[3], const float *const wH[3],
                                         const int lo[3], const int hi[3], float *out)
 {
+	if (p) alisgpu__bind(p->w);
 	if (!p || !wE || !wH || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "phaser_face_flux: bad argument");
 	int rc = alisgpu_phaser_flush(p);
 	if (rc) return rc;
@@ -468,9 +499,9 @@ extern "C" int alisgpu_phaser_face_flux(alisgpu_phaser *p, const float *const wE
 	size_t bytes = (tabFloats + innerFloats + outFloats) * sizeof(float);
 	if (bytes > p->fluxTabBytes) {
 		ALIS_CUDA(cudaStreamSynchronize(st));
-		if (p->fluxTab) cudaFree(p->fluxTab);
+		if (p->fluxTab) alisgpu__freeAsync(p->fluxTab);
 		p->fluxTab = 0, p->fluxTabBytes = 0;
-		ALIS_CUDA(cudaMalloc(&p->fluxTab, bytes));
+		ALIS_CUDA(alisgpu__mallocAsync(&p->fluxTab, bytes));
 		p->fluxTabBytes = bytes;
 	}
 	float *tab = p->fluxTab;
@@ -514,4 +545,5 @@ extern "C" const float2 *alisgpu__phaser_acc(alisgpu_phaser *p, int f, int face,
 	return p->acc + (size_t)f * p->cells * 4 + p->faceStart[face] * 4;
 }
 extern "C" int alisgpu__phaser_nface(alisgpu_phaser *p) { return p->nface; }
+extern "C" void alisgpu__bind_phaser(alisgpu_phaser *p) { if (p) alisgpu__bind(p->w); }
 extern "C" const alisgpu_face *alisgpu__phaser_face(alisgpu_phaser *p, int face) { return &p->faces[face]; }

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 #include <cstring>
 #include <vector>
+#include <algorithm>
 #include "common.cuh"
 
 namespace cg = cooperative_groups;
@@ -350,7 +351,6 @@ struct alisgpu_voxelizer {
 	VoxNode *dNode;
 	float *dPool, *dTab[3];
 	unsigned int *dErr;
-	size_t stack;                          // the context's stack limit before, if raised
 	float *dOut;                           // fill scratch: 3 floats, 3 list entries per cell
 	unsigned long long *dList;
 	unsigned int *dCount;
@@ -358,35 +358,50 @@ struct alisgpu_voxelizer {
 	int refineBlocks;
 };
 
-// per-thread stack for the recursion through compound shapes
-#define VOX_STACK 8192
+// per-thread stack for the recursion through compound shapes: the
+// kernel's own frame and one frame of the compound evaluator and of the
+// lattice fold per level of nesting (raised once, never lowered: a change
+// of the limit waits for the whole device)
+#define VOX_STACK_BASE 1024
+#define VOX_STACK_LEVEL 384
+
+static void vfree(void *p)
+{
+	if (p) cudaFreeAsync(p, 0);
+}
 // cells per fill launch (three floats and three list entries each)
 #define VOX_CHUNK (1 << 23)
 
 static int voxUpload(alisgpu_voxelizer *v, const alisgpu_vox_node *nodes, int nnode, const float *pool, int npool,
                      const float *const tab[3], const int lo[3], const int hi[3], int nslot)
 {
-	ALIS_CUDA(cudaMalloc(&v->dNode, nnode * sizeof(VoxNode)));
+	ALIS_CUDA(cudaMallocAsync((void **)&v->dNode, nnode * sizeof(VoxNode), 0));
 	ALIS_CUDA(cudaMemcpy(v->dNode, nodes, nnode * sizeof(VoxNode), cudaMemcpyHostToDevice));
-	ALIS_CUDA(cudaMalloc(&v->dPool, (npool > 0 ? npool : 1) * sizeof(float)));
+	ALIS_CUDA(cudaMallocAsync((void **)&v->dPool, (npool > 0 ? npool : 1) * sizeof(float), 0));
 	if (npool > 0) ALIS_CUDA(cudaMemcpy(v->dPool, pool, npool * sizeof(float), cudaMemcpyHostToDevice));
 	for (int a = 0; a < 3; a++) {
 		const size_t n = (size_t)(1 + hi[a] - lo[a]) * 3 * nslot;
-		ALIS_CUDA(cudaMalloc(&v->dTab[a], n * sizeof(float)));
+		ALIS_CUDA(cudaMallocAsync((void **)&v->dTab[a], n * sizeof(float), 0));
 		ALIS_CUDA(cudaMemcpy(v->dTab[a], tab[a], n * sizeof(float), cudaMemcpyHostToDevice));
 	}
-	ALIS_CUDA(cudaMalloc(&v->dErr, sizeof(unsigned int)));
+	ALIS_CUDA(cudaMallocAsync((void **)&v->dErr, sizeof(unsigned int), 0));
 	ALIS_CUDA(cudaMemset(v->dErr, 0, sizeof(unsigned int)));
 	int dev = 0, sms = 0;
 	ALIS_CUDA(cudaGetDevice(&dev));
 	ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 	v->refineBlocks = 4 * sms;
+	// nesting depth of the compound shapes (members come after their owner)
+	std::vector<int> depth(nnode, 0);
+	int deepest = 0;
+	for (int n = 0; n < nnode; n++)
+		for (int c = 0; c < nodes[n].nchild; c++) {
+			depth[nodes[n].child + c] = depth[n] + 1;
+			deepest = std::max(deepest, depth[n] + 1);
+		}
+	const size_t need = VOX_STACK_BASE + (size_t)VOX_STACK_LEVEL * deepest;
 	size_t stack = 0;
 	ALIS_CUDA(cudaDeviceGetLimit(&stack, cudaLimitStackSize));
-	if (stack < VOX_STACK) {
-		ALIS_CUDA(cudaDeviceSetLimit(cudaLimitStackSize, VOX_STACK));
-		v->stack = stack;
-	}
+	if (stack < need) ALIS_CUDA(cudaDeviceSetLimit(cudaLimitStackSize, need));
 	return ALISGPU_OK;
 }
 
@@ -426,11 +441,9 @@ extern "C" int alisgpu_voxelizer_create(const alisgpu_vox_node *nodes, int nnode
 extern "C" int alisgpu_voxelizer_destroy(alisgpu_voxelizer *v)
 {
 	if (!v) return ALISGPU_OK;
-	cudaDeviceSynchronize();
-	cudaFree(v->dNode), cudaFree(v->dPool), cudaFree(v->dErr);
-	cudaFree(v->dOut), cudaFree(v->dList), cudaFree(v->dCount);
-	for (int a = 0; a < 3; a++) cudaFree(v->dTab[a]);
-	if (v->stack) cudaDeviceSetLimit(cudaLimitStackSize, v->stack);
+	vfree(v->dNode), vfree(v->dPool), vfree(v->dErr);
+	vfree(v->dOut), vfree(v->dList), vfree(v->dCount);
+	for (int a = 0; a < 3; a++) vfree(v->dTab[a]);
 	delete v;
 	return ALISGPU_OK;
 }
@@ -453,14 +466,14 @@ extern "C" int alisgpu_voxelizer_bounds(alisgpu_voxelizer *v, int nobj, int *box
 		b[0] = V.iMAX, b[1] = V.iMIN, b[2] = V.jMAX, b[3] = V.jMIN, b[4] = V.kMAX, b[5] = V.kMIN;
 	}
 	int *d = 0;
-	ALIS_CUDA(cudaMalloc(&d, init.size() * sizeof(int)));
+	ALIS_CUDA(cudaMallocAsync((void **)&d, init.size() * sizeof(int), 0));
 	ALIS_CUDA(cudaMemcpy(d, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice));
 	const long long cells = (long long)(1 + V.iMAX - V.iMIN) * (1 + V.jMAX - V.jMIN) * (1 + V.kMAX - V.kMIN);
 	k_vox_bounds<<<(unsigned)((cells + 127) / 128), 128>>>(V, nobj, d);
 	alisgpu__count_launch();
 	ALIS_CUDA(cudaGetLastError());
 	ALIS_CUDA(cudaMemcpy(box, d, init.size() * sizeof(int), cudaMemcpyDeviceToHost));
-	cudaFree(d);
+	vfree(d);
 	return voxCheck(v);
 }
 
@@ -470,11 +483,11 @@ static int voxRun(alisgpu_voxelizer *v, int o, FillJob J, long long total, float
 {
 	const int comps = J.edge < 0 ? 3 : 1;
 	if ((size_t)total > v->cap) {
-		cudaFree(v->dOut), cudaFree(v->dList), cudaFree(v->dCount);
+		vfree(v->dOut), vfree(v->dList), vfree(v->dCount);
 		v->dOut = 0, v->dList = 0, v->dCount = 0, v->cap = 0;
-		ALIS_CUDA(cudaMalloc(&v->dOut, 3 * (size_t)total * sizeof(float)));
-		ALIS_CUDA(cudaMalloc(&v->dList, 3 * (size_t)total * sizeof(unsigned long long)));
-		ALIS_CUDA(cudaMalloc(&v->dCount, sizeof(unsigned int)));
+		ALIS_CUDA(cudaMallocAsync((void **)&v->dOut, 3 * (size_t)total * sizeof(float), 0));
+		ALIS_CUDA(cudaMallocAsync((void **)&v->dList, 3 * (size_t)total * sizeof(unsigned long long), 0));
+		ALIS_CUDA(cudaMallocAsync((void **)&v->dCount, sizeof(unsigned int), 0));
 		v->cap = (size_t)total;
 	}
 	for (int c = 0; c < 3; c++) J.out[c] = v->dOut + (size_t)c * total;

@@ -24,9 +24,8 @@
 namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------
-// process-wide state: device, stream, error text, launch counter
+// process-wide state: device, stream groups, error text, launch counter
 // ---------------------------------------------------------------------
-static cudaStream_t gStream;
 static int gInit;
 static char gErr[512];
 static unsigned long long gLaunches;
@@ -47,22 +46,69 @@ extern "C" int alisgpu__check(cudaError_t e, const char *what)
 	return alisgpu__fail(code, "%s: %s", what, cudaGetErrorString(e));
 }
 
-// Side stream for the half steps of TFSF auxiliary worlds, which run
-// concurrently with their parent's half steps.  Ordering: an auxiliary
-// step of field F waits for the parent's last step of the other field
-// (which read the auxiliary F it is about to overwrite); a parent step of
-// field F waits for the last auxiliary step of the other field (whose
-// result it reads).  Any other call that touches world data joins the two
-// streams first, and the next auxiliary step then waits for everything
-// issued before it.
-static cudaStream_t gSide;
-static cudaEvent_t gEvMainDone[2], gEvAuxDone[2], gEvJoin;
-// phaser gathers that run beside the H ghost copies (a second side stream)
-static cudaStream_t gGather;
-static cudaEvent_t gEvGatherDone;
+// The streams of a group of worlds -- a world and its TFSF auxiliary
+// worlds.  Every world belongs to the default group unless it asks for a
+// group of its own; the steps of worlds in different groups overlap on
+// the device.  In a group:
+// * the main stream orders the worlds' half steps, phasers and results;
+// * the side stream runs the half steps of the auxiliary worlds
+//   concurrently with their parent's.  An auxiliary step of field F waits
+//   for the parent's last step of the other field (which read the
+//   auxiliary F it is about to overwrite); a parent step of field F waits
+//   for the last auxiliary step of the other field (whose result it
+//   reads).  Any other call that touches world data joins the two streams
+//   first, and the next auxiliary step then waits for everything issued
+//   before it;
+// * the gather stream runs phaser gathers beside the H ghost copies.
+struct StreamGroup {
+	cudaStream_t main, side, gather;
+	cudaEvent_t evMainDone[2], evAuxDone[2], evJoin, evGatherDone;
+	int mainRec[2], auxRec[2], sideUsed, sideWaitsAll;
+	int users;                                // worlds in an own group
+};
+static StreamGroup gDefaultGroup;
+static std::vector<StreamGroup *> gOwnGroups;
+// the group of the world the current call works on (set by bindWorld)
+static StreamGroup *gGroup = &gDefaultGroup;
+#define gStream (gGroup->main)
+#define gSide (gGroup->side)
+#define gGather (gGroup->gather)
+#define gEvMainDone (gGroup->evMainDone)
+#define gEvAuxDone (gGroup->evAuxDone)
+#define gEvJoin (gGroup->evJoin)
+#define gEvGatherDone (gGroup->evGatherDone)
+#define gMainRec (gGroup->mainRec)
+#define gAuxRec (gGroup->auxRec)
+#define gSideUsed (gGroup->sideUsed)
+#define gSideWaitsAll (gGroup->sideWaitsAll)
 // operations that change world data, enqueued so far (launches and uploads)
 static unsigned long long gOps;
-static int gMainRec[2], gAuxRec[2], gSideUsed, gSideWaitsAll = 1;
+
+static int groupCreate(StreamGroup *g)
+{
+	ALIS_CUDA(cudaStreamCreateWithFlags(&g->main, cudaStreamNonBlocking));
+	// the side stream's small blocks take the first free slots
+	int prLeast = 0, prGreatest = 0;
+	ALIS_CUDA(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
+	ALIS_CUDA(cudaStreamCreateWithPriority(&g->side, cudaStreamNonBlocking, prGreatest));
+	ALIS_CUDA(cudaStreamCreateWithFlags(&g->gather, cudaStreamNonBlocking));
+	for (int f = 0; f < 2; f++) {
+		ALIS_CUDA(cudaEventCreateWithFlags(&g->evMainDone[f], cudaEventDisableTiming));
+		ALIS_CUDA(cudaEventCreateWithFlags(&g->evAuxDone[f], cudaEventDisableTiming));
+	}
+	ALIS_CUDA(cudaEventCreateWithFlags(&g->evJoin, cudaEventDisableTiming));
+	ALIS_CUDA(cudaEventCreateWithFlags(&g->evGatherDone, cudaEventDisableTiming));
+	g->sideWaitsAll = 1;
+	return ALISGPU_OK;
+}
+
+static void groupDestroy(StreamGroup *g)
+{
+	cudaStreamSynchronize(g->side), cudaStreamSynchronize(g->gather), cudaStreamSynchronize(g->main);
+	cudaStreamDestroy(g->main), cudaStreamDestroy(g->side), cudaStreamDestroy(g->gather);
+	for (int f = 0; f < 2; f++) cudaEventDestroy(g->evMainDone[f]), cudaEventDestroy(g->evAuxDone[f]);
+	cudaEventDestroy(g->evJoin), cudaEventDestroy(g->evGatherDone);
+}
 
 static void fullJoin(void)
 {
@@ -77,7 +123,7 @@ extern "C" const char *alisgpu_last_error(void) { return gErr; }
 extern "C" void alisgpu__count_launch(void) { gLaunches++, gOps++; }
 extern "C" unsigned long long alisgpu_launch_count(void) { return gLaunches; }
 extern "C" cudaStream_t alisgpu__stream(void) { return gStream; }
-extern "C" void *alisgpu_stream(void) { return (void *)gStream; }
+extern "C" void *alisgpu_stream(void) { return (void *)gDefaultGroup.main; }
 
 extern "C" int alisgpu_init(void)
 {
@@ -88,18 +134,13 @@ extern "C" int alisgpu_init(void)
 	const char *env = getenv("ALISGPU_DEVICE");
 	int dev = env ? atoi(env) : 0;
 	ALIS_CUDA(cudaSetDevice(dev));
-	ALIS_CUDA(cudaStreamCreateWithFlags(&gStream, cudaStreamNonBlocking));
-	// the side stream's small blocks take the first free slots
-	int prLeast = 0, prGreatest = 0;
-	ALIS_CUDA(cudaDeviceGetStreamPriorityRange(&prLeast, &prGreatest));
-	ALIS_CUDA(cudaStreamCreateWithPriority(&gSide, cudaStreamNonBlocking, prGreatest));
-	for (int f = 0; f < 2; f++) {
-		ALIS_CUDA(cudaEventCreateWithFlags(&gEvMainDone[f], cudaEventDisableTiming));
-		ALIS_CUDA(cudaEventCreateWithFlags(&gEvAuxDone[f], cudaEventDisableTiming));
-	}
-	ALIS_CUDA(cudaEventCreateWithFlags(&gEvJoin, cudaEventDisableTiming));
-	ALIS_CUDA(cudaStreamCreateWithFlags(&gGather, cudaStreamNonBlocking));
-	ALIS_CUDA(cudaEventCreateWithFlags(&gEvGatherDone, cudaEventDisableTiming));
+	int rc = groupCreate(&gDefaultGroup);
+	if (rc) return rc;
+	// freed device memory stays in the pool for the next world
+	cudaMemPool_t pool;
+	ALIS_CUDA(cudaDeviceGetDefaultMemPool(&pool, dev));
+	unsigned long long keep = ~0ull;
+	ALIS_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
 	ALIS_CUDA(cudaMalloc(&gErrWord, sizeof(unsigned int)));
 	ALIS_CUDA(cudaMemset(gErrWord, 0, sizeof(unsigned int)));
 	gInit = 1;
@@ -166,8 +207,11 @@ extern "C" int alisgpu_profile_read(int kind, double *ms, unsigned long long *la
 extern "C" int alisgpu_synchronize(void)
 {
 	if (!gInit) return ALISGPU_OK;
-	fullJoin();
-	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	for (size_t q = 0; q <= gOwnGroups.size(); q++) {
+		gGroup = q < gOwnGroups.size() ? gOwnGroups[q] : &gDefaultGroup;
+		fullJoin();
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+	}
 	unsigned int e = 0;
 	ALIS_CUDA(cudaMemcpy(&e, gErrWord, sizeof e, cudaMemcpyDeviceToHost));
 	if (e) return alisgpu__fail(ALISGPU_ERANGE, "device error word %#x", e);
@@ -178,7 +222,13 @@ extern "C" int alisgpu_synchronize(void)
 // world storage
 // ---------------------------------------------------------------------
 struct alisgpu_world {
+	StreamGroup *group;                    // own stream group, or null: the default group
 	alisgpu_geometry g;
+	float *vbuf;                           // source values of large patches
+	int vcap;
+	float *vpin[2];                        // their pinned host staging, two in turn
+	cudaEvent_t vpinFree[2];
+	int vpinCap, vpinNext;
 	Layout L;
 	float *E[2][3], *H[2][3];
 	float *C[3];
@@ -214,6 +264,21 @@ struct alisgpu_world {
 	float4 *matTab;
 };
 
+static inline void bindWorld(const alisgpu_world *w)
+{
+	gGroup = w && w->group ? w->group : &gDefaultGroup;
+}
+
+extern "C" void alisgpu__bind(alisgpu_world *w) { bindWorld(w); }
+
+// A blocking copy ordered on the current group's main stream: device
+// memory from the stream-ordered pool is valid in that stream's order.
+static cudaError_t orderedCopy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind)
+{
+	cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, gStream);
+	return e == cudaSuccess ? cudaStreamSynchronize(gStream) : e;
+}
+
 static int applyPendingGhosts(alisgpu_world *w);
 
 static Layout makeLayout(const alisgpu_geometry *g)
@@ -230,7 +295,7 @@ static Layout makeLayout(const alisgpu_geometry *g)
 
 static int devAlloc(alisgpu_world *w, float **p, size_t n)
 {
-	ALIS_CUDA(cudaMalloc(p, n * sizeof(float)));
+	ALIS_CUDA(alisgpu__mallocAsync(p, n * sizeof(float)));
 	ALIS_CUDA(cudaMemsetAsync(*p, 0, n * sizeof(float), gStream));
 	w->bytes += n * sizeof(float);
 	return ALISGPU_OK;
@@ -262,6 +327,7 @@ extern "C" int alisgpu_world_create(const alisgpu_geometry *g, alisgpu_world **o
 	if (g->iMAX < g->iMIN || g->jMAX < g->jMIN || g->kMAX < g->kMIN)
 		return alisgpu__fail(ALISGPU_EINVAL, "world_create: empty grid");
 	alisgpu_world *w = new alisgpu_world();
+	bindWorld(w);
 	w->g = *g;
 	w->L = makeLayout(g);
 	size_t n = w->L.elems();
@@ -283,43 +349,106 @@ extern "C" int alisgpu_world_create(const alisgpu_geometry *g, alisgpu_world **o
 
 static void freeObjects(alisgpu_world *w)
 {
-	for (void *p : w->objMem) cudaFree(p);
+	for (void *p : w->objMem) alisgpu__freeAsync(p);
 	w->objMem.clear();
 	w->objs.clear();
-	if (w->dObjs) cudaFree(w->dObjs), w->dObjs = 0;
+	if (w->dObjs) alisgpu__freeAsync(w->dObjs), w->dObjs = 0;
 }
 
 extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w) return ALISGPU_OK;
 	cudaStreamSynchronize(gStream);
 	for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
-		if (w->E[m][c]) cudaFree(w->E[m][c]);
-		if (w->H[m][c]) cudaFree(w->H[m][c]);
+		if (w->E[m][c]) alisgpu__freeAsync(w->E[m][c]);
+		if (w->H[m][c]) alisgpu__freeAsync(w->H[m][c]);
 	}
-	for (int c = 0; c < 3; c++) if (w->C[c]) cudaFree(w->C[c]);
-	if (w->planeTab) cudaFree(w->planeTab);
-	if (w->matIdx) cudaFree(w->matIdx);
-	if (w->matTab) cudaFree(w->matTab);
-	for (int grid = 0; grid < 2; grid++) for (int a = 0; a < 3; a++) if (w->sp[grid][a]) cudaFree(w->sp[grid][a]);
+	for (int c = 0; c < 3; c++) if (w->C[c]) alisgpu__freeAsync(w->C[c]);
+	if (w->planeTab) alisgpu__freeAsync(w->planeTab);
+	if (w->matIdx) alisgpu__freeAsync(w->matIdx);
+	if (w->matTab) alisgpu__freeAsync(w->matTab);
+	for (int grid = 0; grid < 2; grid++) for (int a = 0; a < 3; a++) if (w->sp[grid][a]) alisgpu__freeAsync(w->sp[grid][a]);
 	for (int grid = 0; grid < 2; grid++) {
-		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) cudaFree(w->dtd[grid][c]);
-		for (int c = 0; c < 9; c++) if (w->cp[grid][c]) cudaFree(w->cp[grid][c]);
+		for (int c = 0; c < 3; c++) if (w->dtd[grid][c]) alisgpu__freeAsync(w->dtd[grid][c]);
+		for (int c = 0; c < 9; c++) if (w->cp[grid][c]) alisgpu__freeAsync(w->cp[grid][c]);
 		for (int m = 0; m < 2; m++) for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++)
-			if (w->psi[grid][m][f][q].p) cudaFree(w->psi[grid][m][f][q].p);
+			if (w->psi[grid][m][f][q].p) alisgpu__freeAsync(w->psi[grid][m][f][q].p);
 	}
 	freeObjects(w);
-	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) cudaFree(w->cls[f][a]);
+	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) alisgpu__freeAsync(w->cls[f][a]);
 	if (w->evHCells) cudaEventDestroy(w->evHCells);
+	if (w->vbuf) alisgpu__freeAsync(w->vbuf);
+	for (int b = 0; b < 2; b++)
+		if (w->vpin[b]) cudaEventSynchronize(w->vpinFree[b]), cudaFreeHost(w->vpin[b]), cudaEventDestroy(w->vpinFree[b]);
+	StreamGroup *grp = w->group;
 	delete w;
+	if (grp && --grp->users == 0) {
+		groupDestroy(grp);
+		gOwnGroups.erase(std::find(gOwnGroups.begin(), gOwnGroups.end(), grp));
+		delete grp;
+	}
+	gGroup = &gDefaultGroup;
 	return ALISGPU_OK;
 }
 
 extern "C" size_t alisgpu_world_bytes(const alisgpu_world *w) { return w ? w->bytes : 0; }
 
+// Move world w to a stream group of its own (after the work it has
+// queued), so that its steps overlap on the device with those of worlds in
+// other groups.
+extern "C" int alisgpu_world_own_streams(alisgpu_world *w)
+{
+	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_own_streams: null world");
+	if (w->group && w->group->users == 1) return ALISGPU_OK;
+	bindWorld(w);
+	fullJoin();
+	cudaEvent_t done = gEvJoin;
+	ALIS_CUDA(cudaEventRecord(done, gStream));
+	StreamGroup *grp = new StreamGroup();
+	int rc = groupCreate(grp);
+	if (rc) { delete grp; return rc; }
+	ALIS_CUDA(cudaStreamWaitEvent(grp->main, done, 0));
+	if (w->group) w->group->users--;
+	grp->users = 1;
+	gOwnGroups.push_back(grp);
+	w->group = grp;
+	bindWorld(w);
+	return ALISGPU_OK;
+}
+
+// Put world w into the stream group of world parent (a TFSF auxiliary
+// world and the world whose box it feeds).
+extern "C" int alisgpu_world_share_streams(alisgpu_world *w, alisgpu_world *parent)
+{
+	if (!w || !parent) return alisgpu__fail(ALISGPU_EINVAL, "world_share_streams: null world");
+	if (w->group == parent->group) return ALISGPU_OK;
+	bindWorld(w);
+	fullJoin();
+	cudaEvent_t done = gEvJoin;
+	ALIS_CUDA(cudaEventRecord(done, gStream));
+	bindWorld(parent);
+	ALIS_CUDA(cudaStreamWaitEvent(gStream, done, 0));
+	if (w->group && --w->group->users == 0) {
+		StreamGroup *old = w->group;
+		groupDestroy(old);
+		gOwnGroups.erase(std::find(gOwnGroups.begin(), gOwnGroups.end(), old));
+		delete old;
+	}
+	w->group = parent->group;
+	if (w->group) w->group->users++;
+	return ALISGPU_OK;
+}
+
+extern "C" void *alisgpu_world_stream(const alisgpu_world *w)
+{
+	return (void *)(w && w->group ? w->group->main : gDefaultGroup.main);
+}
+
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
+	bindWorld(w);
 	gOps++;
 	fullJoin();
 	if (w) w->pendingE.clear();
@@ -348,16 +477,17 @@ extern "C" int alisgpu_world_reset(alisgpu_world *w)
 // ---------------------------------------------------------------------
 static int upload1D(alisgpu_world *w, float **dst, const float *src, int n)
 {
-	if (*dst) { cudaFree(*dst); *dst = 0; }
+	if (*dst) { alisgpu__freeAsync(*dst); *dst = 0; }
 	if (!src) return ALISGPU_OK;
-	ALIS_CUDA(cudaMalloc(dst, n * sizeof(float)));
-	ALIS_CUDA(cudaMemcpy(*dst, src, n * sizeof(float), cudaMemcpyHostToDevice));
+	ALIS_CUDA(alisgpu__mallocAsync(dst, n * sizeof(float)));
+	ALIS_CUDA(orderedCopy(*dst, src, n * sizeof(float), cudaMemcpyHostToDevice));
 	(void)w;
 	return ALISGPU_OK;
 }
 
 extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *const dtd[3], const float *const cpml[9])
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w || grid < 0 || grid > 1 || !dtd) return alisgpu__fail(ALISGPU_EINVAL, "set_line_tables: bad argument");
 	int len[3] = { w->g.iMAX - w->g.iMIN + 1, w->g.jMAX - w->g.jMIN + 1, w->g.kMAX - w->g.kMIN + 1 };
@@ -369,6 +499,7 @@ extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *
 
 extern "C" int alisgpu_set_spacing(alisgpu_world *w, const float *const dE[3], const float *const dH[3])
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w || !dE || !dH) return alisgpu__fail(ALISGPU_EINVAL, "set_spacing: bad argument");
 	const alisgpu_geometry &g = w->g;
@@ -395,6 +526,7 @@ static int uploadBoxToLayout(alisgpu_world *w, float *dev, const float *host, in
 
 extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *cy, const float *cz)
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "set_eps: null world");
 	const alisgpu_geometry &g = w->g;
@@ -402,7 +534,7 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 	int rc;
 	for (int a = 0; a < 3; a++) {
 		if (!src[a]) {
-			if (w->C[a]) { cudaStreamSynchronize(gStream); cudaFree(w->C[a]); w->bytes -= w->L.elems() * sizeof(float); w->C[a] = 0; }
+			if (w->C[a]) { cudaStreamSynchronize(gStream); alisgpu__freeAsync(w->C[a]); w->bytes -= w->L.elems() * sizeof(float); w->C[a] = 0; }
 			continue;
 		}
 		if (!w->C[a] && (rc = devAlloc(w, &w->C[a], w->L.elems()))) return rc;
@@ -412,8 +544,8 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	// the E half step reads (C[0], C[1], C[2]) at the cells of [MIN, MAX]^3:
 	// with at most 256 distinct triples it reads a byte per cell instead
-	if (w->matIdx) { cudaFree(w->matIdx); w->matIdx = 0; }
-	if (w->matTab) { cudaFree(w->matTab); w->matTab = 0; }
+	if (w->matIdx) { alisgpu__freeAsync(w->matIdx); w->matIdx = 0; }
+	if (w->matTab) { alisgpu__freeAsync(w->matTab); w->matTab = 0; }
 	if (cx && cy && cz) {
 		const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
 		std::vector<unsigned char> idx(w->L.elems(), 0);
@@ -439,10 +571,10 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 			idx[w->L.at(g.iMIN + i, g.jMIN + j, g.kMIN + k)] = (unsigned char)q;
 		}
 		if (ok) {
-			ALIS_CUDA(cudaMalloc(&w->matIdx, idx.size()));
-			ALIS_CUDA(cudaMemcpy(w->matIdx, idx.data(), idx.size(), cudaMemcpyHostToDevice));
-			ALIS_CUDA(cudaMalloc(&w->matTab, tab.size() * sizeof(float4)));
-			ALIS_CUDA(cudaMemcpy(w->matTab, tab.data(), tab.size() * sizeof(float4), cudaMemcpyHostToDevice));
+			ALIS_CUDA(alisgpu__mallocAsync(&w->matIdx, idx.size()));
+			ALIS_CUDA(orderedCopy(w->matIdx, idx.data(), idx.size(), cudaMemcpyHostToDevice));
+			ALIS_CUDA(alisgpu__mallocAsync(&w->matTab, tab.size() * sizeof(float4)));
+			ALIS_CUDA(orderedCopy(w->matTab, tab.data(), tab.size() * sizeof(float4), cudaMemcpyHostToDevice));
 		}
 	}
 	return ALISGPU_OK;
@@ -450,6 +582,7 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 
 extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *objs)
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w || n < 0 || (n && !objs)) return alisgpu__fail(ALISGPU_EINVAL, "set_dispersive: bad argument");
 	cudaStreamSynchronize(gStream);
@@ -475,7 +608,7 @@ extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dis
 			int rc = devAlloc(w, &d, cells);
 			if (rc) return rc;
 			w->objMem.push_back(d);
-			ALIS_CUDA(cudaMemcpy(d, s.fill[a], cells * sizeof(float), cudaMemcpyHostToDevice));
+			ALIS_CUDA(orderedCopy(d, s.fill[a], cells * sizeof(float), cudaMemcpyHostToDevice));
 			o.fill[a] = d;
 		}
 		o.cond = s.a[0] != 0 || s.a[1] != 0 || s.a[2] != 0;
@@ -494,8 +627,8 @@ extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dis
 		w->objs.push_back(o);
 	}
 	if (n) {
-		ALIS_CUDA(cudaMalloc(&w->dObjs, n * sizeof(DevObj)));
-		ALIS_CUDA(cudaMemcpy(w->dObjs, w->objs.data(), n * sizeof(DevObj), cudaMemcpyHostToDevice));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->dObjs, n * sizeof(DevObj)));
+		ALIS_CUDA(orderedCopy(w->dObjs, w->objs.data(), n * sizeof(DevObj), cudaMemcpyHostToDevice));
 	}
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	return ALISGPU_OK;
@@ -509,6 +642,7 @@ static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
 
 extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
 {
+	bindWorld(w);
 	fullJoin();
 	if (w) {
 		int rc = applyPendingGhosts(w);
@@ -525,6 +659,7 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 
 extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
 {
+	bindWorld(w);
 	gOps++;
 	fullJoin();
 	if (w && field == 0) w->pendingE.clear();        // the host's halo wins
@@ -550,6 +685,7 @@ __global__ void k_current_gather(const CurGather P)
 
 extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *host)
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w || !host || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_currents_download: bad argument");
 	const DevObj &o = w->objs[n];
@@ -565,9 +701,9 @@ extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *
 	const size_t n4 = (size_t)P.cells * P.count;
 	if (n4 > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
-		if (w->planeTab) cudaFree(w->planeTab);
+		if (w->planeTab) alisgpu__freeAsync(w->planeTab);
 		w->planeTab = 0, w->planeTabFloats = 0;
-		ALIS_CUDA(cudaMalloc(&w->planeTab, n4 * sizeof(float)));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->planeTab, n4 * sizeof(float)));
 		w->planeTabFloats = n4;
 	}
 	P.out = w->planeTab;
@@ -581,6 +717,7 @@ extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *
 
 extern "C" int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host)
 {
+	bindWorld(w);
 	fullJoin();
 	if (!w || !host || n < 0 || n >= (int)w->objs.size() || m < 0 || m > w->g.complexField || comp < 0 || comp > 2)
 		return alisgpu__fail(ALISGPU_EINVAL, "current_download: bad argument");
@@ -991,7 +1128,10 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 // sources, in list order; one block so later patches see earlier ones
 // (reference src/update.c:161-179)
 #define ALIS_MAXSRC 32
-#define ALIS_MAXSRCV 2048
+// source values travel in the launch parameters up to this count, beyond
+// it through the world's device buffer (large launch parameters cost every
+// launch host and device time)
+#define ALIS_MAXSRCV 256
 struct SourceParams {
 	int n;
 	Layout L;
@@ -1207,6 +1347,7 @@ struct SmallStepParams {
 	float *F[2][3];                           // the stepped field per m (m clamped)
 	alisgpu_source_patch src[ALIS_MAXSRC];
 	alisgpu_ghost_copy ghost[ALIS_SMALL_GHOSTS];
+	const float *vdev;                        // values beyond the inline buffer
 	float v[ALIS_MAXSRCV];
 };
 
@@ -1234,7 +1375,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_const
 				atomicOr(S.P[0].err, 4u);
 				continue;
 			}
-			F[L.at(i, j, k)] += S.v[p.voff + t];
+			F[L.at(i, j, k)] += S.vdev ? S.vdev[p.voff + t] : S.v[p.voff + t];
 		}
 		__syncthreads();
 	}
@@ -1286,8 +1427,8 @@ static void fillTfsf(DevTfsf &T, const alisgpu_tfsf &s, int field, const float *
 	int top[3] = { g.iMAX, g.jMAX, g.kMAX };
 	for (int a = 0; a < 3; a++) {
 		float v0 = 0, v1 = 0;
-		if (lo[a] >= base[a] && lo[a] <= top[a]) cudaMemcpy(&v0, dtdMain[a] + (lo[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
-		if (hi[a] >= base[a] && hi[a] <= top[a]) cudaMemcpy(&v1, dtdMain[a] + (hi[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
+		if (lo[a] >= base[a] && lo[a] <= top[a]) orderedCopy(&v0, dtdMain[a] + (lo[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
+		if (hi[a] >= base[a] && hi[a] <= top[a]) orderedCopy(&v1, dtdMain[a] + (hi[a] - base[a]), sizeof(float), cudaMemcpyDeviceToHost);
 		T.dtdMin[a] = v0, T.dtdMax[a] = v1;
 	}
 }
@@ -1390,14 +1531,14 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 			if (!same) {
 				seen.assign(gl, gl + n);
 				unsigned int *flag = 0, h = 0;
-				ALIS_CUDA(cudaMalloc(&flag, sizeof h));
+				ALIS_CUDA(alisgpu__mallocAsync(&flag, sizeof h));
 				ALIS_CUDA(cudaMemsetAsync(flag, 0, sizeof h, gStream));
 				k_ghost_chain<true><<<blocks, 256, 0, gStream>>>(GL, flag);
 				alisgpu__count_launch();
 				ALIS_CUDA(cudaGetLastError());
 				ALIS_CUDA(cudaMemcpyAsync(&h, flag, sizeof h, cudaMemcpyDeviceToHost, gStream));
 				ALIS_CUDA(cudaStreamSynchronize(gStream));
-				cudaFree(flag);
+				alisgpu__freeAsync(flag);
 				w->ghostChain[field] = h == 0;
 			}
 			if (w->ghostChain[field]) {
@@ -1485,8 +1626,45 @@ static int applyPendingGhosts(alisgpu_world *w)
 	return rc;
 }
 
+// Source values of a half step into the world's device buffer on stream
+// st, through two pinned host buffers in turn: the copy is asynchronous
+// and the consuming launch on st follows it.
+static int stageValues(alisgpu_world *w, const float *vals, int n, cudaStream_t st, const float **dev)
+{
+	if (n > w->vcap) {
+		// ordered on the stream that uses the buffer
+		if (w->vbuf) ALIS_CUDA(cudaFreeAsync(w->vbuf, st));
+		w->vbuf = 0, w->vcap = 0;
+		ALIS_CUDA(cudaMallocAsync((void **)&w->vbuf, n * sizeof(float), st));
+		w->vcap = n;
+	}
+	if (n > w->vpinCap) {
+		for (int b = 0; b < 2; b++) {
+			if (w->vpin[b]) {
+				ALIS_CUDA(cudaEventSynchronize(w->vpinFree[b]));
+				ALIS_CUDA(cudaFreeHost(w->vpin[b]));
+				w->vpin[b] = 0;
+			} else {
+				ALIS_CUDA(cudaEventCreateWithFlags(&w->vpinFree[b], cudaEventDisableTiming));
+				ALIS_CUDA(cudaEventRecord(w->vpinFree[b], st));
+			}
+			ALIS_CUDA(cudaMallocHost(&w->vpin[b], n * sizeof(float)));
+		}
+		w->vpinCap = n;
+	}
+	const int b = w->vpinNext;
+	w->vpinNext ^= 1;
+	ALIS_CUDA(cudaEventSynchronize(w->vpinFree[b]));
+	memcpy(w->vpin[b], vals, n * sizeof(float));
+	ALIS_CUDA(cudaMemcpyAsync(w->vbuf, w->vpin[b], n * sizeof(float), cudaMemcpyHostToDevice, st));
+	ALIS_CUDA(cudaEventRecord(w->vpinFree[b], st));
+	*dev = w->vbuf;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s)
 {
+	bindWorld(w);
 	if (!w || !s || s->field < 0 || s->field > 1) return alisgpu__fail(ALISGPU_EINVAL, "half_step: bad argument");
 	if (s->ntfsf > ALIS_MAXTFSF) return alisgpu__fail(ALISGPU_ERANGE, "half_step: %d TFSF boxes (max %d)", s->ntfsf, ALIS_MAXTFSF);
 	const alisgpu_geometry &g = w->g;
@@ -1541,7 +1719,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			mark(0, o.i0, o.i1, bit), mark(1, o.j0, o.j1, bit), mark(2, o.k0, o.k1, bit);
 		}
 		for (int a = 0; a < 3; a++) {
-			if (!w->cls[field][a]) ALIS_CUDA(cudaMalloc(&w->cls[field][a], n[a] * sizeof(unsigned short)));
+			if (!w->cls[field][a]) ALIS_CUDA(alisgpu__mallocAsync(&w->cls[field][a], n[a] * sizeof(unsigned short)));
 			if (w->clsHost[field][a] != t[a]) {
 				w->clsHost[field][a] = t[a];
 				ALIS_CUDA(cudaMemcpyAsync(w->cls[field][a], w->clsHost[field][a].data(), n[a] * sizeof(unsigned short), cudaMemcpyHostToDevice, gStream));
@@ -1557,7 +1735,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	const bool side = s->concurrent && !gProfOn;
 	if (!side && gAuxRec[1 - field]) ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvAuxDone[1 - field], 0));
 	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
-	if (cells <= ALIS_SMALL_CELLS && s->nsrc <= ALIS_MAXSRC && s->nvalues <= ALIS_MAXSRCV && s->nghost <= ALIS_SMALL_GHOSTS) {
+	if (cells <= ALIS_SMALL_CELLS && s->nsrc <= ALIS_MAXSRC && s->nghost <= ALIS_SMALL_GHOSTS) {
 		static SmallStepParams S;
 		S.nm = 1 + g.complexField;
 		for (int m = 0; m < S.nm; m++) {
@@ -1579,7 +1757,6 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		S.nsrc = s->nsrc, S.nghost = s->nghost;
 		if (s->nsrc) memcpy(S.src, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		if (s->nghost) memcpy(S.ghost, s->ghost, s->nghost * sizeof(alisgpu_ghost_copy));
-		if (s->nvalues) memcpy(S.v, s->values, s->nvalues * sizeof(float));
 		// on the side stream: after the parent's last step of the other
 		// field, or after everything when a join asked for that
 		cudaStream_t st = gStream;
@@ -1592,6 +1769,13 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			} else if (gMainRec[1 - field]) {
 				ALIS_CUDA(cudaStreamWaitEvent(gSide, gEvMainDone[1 - field], 0));
 			}
+		}
+		S.vdev = 0;
+		if (s->nvalues > ALIS_MAXSRCV) {
+			int rc = stageValues(w, s->values, s->nvalues, st, &S.vdev);
+			if (rc) return rc;
+		} else if (s->nvalues) {
+			memcpy(S.v, s->values, s->nvalues * sizeof(float));
 		}
 		int slot = alisgpu__prof_start();
 		if (field == 0) k_small_step<1><<<1, SMALL_THREADS, 0, st>>>(S);
@@ -1644,21 +1828,11 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		memcpy(SP.p, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		SP.vdev = 0;
 		SP.err = gErrWord;
-		static float *vbuf;
-		static int vcap;
 		if (s->nvalues <= ALIS_MAXSRCV) {
 			memcpy(SP.v, s->values, s->nvalues * sizeof(float));
 		} else {
-			// large patches: values staged in device memory (ordered on the stream)
-			if (s->nvalues > vcap) {
-				cudaStreamSynchronize(gStream);
-				if (vbuf) cudaFree(vbuf);
-				ALIS_CUDA(cudaMalloc(&vbuf, s->nvalues * sizeof(float)));
-				vcap = s->nvalues;
-			}
-			ALIS_CUDA(cudaMemcpyAsync(vbuf, s->values, s->nvalues * sizeof(float), cudaMemcpyHostToDevice, gStream));
-			ALIS_CUDA(cudaStreamSynchronize(gStream));
-			SP.vdev = vbuf;
+			int rc = stageValues(w, s->values, s->nvalues, gStream, &SP.vdev);
+			if (rc) return rc;
 		}
 		int slot = alisgpu__prof_start();
 		k_sources<<<1, 256, 0, gStream>>>(SP);
@@ -1783,6 +1957,7 @@ __global__ void __launch_bounds__(256) k_plane_total(const PlaneParams P)
 
 extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2], float *out)
 {
+	bindWorld(w);
 	if (!w || axis < 0 || axis > 2 || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: bad argument");
 	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: spacing tables not set");
 	const alisgpu_geometry &g = w->g;
@@ -1801,9 +1976,9 @@ extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int
 	const size_t floats = 1 + (size_t)n1 + n2;
 	if (floats > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
-		if (w->planeTab) cudaFree(w->planeTab);
+		if (w->planeTab) alisgpu__freeAsync(w->planeTab);
 		w->planeTab = 0, w->planeTabFloats = 0;
-		ALIS_CUDA(cudaMalloc(&w->planeTab, floats * sizeof(float)));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->planeTab, floats * sizeof(float)));
 		w->planeTabFloats = floats;
 	}
 	PlaneParams P;
@@ -1859,6 +2034,7 @@ __global__ void k_box_gather(const BoxGatherParams P)
 
 extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1, int k0, int k1, float *host)
 {
+	bindWorld(w);
 	if (!w || !host || i1 < i0 || j1 < j0 || k1 < k0) return alisgpu__fail(ALISGPU_EINVAL, "field_box_download: bad argument");
 	const Layout &L = w->L;
 	if (i0 < L.i0 || i1 >= L.i0 + L.ni || j0 < L.j0 || j1 >= L.j0 + L.nj || k0 < L.k0 || k1 >= L.k0 + L.nk)
@@ -1879,9 +2055,9 @@ extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int 
 	if (n >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box of %zu values too large", n);
 	if (n > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
-		if (w->planeTab) cudaFree(w->planeTab);
+		if (w->planeTab) alisgpu__freeAsync(w->planeTab);
 		w->planeTab = 0, w->planeTabFloats = 0;
-		ALIS_CUDA(cudaMalloc(&w->planeTab, n * sizeof(float)));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->planeTab, n * sizeof(float)));
 		w->planeTabFloats = n;
 	}
 	P.out = w->planeTab;
@@ -1945,6 +2121,7 @@ __global__ void k_slice_dft(const SliceDftParams P)
 
 extern "C" int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alisgpu_slice_dft **out)
 {
+	bindWorld(w);
 	if (!w || !box || !out || box[1] < box[0] || box[3] < box[2] || box[5] < box[4])
 		return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_create: bad argument");
 	const size_t cells = (size_t)(1 + box[1] - box[0]) * (1 + box[3] - box[2]) * (1 + box[5] - box[4]);
@@ -1952,10 +2129,10 @@ extern "C" int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alis
 	alisgpu_slice_dft *d = new alisgpu_slice_dft();
 	d->w = w;
 	d->i0 = box[0], d->i1 = box[1], d->j0 = box[2], d->j1 = box[3], d->k0 = box[4], d->k1 = box[5];
-	cudaError_t e = cudaMalloc(&d->acc, 2 * cells * sizeof(float));
+	cudaError_t e = alisgpu__mallocAsync(&d->acc, 2 * cells * sizeof(float));
 	if (e == cudaSuccess) e = cudaMemsetAsync(d->acc, 0, 2 * cells * sizeof(float), gStream);
 	if (e != cudaSuccess) {
-		cudaFree(d->acc);
+		alisgpu__freeAsync(d->acc);
 		delete d;
 		return alisgpu__check(e, "slice_dft_create");
 	}
@@ -1966,6 +2143,7 @@ extern "C" int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alis
 extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int comp, int avg, const int sym[3], const float par[3],
                                      float re, float im)
 {
+	if (d) bindWorld(d->w);
 	if (!d || field < 0 || field > 1 || m < 0 || m > 1 || comp < 0 || comp > 2 || avg < 0 || avg > 1 || !sym || !par)
 		return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_add: bad argument");
 	alisgpu_world *w = d->w;
@@ -2019,6 +2197,7 @@ extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int
 
 extern "C" int alisgpu_slice_dft_download(alisgpu_slice_dft *d, float *F, float *G)
 {
+	if (d) bindWorld(d->w);
 	if (!d || !F || !G) return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_download: bad argument");
 	const size_t cells = (size_t)(1 + d->i1 - d->i0) * (1 + d->j1 - d->j0) * (1 + d->k1 - d->k0);
 	ALIS_CUDA(cudaMemcpyAsync(F, d->acc, cells * sizeof(float), cudaMemcpyDeviceToHost, gStream));
@@ -2029,9 +2208,10 @@ extern "C" int alisgpu_slice_dft_download(alisgpu_slice_dft *d, float *F, float 
 
 extern "C" int alisgpu_slice_dft_destroy(alisgpu_slice_dft *d)
 {
+	if (d) bindWorld(d->w);
 	if (!d) return ALISGPU_OK;
 	cudaStreamSynchronize(gStream);
-	cudaFree(d->acc);
+	alisgpu__freeAsync(d->acc);
 	delete d;
 	return ALISGPU_OK;
 }
@@ -2142,6 +2322,7 @@ __global__ void __launch_bounds__(256) k_absorb_total(const AbsorbParams P)
 
 extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 {
+	bindWorld(w);
 	if (!w || !out || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: bad argument");
 	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: spacing tables not set");
 	if (!w->C[0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: world has no eps maps");
@@ -2160,9 +2341,9 @@ extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 	const size_t floats = 3 * cols + 1;
 	if (floats > w->planeTabFloats) {
 		ALIS_CUDA(cudaStreamSynchronize(gStream));
-		if (w->planeTab) cudaFree(w->planeTab);
+		if (w->planeTab) alisgpu__freeAsync(w->planeTab);
 		w->planeTab = 0, w->planeTabFloats = 0;
-		ALIS_CUDA(cudaMalloc(&w->planeTab, floats * sizeof(float)));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->planeTab, floats * sizeof(float)));
 		w->planeTabFloats = floats;
 	}
 	float *t = w->planeTab;
@@ -2260,13 +2441,35 @@ __global__ void k_twm(const TwmParams P)
 	P.F[A][c] = f;
 }
 
+// Order the signal world's stream after (before = false) or the pump
+// world's stream before (before = true) the other when they are in
+// different stream groups.
+static int crossGroup(const alisgpu_world *ws, const alisgpu_world *wp, bool pumpFirst)
+{
+	StreamGroup *gs = ws->group ? ws->group : &gDefaultGroup, *gp = wp->group ? wp->group : &gDefaultGroup;
+	if (gs == gp) return ALISGPU_OK;
+	StreamGroup *from = pumpFirst ? gp : gs, *to = pumpFirst ? gs : gp;
+	StreamGroup *keep = gGroup;
+	gGroup = from;
+	fullJoin();
+	ALIS_CUDA(cudaEventRecord(from->evJoin, from->main));
+	ALIS_CUDA(cudaStreamWaitEvent(to->main, from->evJoin, 0));
+	gGroup = keep;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
                                      const float d[3][6], float Alt)
 {
-	fullJoin();
 	if (!ws || !wp1 || !wp2 || !d || n < 0 || n >= (int)ws->objs.size() || m < 0 || m > ws->g.complexField ||
 	    m > wp1->g.complexField || m > wp2->g.complexField)
 		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: bad argument");
+	// the pumps' fields are read on the signal world's stream
+	int rc = crossGroup(ws, wp1, true);
+	if (!rc) rc = crossGroup(ws, wp2, true);
+	if (rc) return rc;
+	bindWorld(ws);
+	fullJoin();
 	if (!ws->C[0]) return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: signal world has no eps maps");
 	if (memcmp(&ws->L, &wp1->L, sizeof(Layout)) || memcmp(&ws->L, &wp2->L, sizeof(Layout)))
 		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: pump and signal worlds differ in grid");
@@ -2299,7 +2502,11 @@ extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1
 		alisgpu__count_launch();
 		ALIS_CUDA(cudaGetLastError());
 	}
-	return ALISGPU_OK;
+	// the pumps' next steps overwrite what was read
+	rc = crossGroup(ws, wp1, false);
+	if (!rc) rc = crossGroup(ws, wp2, false);
+	bindWorld(ws);
+	return rc;
 }
 
 // field pointers of set m for the phaser gather kernel

@@ -88,6 +88,9 @@ int alis_be_vox_bounds(void *v, int N, int *box);
 int alis_be_vox_fill(void *v, int o, const int *b, float *fx, float *fy, float *fz);
 int alis_be_vox_fill_edge(void *v, int o, int axis, int n, int u0, int u1, int v0, int v1, float *out);
 void alis_be_vox_end(void *v);
+/* Streams of W's own for W and its TFSF auxiliary worlds (a backend
+ * without streams does nothing). */
+void alis_be_world_streams(world W);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
 

@@ -488,6 +488,11 @@ void alisSyncHost(world W)
 	alis_be_sync_phasers_of(W);
 }
 
+void alisWorldStreams(world W)
+{
+	alis_be_world_streams(W);
+}
+
 
 /* --- HDF5 I/O (reference src/world.c:469-537) ---
  * libhdf5 is not part of this build; the two entry points exist so that

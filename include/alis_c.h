@@ -149,8 +149,11 @@ void *h5read(int*, char*, ...);
 void h5write(int*, float*, char*, ...);
 
 /* Engine additions (no reference counterpart): refresh every host mirror
- * of W (fields, ADE currents, phasers) from the device. */
+ * of W (fields, ADE currents, phasers) from the device; give W (with its
+ * TFSF auxiliary worlds) streams of its own, so that the steps of several
+ * worlds driven in turn overlap on the device. */
 void alisSyncHost(world W);
+void alisWorldStreams(world W);
 
 
 /* ---- objects and shapes (reference src/alis_c.h:144-176) ---- */

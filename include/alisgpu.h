@@ -84,6 +84,16 @@ int alisgpu_world_destroy(alisgpu_world *w);
 int alisgpu_world_reset(alisgpu_world *w);
 /* Device bytes held by the world (fields, psi, maps, currents). */
 size_t alisgpu_world_bytes(const alisgpu_world *w);
+/* Stream groups (no counterpart in the reference, which runs one world at
+ * a time on the host cores).  Every world starts in the default group,
+ * whose main stream alisgpu_stream() returns.  own_streams moves w to a
+ * group of its own after its queued work, so its steps overlap on the
+ * device with those of worlds in other groups; share_streams puts w into
+ * parent's group (a TFSF auxiliary world with the world it feeds).
+ * alisgpu_synchronize() waits for every group. */
+int alisgpu_world_own_streams(alisgpu_world *w);
+int alisgpu_world_share_streams(alisgpu_world *w, alisgpu_world *parent);
+void *alisgpu_world_stream(const alisgpu_world *w);
 
 /* 1-D tables of the E (grid 0) or H (grid 1) lattice: dtd[3] = dt/dx,
  * dt/dy, dt/dz indexed from iMIN/jMIN/kMIN; cpml[9] = xP, xPy, xPz, yP,

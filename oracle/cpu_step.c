@@ -622,6 +622,7 @@ int alis_be_sync_box(world W, int i0, int i1, int j0, int j1, int k0, int k1)
 }
 void alis_be_hold_sync(world W) { (void)W; }
 int alis_be_object_absorption(world W, int n, float *out) { (void)W, (void)n, (void)out; return 0; }
+void alis_be_world_streams(world W) { (void)W; }
 void *alis_be_slice_dft_begin(world W, const int b[6]) { (void)W, (void)b; return NULL; }
 int alis_be_slice_dft_add(void *h, world W, field *f, float re, float im) { (void)h, (void)W, (void)f, (void)re, (void)im; return 0; }
 int alis_be_slice_dft_read(void *h, float *F, float *G) { (void)h, (void)F, (void)G; return 0; }

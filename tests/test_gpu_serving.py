@@ -1,0 +1,54 @@
+"""The served form (alis_gb300/bench/serve.c): a Poisson stream of mixed
+requests -- vacuum with a dielectric ball, Drude bowtie antennas,
+photonic-crystal k-point runs with complex fields -- admitted by device
+footprint and stepped in turn, each world on streams of its own so that
+their work overlaps on the device.  Every request's result (its outgoing
+phaser flux summed over frequencies and k-points) must be bit-identical
+in the mix, run one after another on the default streams, and run alone.
+Prints the throughput of the served and the sequential runs and the
+served latency percentiles."""
+import json
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _run(exe, args):
+    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    res, summary = {}, None
+    for line in r.stdout.splitlines():
+        p = line.split()
+        if p and p[0] == "R":
+            res[int(p[1])] = (int(p[2]), p[6])
+        elif line.startswith("{"):
+            summary = json.loads(line)
+    assert summary is not None, r.stdout[-2000:]
+    return res, summary
+
+
+@pytest.mark.gpu
+def test_served_results_equal_alone_and_sequential():
+    from alis_gb300 import build
+    build.build_engine()
+    exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                             os.path.join(ROOT, "tests", "drivers", "bin", "serve"), "engine", extra=["-lm"])
+    n, seed = 24, 7
+    served, s1 = _run(exe, ["served", n, 2000, seed, "small", 8])
+    seq, s2 = _run(exe, ["sequential", n, 2000, seed, "small"])
+    assert len(served) == n and len(seq) == n
+    for q in range(n):
+        assert served[q] == seq[q], (q, served[q], seq[q])
+    # alone: one request of each kind
+    kinds = {}
+    for q in range(n):
+        kinds.setdefault(served[q][0], q)
+    assert set(kinds) == {0, 1, 2}
+    for kind, q in sorted(kinds.items()):
+        alone, _ = _run(exe, ["alone", n, 2000, seed, "small", q])
+        assert alone[q] == served[q], (q, alone[q], served[q])
+    print("served %.2f Gcell/s (p50 %.1f ms, p99 %.1f ms), sequential %.2f Gcell/s" %
+          (s1["gcell_per_s"], s1["latency_ms"]["p50"], s1["latency_ms"]["p99"], s2["gcell_per_s"]))
