@@ -1339,6 +1339,10 @@ __global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ Gho
 // path; one launch instead of one per phase and ghost group.  The block
 // is small so that it finds room beside a running large-world kernel.
 #define ALIS_SMALL_CELLS 65536
+// a world stepped on its own takes one block only up to this size: one
+// block is one SM, so larger worlds run faster as a grid even with the
+// extra source and ghost launches
+#define ALIS_TINY_CELLS 4096
 #define ALIS_SMALL_GHOSTS 48
 struct SmallStepParams {
 	HalfStepParams P[2];                      // per m
@@ -1735,7 +1739,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	const bool side = s->concurrent && !gProfOn;
 	if (!side && gAuxRec[1 - field]) ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvAuxDone[1 - field], 0));
 	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
-	if (cells <= ALIS_SMALL_CELLS && s->nsrc <= ALIS_MAXSRC && s->nghost <= ALIS_SMALL_GHOSTS) {
+	if (cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC && s->nghost <= ALIS_SMALL_GHOSTS) {
 		static SmallStepParams S;
 		S.nm = 1 + g.complexField;
 		for (int m = 0; m < S.nm; m++) {
