@@ -4,7 +4,7 @@
  * stepped in turn, each world on streams of its own so that their steps
  * overlap on the device.
  *
- *   serve <mode> <requests> <rate/s> <seed> <small|large> [slots] [budget GB]
+ *   serve <mode> <requests> <rate/s> <seed> <small|large|sweep> [slots] [budget GB]
  *
  * mode served:     Poisson arrivals at <rate>; a request is admitted when
  *                  a slot is free and its footprint fits the budget; the
@@ -20,6 +20,14 @@
  * Pulse waveforms; grid and step counts drawn per request.  Each request
  * reports the outgoing flux of its phaser box summed over frequencies
  * (and k-points) as its result.
+ *
+ * The sweep mix is the batched metasurface sweep instead: unit cells of
+ * 32-96 cells laterally (periodic) and 64-256 along z (10-cell CPML on
+ * both z faces), a TiO2-like Lorentz pillar of radius 40-120 nm and
+ * height 200-600 nm on a glass substrate, a normal-incidence pulse
+ * through a TFSF box, and a transmission phaser plane of 32 wavelengths;
+ * 3000 steps each (SERVE_STEPS overrides).  Result: the plane's flux
+ * summed over the wavelengths.
  *
  * Output: one line per finished request "R id kind cells steps latency_ms
  * result(hex)", then one JSON line with throughput and latency percentiles.
@@ -49,6 +57,8 @@ static double uniform(void)
 
 typedef struct {
 	int kind, half, steps, nk, ndip, gap;
+	int nx, nz;                              /* unit cell: lateral and z cells */
+	float rad, hgt;                          /* unit cell: pillar radius and height (nm) */
 	float dip[3][3];
 	int wave[3];
 	double arrival;
@@ -62,7 +72,7 @@ typedef struct {
 } request;
 
 static request R[MAXREQ];
-static int small = 1;
+static int small = 1, sweep = 0;
 /* host wall time spent setting requests up, stepping them, finishing them */
 static double tSetup, tStep, tFinish;
 
@@ -70,6 +80,18 @@ static double tSetup, tStep, tFinish;
 static void drawRequest(int q, double *t, double rate)
 {
 	request *r = &R[q];
+	if (sweep) {
+		r->kind = 3, r->nk = 1;
+		r->nx = 32 + (int)(65 * uniform());
+		r->nz = 64 + (int)(193 * uniform());
+		r->rad = (float)(40 + 80 * uniform());
+		r->hgt = (float)(200 + 400 * uniform());
+		const char *e = getenv("SERVE_STEPS");
+		r->steps = e ? atoi(e) : 3000;
+		*t += -log(1 - uniform()) / rate;
+		r->arrival = *t;
+		return;
+	}
 	double u = uniform();
 	r->kind = u < 0.5 ? 0 : u < 0.8 ? 1 : 2;
 	int lo = small ? 14 : 40, hi = small ? 24 : 96;                /* half size in cells */
@@ -94,6 +116,33 @@ static void setupRequest(int q, int streams)
 	request *r = &R[q];
 	float L = 10.0f * r->half;
 	r->cells = 0;
+	if (r->kind == 3) {
+		/* a unit cell of the sweep: the pillar sits on the substrate, whose
+		 * top lies 50 nm above the lower CPML; the TFSF box starts 50 nm
+		 * below the substrate top and ends 120 nm below the upper CPML; the
+		 * phaser plane lies 20 nm above the TFSF box */
+		float a = 10.0f * r->nx, Lz = 10.0f * r->nz;
+		dom D = {{-a / 2, a / 2 - 10}, {-a / 2, a / 2 - 10}, {-Lz / 2, Lz / 2 - 10}};
+		res Re = {5, {10}, {1240}};
+		sur S = {{PBC}, {PBC}, {PML, PML}, {10}};
+		world W = createWorld(D, Re, S, "");
+		float zb = -Lz / 2 + 150, ztop = Lz / 2 - 10 - 100 - 120;
+		float h = r->hgt < ztop - zb - 40 ? r->hgt : ztop - zb - 40;
+		float rr = r->rad < a / 2 - 20 ? r->rad : a / 2 - 20;
+		object Pillar = {RodZ, {{-rr, rr}, {-rr, rr}, {zb, zb + h}}};
+		object Sub = {Box, {{-INF, INF}, {-INF, INF}, {-INF, zb}}};
+		matter TiO2 = {{5.5}, {{4.5, 0.05, 1.0}}};
+		putObjects(W, TiO2, Pillar, n(1.45), Sub, Air);
+		dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {zb - 50, ztop}};
+		planewave(W, T, Ppol, 0, 0, Pulse, 600, 150);
+		phaser P = createPhasers(W, 400, 800, 400.0f / 31, -INF, INF, -INF, INF, ztop + 20, ztop + 20);
+		if (streams) alisWorldStreams(W);
+		r->W[0] = W, r->P[0] = P;
+		r->cells = (long)W->iNUM * W->jNUM * W->kNUM;
+		r->done = 0;
+		tSetup += now() - t0;
+		return;
+	}
 	for (int k = 0; k < r->nk; k++) {
 		world W;
 		if (r->kind == 0) {
@@ -153,6 +202,11 @@ static void setupRequest(int q, int streams)
 static double footprint(int q)
 {
 	request *r = &R[q];
+	if (r->kind == 3) {
+		/* fields, eps^-1, two CPML slabs, a phaser plane of 32 wavelengths, the TFSF column */
+		double cells = (r->nx + 2.0) * (r->nx + 2.0) * (r->nz + 2.0), face = (r->nx + 2.0) * (r->nx + 2.0);
+		return cells * (24 + 12) + 2 * 10 * face * 32 + face * (4 * 8 * 32 * 2 + 16 * 64);
+	}
 	double n = 2 * r->half + 2;
 	double cells = n * n * n, face = n * n;
 	double per = (r->kind == 2 ? 2 : 1) * 6 * 4.0 + 12 + 0.5 * 16;
@@ -203,7 +257,8 @@ int main(int argc, char **argv)
 	int nreq = atoi(argv[2]);
 	double rate = atof(argv[3]);
 	rng = strtoull(argv[4], 0, 10);
-	small = strcmp(argv[5], "large") != 0;
+	small = strcmp(argv[5], "large") != 0 && strcmp(argv[5], "sweep") != 0;
+	sweep = strcmp(argv[5], "sweep") == 0;
 	int slots = argc > 6 ? atoi(argv[6]) : 16;
 	double budget = (argc > 7 ? atof(argv[7]) : 64) * 1e9;
 	if (nreq < 1 || nreq > MAXREQ) return 2;
@@ -285,7 +340,7 @@ int main(int argc, char **argv)
 	       "\"budget_gb\": %g, \"wall_s\": %.4f, \"cell_updates\": %.6g, \"gcell_per_s\": %.4f, "
 	       "\"latency_ms\": {\"p50\": %.3f, \"p99\": %.3f, \"max\": %.3f}, \"achieved_per_s\": %.3f, "
 	       "\"host_s\": {\"setup\": %.4f, \"step\": %.4f, \"finish\": %.4f}}\n",
-	       mode, finished, rate, argv[4], small ? "small" : "large", slots, budget / 1e9, wall, cellSteps,
+	       mode, finished, rate, argv[4], argv[5], slots, budget / 1e9, wall, cellSteps,
 	       cellSteps / wall / 1e9, 1e3 * p50, 1e3 * p99, 1e3 * lat[nl - 1], finished / wall, tSetup, tStep, tFinish);
 	return 0;
 }

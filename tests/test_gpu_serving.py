@@ -16,8 +16,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _run(exe, args):
-    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=900)
+def _run(exe, args, env=None):
+    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, timeout=900, env=env)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     res, summary = {}, None
     for line in r.stdout.splitlines():
@@ -52,3 +52,19 @@ def test_served_results_equal_alone_and_sequential():
         assert alone[q] == served[q], (q, alone[q], served[q])
     print("served %.2f Gcell/s (p50 %.1f ms, p99 %.1f ms), sequential %.2f Gcell/s" %
           (s1["gcell_per_s"], s1["latency_ms"]["p50"], s1["latency_ms"]["p99"], s2["gcell_per_s"]))
+
+
+@pytest.mark.gpu
+def test_served_unit_cell_sweep_equals_sequential():
+    """The metasurface sweep mix (periodic unit cells with a TFSF pulse and
+    a transmission plane), shortened to 400 steps per cell."""
+    from alis_gb300 import build
+    build.build_engine()
+    exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                             os.path.join(ROOT, "tests", "drivers", "bin", "serve"), "engine", extra=["-lm"])
+    env = dict(os.environ, SERVE_STEPS="400")
+    served, s1 = _run(exe, ["served", 12, 2000, 7, "sweep", 8], env)
+    seq, s2 = _run(exe, ["sequential", 12, 2000, 7, "sweep"], env)
+    assert len(served) == 12 and served == seq
+    assert any(int(v[1], 16) for v in served.values())
+    print("sweep: served %.2f Gcell/s, sequential %.2f Gcell/s" % (s1["gcell_per_s"], s2["gcell_per_s"]))
