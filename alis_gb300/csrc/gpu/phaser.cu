@@ -18,6 +18,7 @@
 // operands); when halving is inexact (p*Hs subnormal) the add is done in
 // double.  Optional Kahan compensation keeps a second accumulator.
 #include <cstring>
+#include <mutex>
 #include <vector>
 #include "common.cuh"
 
@@ -205,9 +206,11 @@ extern "C" int alisgpu_phaser_create(alisgpu_world *w, int nfreq, int nface, con
 // Pinned staging buffers outlive their phasers: freeing pinned memory
 // waits for the whole device, which a served loop of many worlds avoids.
 static std::vector<std::pair<float2 *, size_t>> gPinnedSpare;
+static std::mutex gPinnedLock;
 
 static float2 *pinnedTake(size_t n)
 {
+	std::lock_guard<std::mutex> lock(gPinnedLock);
 	for (size_t q = 0; q < gPinnedSpare.size(); q++)
 		if (gPinnedSpare[q].second >= n) {
 			float2 *b = gPinnedSpare[q].first;
@@ -220,6 +223,7 @@ static float2 *pinnedTake(size_t n)
 
 static void pinnedRelease(float2 *b, size_t n)
 {
+	std::lock_guard<std::mutex> lock(gPinnedLock);
 	if (b) gPinnedSpare.push_back(std::make_pair(b, n));
 }
 

@@ -19,6 +19,8 @@
 #include <cstdlib>
 #include <vector>
 #include <algorithm>
+#include <atomic>
+#include <mutex>
 #include <cooperative_groups.h>
 #include "common.cuh"
 namespace cg = cooperative_groups;
@@ -26,9 +28,12 @@ namespace cg = cooperative_groups;
 // ---------------------------------------------------------------------
 // process-wide state: device, stream groups, error text, launch counter
 // ---------------------------------------------------------------------
+// Several host threads may step different worlds at once: what a call
+// uses besides its world is per thread (the current stream group, the
+// launch-parameter staging, the error text) or atomic (the counters).
 static int gInit;
-static char gErr[512];
-static unsigned long long gLaunches;
+static thread_local char gErr[512];
+static std::atomic<unsigned long long> gLaunches;
 static unsigned int *gErrWord;
 
 extern "C" int alisgpu__fail(int code, const char *fmt, ...)
@@ -68,8 +73,9 @@ struct StreamGroup {
 };
 static StreamGroup gDefaultGroup;
 static std::vector<StreamGroup *> gOwnGroups;
+static std::mutex gGroupsLock;
 // the group of the world the current call works on (set by bindWorld)
-static StreamGroup *gGroup = &gDefaultGroup;
+static thread_local StreamGroup *gGroup = &gDefaultGroup;
 #define gStream (gGroup->main)
 #define gSide (gGroup->side)
 #define gGather (gGroup->gather)
@@ -82,7 +88,7 @@ static StreamGroup *gGroup = &gDefaultGroup;
 #define gSideUsed (gGroup->sideUsed)
 #define gSideWaitsAll (gGroup->sideWaitsAll)
 // operations that change world data, enqueued so far (launches and uploads)
-static unsigned long long gOps;
+static std::atomic<unsigned long long> gOps;
 
 static int groupCreate(StreamGroup *g)
 {
@@ -207,6 +213,7 @@ extern "C" int alisgpu_profile_read(int kind, double *ms, unsigned long long *la
 extern "C" int alisgpu_synchronize(void)
 {
 	if (!gInit) return ALISGPU_OK;
+	std::lock_guard<std::mutex> lock(gGroupsLock);
 	for (size_t q = 0; q <= gOwnGroups.size(); q++) {
 		gGroup = q < gOwnGroups.size() ? gOwnGroups[q] : &gDefaultGroup;
 		fullJoin();
@@ -250,6 +257,10 @@ struct alisgpu_world {
 	// for the one-launch form (k_ghost_chain)
 	std::vector<alisgpu_ghost_copy> ghostSeen[2];
 	bool ghostChain[2];
+	// an auxiliary world's half step waiting to run inside its parent's
+	// launch of the same field
+	struct SmallStepParams *staged[2];
+	bool stagedValid[2];
 	// the last H half step: its ghost copies, an event after its cell
 	// updates, and the operation count after its ghost launch (a phaser
 	// gather that follows directly may run beside the ghost copies)
@@ -280,6 +291,7 @@ static cudaError_t orderedCopy(void *dst, const void *src, size_t bytes, cudaMem
 }
 
 static int applyPendingGhosts(alisgpu_world *w);
+static void freeStaged(alisgpu_world *w);
 
 static Layout makeLayout(const alisgpu_geometry *g)
 {
@@ -380,12 +392,14 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) alisgpu__freeAsync(w->cls[f][a]);
 	if (w->evHCells) cudaEventDestroy(w->evHCells);
 	if (w->vbuf) alisgpu__freeAsync(w->vbuf);
+	freeStaged(w);
 	for (int b = 0; b < 2; b++)
 		if (w->vpin[b]) cudaEventSynchronize(w->vpinFree[b]), cudaFreeHost(w->vpin[b]), cudaEventDestroy(w->vpinFree[b]);
 	StreamGroup *grp = w->group;
 	delete w;
 	if (grp && --grp->users == 0) {
 		groupDestroy(grp);
+		std::lock_guard<std::mutex> lock(gGroupsLock);
 		gOwnGroups.erase(std::find(gOwnGroups.begin(), gOwnGroups.end(), grp));
 		delete grp;
 	}
@@ -412,7 +426,10 @@ extern "C" int alisgpu_world_own_streams(alisgpu_world *w)
 	ALIS_CUDA(cudaStreamWaitEvent(grp->main, done, 0));
 	if (w->group) w->group->users--;
 	grp->users = 1;
-	gOwnGroups.push_back(grp);
+	{
+		std::lock_guard<std::mutex> lock(gGroupsLock);
+		gOwnGroups.push_back(grp);
+	}
 	w->group = grp;
 	bindWorld(w);
 	return ALISGPU_OK;
@@ -433,6 +450,7 @@ extern "C" int alisgpu_world_share_streams(alisgpu_world *w, alisgpu_world *pare
 	if (w->group && --w->group->users == 0) {
 		StreamGroup *old = w->group;
 		groupDestroy(old);
+		std::lock_guard<std::mutex> lock(gGroupsLock);
 		gOwnGroups.erase(std::find(gOwnGroups.begin(), gOwnGroups.end(), old));
 		delete old;
 	}
@@ -1062,7 +1080,7 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 #define ALIS_KPT 1
 #endif
 template <int ALT>
-__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const __grid_constant__ HalfStepParams P)
+__device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int plane)
 {
 	constexpr int TY_ = STEP_TY(ALT), KW = TX * ALIS_KPT;
 	__shared__ int tileList[ALIS_TILE_OBJ];
@@ -1071,7 +1089,7 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 	const int j = P.jMIN + blockIdx.y * TY_ + threadIdx.y;
 	// E sweeps i downwards, H upwards: each starts on the planes the other
 	// touched last, which are still in L2
-	const int i = ALT == 1 ? P.iMAX - (int)blockIdx.z : P.iMIN + (int)blockIdx.z;
+	const int i = ALT == 1 ? P.iMAX - plane : P.iMIN + plane;
 	const bool manyObj = P.nobj > 8;
 	if (manyObj) {
 		// objects whose box meets this tile, in list order (one warp)
@@ -1123,6 +1141,12 @@ __global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step
 		if (((bi | bj) & CLS_TFSF) || (bi & bj & bk[q] & 0x1FFu)) hardCell<ALT>(P, i, j, kq, list, nIter);
 		else leanCells<ALT, 1>(P, i, j, kq, bi, bj, bk + q);
 	}
+}
+
+template <int ALT>
+__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const __grid_constant__ HalfStepParams P)
+{
+	halfStepBlock<ALT>(P, (int)blockIdx.z);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1356,15 +1380,16 @@ struct SmallStepParams {
 };
 
 #define SMALL_THREADS 128
+// the whole half step of a small world by the threads tid = 0..nth-1 of one block
 template <int ALT>
-__global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_constant__ SmallStepParams S)
+__device__ __noinline__ void smallStepBlock(const SmallStepParams &S, int tid, int nth)
 {
 	const Layout &L = S.P[0].L;
 	for (int m = 0; m < S.nm; m++) {
 		const HalfStepParams &P = S.P[m];
 		const int nk = P.kMAX - P.kMIN + 1, nj = P.jMAX - P.jMIN + 1, ni = P.iMAX - P.iMIN + 1;
 		const int cells = ni * nj * nk;
-		for (int t = threadIdx.x; t < cells; t += blockDim.x)
+		for (int t = tid; t < cells; t += nth)
 			stepCell<ALT>(P, P.iMIN + t / (nk * nj), P.jMIN + (t / nk) % nj, P.kMIN + t % nk, 0, P.nobj);
 	}
 	__syncthreads();
@@ -1373,7 +1398,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_const
 		const alisgpu_source_patch &p = S.src[q];
 		const int nk = 1 + p.k1 - p.k0, nj = 1 + p.j1 - p.j0, ni = 1 + p.i1 - p.i0;
 		float *F = S.F[p.m][p.comp];
-		for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
+		for (int t = tid; t < ni * nj * nk; t += nth) {
 			const int i = p.i0 + t / (nk * nj), j = p.j0 + (t / nk) % nj, k = p.k0 + t % nk;
 			if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk) {
 				atomicOr(S.P[0].err, 4u);
@@ -1388,7 +1413,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_const
 		const alisgpu_ghost_copy &g = S.ghost[q];
 		const int nk = 1 + g.k1 - g.k0, nj = 1 + g.j1 - g.j0, ni = 1 + g.i1 - g.i0;
 		const int cells = (ni > 0 && nj > 0 && nk > 0) ? ni * nj * nk : 0;
-		for (int t = threadIdx.x; t < cells; t += blockDim.x) {
+		for (int t = tid; t < cells; t += nth) {
 			const int i = g.i0 + t / (nk * nj), j = g.j0 + (t / nk) % nj, k = g.k0 + t % nk;
 			const int si = i + g.di, sj = j + g.dj, sk = k + g.dk;
 			if (i < L.i0 || i >= L.i0 + L.ni || j < L.j0 || j >= L.j0 + L.nj || k < L.k0 || k >= L.k0 + L.nk ||
@@ -1409,6 +1434,53 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_const
 		}
 		__syncthreads();
 	}
+}
+
+static void freeStaged(alisgpu_world *w)
+{
+	for (int f = 0; f < 2; f++) delete w->staged[f], w->staged[f] = 0;
+}
+
+// an auxiliary step handed over for a launch that did not take it runs on its own
+template <int ALT> __global__ void k_small_step(const __grid_constant__ SmallStepParams S);
+static int runStagedAux(const alisgpu_half_step *s, int field)
+{
+	alisgpu_world *aux = s->ntfsf == 1 ? s->tfsf[0].aux : 0;
+	if (!aux || !aux->stagedValid[field]) return ALISGPU_OK;
+	aux->stagedValid[field] = false;
+	if (field == 0) k_small_step<1><<<1, SMALL_THREADS, 0, gStream>>>(*aux->staged[field]);
+	else k_small_step<-1><<<1, SMALL_THREADS, 0, gStream>>>(*aux->staged[field]);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	return ALISGPU_OK;
+}
+
+template <int ALT>
+__global__ void __launch_bounds__(SMALL_THREADS) k_small_step(const __grid_constant__ SmallStepParams S)
+{
+	smallStepBlock<ALT>(S, threadIdx.x, blockDim.x);
+}
+
+// A large world's half step with its TFSF auxiliary column in the same
+// launch: the first plane of blocks is the column's (one block of
+// TX x TY = SMALL_THREADS threads runs it, the rest return), the planes
+// after it are the world's.  The column's step of this field reads and
+// writes only the column, and the world's step reads the column's other
+// field, so the two are independent within the launch; the launch order
+// gives the reference's order across fields.
+struct FusedStepParams {
+	HalfStepParams P;
+	SmallStepParams aux;
+};
+
+template <int ALT>
+__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step_aux(const __grid_constant__ FusedStepParams F)
+{
+	if (blockIdx.z == 0) {
+		if (blockIdx.x == 0 && blockIdx.y == 0) smallStepBlock<ALT>(F.aux, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+		return;
+	}
+	halfStepBlock<ALT>(F.P, (int)blockIdx.z - 1);
 }
 
 // ---------------------------------------------------------------------
@@ -1440,9 +1512,11 @@ static void fillTfsf(DevTfsf &T, const alisgpu_tfsf &s, int field, const float *
 // cached dt/ds face values: the TFSF box is fixed once set up
 struct TfsfCache { const alisgpu_tfsf *key; int field; DevTfsf T; };
 static std::vector<TfsfCache> gTfsfCache;
+static std::mutex gTfsfLock;
 
-static const DevTfsf &tfsfFor(alisgpu_world *w, const alisgpu_tfsf &s, int field)
+static DevTfsf tfsfFor(alisgpu_world *w, const alisgpu_tfsf &s, int field)
 {
+	std::lock_guard<std::mutex> lock(gTfsfLock);
 	for (TfsfCache &c : gTfsfCache)
 		if (c.key == &s && c.field == field && c.T.iMin == s.iMin && c.T.kMax == s.kMax && c.T.L.ni == s.aux->L.ni) return c.T;
 	TfsfCache c;
@@ -1450,11 +1524,12 @@ static const DevTfsf &tfsfFor(alisgpu_world *w, const alisgpu_tfsf &s, int field
 	const float *dtd[3] = { w->dtd[field][0], w->dtd[field][1], w->dtd[field][2] };
 	fillTfsf(c.T, s, field, dtd, w->g);
 	gTfsfCache.push_back(c);
-	return gTfsfCache.back().T;
+	return c.T;
 }
 
 extern "C" void alisgpu__forget_tfsf(const alisgpu_tfsf *s)
 {
+	std::lock_guard<std::mutex> lock(gTfsfLock);
 	for (size_t q = 0; q < gTfsfCache.size();)
 		if (gTfsfCache[q].key == s) gTfsfCache.erase(gTfsfCache.begin() + q); else q++;
 }
@@ -1492,7 +1567,7 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 		}
 		if (total >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "ghost copies of %lld cells exceed 32-bit indexing", total);
 		if (total == 0) return ALISGPU_OK;
-		static GhostLevels GL;
+		static thread_local GhostLevels GL;
 		memset(&GL, 0, sizeof GL);
 		GL.L = w->L;
 		GL.err = gErrWord;
@@ -1740,7 +1815,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	if (!side && gAuxRec[1 - field]) ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvAuxDone[1 - field], 0));
 	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
 	if (cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC && s->nghost <= ALIS_SMALL_GHOSTS) {
-		static SmallStepParams S;
+		static thread_local SmallStepParams S;
 		S.nm = 1 + g.complexField;
 		for (int m = 0; m < S.nm; m++) {
 			S.P[m] = P;
@@ -1775,11 +1850,28 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			}
 		}
 		S.vdev = 0;
+		if (s->attach && s->concurrent && !gProfOn) {
+			// runs inside the parent's next launch of this field, on the main stream
+			if (s->nvalues > ALIS_MAXSRCV) {
+				int rc = stageValues(w, s->values, s->nvalues, gStream, &S.vdev);
+				if (rc) return rc;
+			} else if (s->nvalues) {
+				memcpy(S.v, s->values, s->nvalues * sizeof(float));
+			}
+			if (!w->staged[field]) w->staged[field] = new SmallStepParams();
+			*w->staged[field] = S;
+			w->stagedValid[field] = true;
+			return ALISGPU_OK;
+		}
 		if (s->nvalues > ALIS_MAXSRCV) {
 			int rc = stageValues(w, s->values, s->nvalues, st, &S.vdev);
 			if (rc) return rc;
 		} else if (s->nvalues) {
 			memcpy(S.v, s->values, s->nvalues * sizeof(float));
+		}
+		if (!s->concurrent) {
+			int rc = runStagedAux(s, field);
+			if (rc) return rc;
 		}
 		int slot = alisgpu__prof_start();
 		if (field == 0) k_small_step<1><<<1, SMALL_THREADS, 0, st>>>(S);
@@ -1812,17 +1904,31 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		P.matTab = field == 0 ? w->matTab : 0;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
 		int slot = alisgpu__prof_start();
-		if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
+		alisgpu_world *aux = s->ntfsf == 1 && m == 0 ? s->tfsf[0].aux : 0;
+		if (aux && aux->stagedValid[field]) {
+			// with the auxiliary column's step of this field as the first plane of blocks
+			static thread_local FusedStepParams FP;
+			FP.P = P;
+			FP.aux = *aux->staged[field];
+			aux->stagedValid[field] = false;
+			dim3 gridA(grid.x, grid.y, grid.z + 1);
+			if (field == 0) k_half_step_aux<1><<<gridA, block, 0, gStream>>>(FP);
+			else k_half_step_aux<-1><<<gridA, block, 0, gStream>>>(FP);
+		} else if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
 		else k_half_step<-1><<<grid, block, 0, gStream>>>(P);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 	}
 	ALIS_CUDA(cudaGetLastError());
+	{
+		int rc = runStagedAux(s, field);
+		if (rc) return rc;
+	}
 
 	// sources
 	if (s->nsrc > 0) {
 		if (s->nsrc > ALIS_MAXSRC) return alisgpu__fail(ALISGPU_ERANGE, "half_step: %d source patches (max %d)", s->nsrc, ALIS_MAXSRC);
-		static SourceParams SP;
+		static thread_local SourceParams SP;
 		SP.n = s->nsrc;
 		SP.L = w->L;
 		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {

@@ -183,6 +183,9 @@ typedef struct alisgpu_half_step {
 	int concurrent;                             /* 1: a TFSF auxiliary world, read only by its
 	                                               parent's half steps; it may run concurrently
 	                                               with the parent's step of the same field */
+	int attach;                                 /* with concurrent: run this step inside the
+	                                               parent's next half step of the same field
+	                                               (one launch) when both forms allow it */
 } alisgpu_half_step;
 
 /* One half step of a world: conductivity, ADE subtraction, curl with

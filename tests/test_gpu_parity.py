@@ -83,3 +83,18 @@ def test_kahan_phasers_against_fp64_accumulation(scene, scale, steps):
         if k.endswith(".flux"):
             x, y = float(gpu[k].reshape(-1)[0]), float(wide[k].reshape(-1)[0])
             assert abs(x - y) <= 1e-5 * max(abs(y), 1e-30), (k, x, y)
+
+
+# every TFSF scene with its auxiliary column inside the world's launches
+# (the form large worlds and served worlds take)
+ATTACH = [c for c in scenes.CASES if (c[0], c[1]) in (("c1", 1), ("c2", 1), ("bloch", 1), ("beamtf", 1), ("unitcell", 1))]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale,steps", ATTACH, ids=["%s-x%d" % (c[0], c[1]) for c in ATTACH])
+def test_attached_auxiliary_column_bit_identical(scene, scale, steps):
+    gpu = scenes.run("engine", scene, scale, steps, env={"ALISGPU_AUX_ATTACH": "2"})
+    cpu = scenes.run("oracle", scene, scale, steps)
+    near = {k: v for k, v in gpu.items() if not k.startswith("F.")}
+    bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith("F.")})
+    assert not bad, "differs from the oracle: %s" % bad[:10]
