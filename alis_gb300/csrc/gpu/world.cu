@@ -257,6 +257,13 @@ struct alisgpu_world {
 	// for the one-launch form (k_ghost_chain)
 	std::vector<alisgpu_ghost_copy> ghostSeen[2];
 	bool ghostChain[2];
+	// the block shape of each field's half step: timed over the first
+	// ALIS_TUNE_STEPS launches, then fixed
+	struct TyTuner {
+		int choice = -1, seen = 0;
+		cudaEvent_t a[9], b[9];
+		int variant[9];
+	} tune[2];
 	// an auxiliary world's half step waiting to run inside its parent's
 	// launch of the same field
 	struct SmallStepParams *staged[2];
@@ -393,6 +400,9 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 	if (w->evHCells) cudaEventDestroy(w->evHCells);
 	if (w->vbuf) alisgpu__freeAsync(w->vbuf);
 	freeStaged(w);
+	for (int f = 0; f < 2; f++)
+		if (w->tune[f].choice < 0)
+			for (int q = 0; q < w->tune[f].seen; q++) cudaEventDestroy(w->tune[f].a[q]), cudaEventDestroy(w->tune[f].b[q]);
 	for (int b = 0; b < 2; b++)
 		if (w->vpin[b]) cudaEventSynchronize(w->vpinFree[b]), cudaFreeHost(w->vpin[b]), cudaEventDestroy(w->vpinFree[b]);
 	StreamGroup *grp = w->group;
@@ -993,18 +1003,14 @@ __device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int
 }
 
 #define TX 32
-// launch shapes, measured on the 256^3 dispersive world: 32x4 threads,
-// 16 blocks per SM (32 registers) for both fields; -D overrides for tuning
-#ifndef ALIS_E_TY
-#define ALIS_E_TY 4
-#define ALIS_E_MINB 16
-#endif
-#ifndef ALIS_H_TY
-#define ALIS_H_TY 4
-#define ALIS_H_MINB 16
-#endif
-#define STEP_TY(ALT) ((ALT) == 1 ? ALIS_E_TY : ALIS_H_TY)
-#define STEP_MINB(ALT) ((ALT) == 1 ? ALIS_E_MINB : ALIS_H_MINB)
+// Block shapes: TX x TY threads over one i plane, TY rows of 32 cells,
+// 32 registers at full occupancy (2048 threads per SM) for every TY.  The
+// tuner picks TY per world and field from these by timing its first half
+// steps (32 x 4 measured best on the 256^3 dispersive world).
+#define ALIS_TY_CHOICES 3
+static const int kTyChoice[ALIS_TY_CHOICES] = { 2, 4, 8 };
+#define ALIS_TY_DEFAULT 1
+#define STEP_MINB(TY) (2048 / (TX * (TY)))
 // The lean tiers for NC cells k, k + TX, ... of one row, all in range and
 // none of them hard: the loads of every cell first, then the updates, so
 // the cells' memory round trips overlap and share their index arithmetic.
@@ -1079,10 +1085,10 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 #ifndef ALIS_KPT
 #define ALIS_KPT 1
 #endif
-template <int ALT>
+template <int ALT, int TY_>
 __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int plane)
 {
-	constexpr int TY_ = STEP_TY(ALT), KW = TX * ALIS_KPT;
+	constexpr int KW = TX * ALIS_KPT;
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
 	const int k = P.kMIN + blockIdx.x * KW + threadIdx.x;
@@ -1143,10 +1149,10 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int plane
 	}
 }
 
-template <int ALT>
-__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step(const __grid_constant__ HalfStepParams P)
+template <int ALT, int TY>
+__global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
-	halfStepBlock<ALT>(P, (int)blockIdx.z);
+	halfStepBlock<ALT, TY>(P, (int)blockIdx.z);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1473,14 +1479,28 @@ struct FusedStepParams {
 	SmallStepParams aux;
 };
 
-template <int ALT>
-__global__ void __launch_bounds__(TX * STEP_TY(ALT), STEP_MINB(ALT)) k_half_step_aux(const __grid_constant__ FusedStepParams F)
+template <int ALT, int TY>
+__global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const __grid_constant__ FusedStepParams F)
 {
 	if (blockIdx.z == 0) {
 		if (blockIdx.x == 0 && blockIdx.y == 0) smallStepBlock<ALT>(F.aux, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
 		return;
 	}
-	halfStepBlock<ALT>(F.P, (int)blockIdx.z - 1);
+	halfStepBlock<ALT, TY>(F.P, (int)blockIdx.z - 1);
+}
+
+// one half-step launch with block height kTyChoice[v] (v a runtime choice)
+template <int ALT>
+static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
+{
+	const int ty = kTyChoice[v];
+	dim3 block(TX, ty, 1);
+	dim3 g(grid.x, grid.y, grid.z + (F ? 1 : 0));
+#define ALIS_LAUNCH(TY) do { if (F) k_half_step_aux<ALT, TY><<<g, block, 0, st>>>(*F); else k_half_step<ALT, TY><<<g, block, 0, st>>>(P); } while (0)
+	if (ty == 2) ALIS_LAUNCH(2);
+	else if (ty == 8) ALIS_LAUNCH(8);
+	else ALIS_LAUNCH(4);
+#undef ALIS_LAUNCH
 }
 
 // ---------------------------------------------------------------------
@@ -1705,6 +1725,42 @@ static int applyPendingGhosts(alisgpu_world *w)
 	return rc;
 }
 
+// The block shape of this half step: while undecided, the first 3 x 3
+// half steps of the field cycle through the shapes with events around
+// them; once every one of them has completed, the shape with the least
+// time (each shape's fastest run) stays.  ALISGPU_TUNE=0 keeps 32 x 4.
+#define ALIS_TUNE_STEPS 9
+static int tunedShape(alisgpu_world *w, int field, bool *timed)
+{
+	alisgpu_world::TyTuner &t = w->tune[field];
+	*timed = false;
+	if (t.choice >= 0) return t.choice;
+	static int enabled = -1;
+	if (enabled < 0) {
+		const char *e = getenv("ALISGPU_TUNE");
+		enabled = !(e && e[0] == '0');
+	}
+	if (!enabled) return t.choice = ALIS_TY_DEFAULT;
+	if (gProfOn) return ALIS_TY_DEFAULT;
+	if (t.seen < ALIS_TUNE_STEPS) {
+		if (cudaEventCreate(&t.a[t.seen]) != cudaSuccess || cudaEventCreate(&t.b[t.seen]) != cudaSuccess)
+			return t.choice = ALIS_TY_DEFAULT;
+		*timed = true;
+		return t.seen % ALIS_TY_CHOICES;
+	}
+	for (int q = 0; q < ALIS_TUNE_STEPS; q++) if (cudaEventQuery(t.b[q]) != cudaSuccess) return ALIS_TY_DEFAULT;
+	float best[ALIS_TY_CHOICES];
+	for (int c = 0; c < ALIS_TY_CHOICES; c++) best[c] = 1e30f;
+	for (int q = 0; q < ALIS_TUNE_STEPS; q++) {
+		float ms = 0;
+		if (cudaEventElapsedTime(&ms, t.a[q], t.b[q]) == cudaSuccess && ms < best[t.variant[q]]) best[t.variant[q]] = ms;
+		cudaEventDestroy(t.a[q]), cudaEventDestroy(t.b[q]);
+	}
+	int c = ALIS_TY_DEFAULT;
+	for (int q = 0; q < ALIS_TY_CHOICES; q++) if (best[q] < best[c]) c = q;
+	return t.choice = c;
+}
+
 // Source values of a half step into the world's device buffer on stream
 // st, through two pinned host buffers in turn: the copy is asynchronous
 // and the consuming launch on st follows it.
@@ -1889,9 +1945,11 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		return ALISGPU_OK;
 	}
 	const int ni = g.iMAX - g.iMIN + 1;
-	const int ty = STEP_TY(field == 0 ? 1 : -1);
-	dim3 block(TX, ty, 1);
+	bool timed = false;
+	const int v = tunedShape(w, field, &timed);
+	const int ty = kTyChoice[v];
 	dim3 grid((g.kMAX - g.kMIN + TX * ALIS_KPT) / (TX * ALIS_KPT), (g.jMAX - g.jMIN + ty) / ty, ni);
+	if (timed) ALIS_CUDA(cudaEventRecord(w->tune[field].a[w->tune[field].seen], gStream));
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -1911,15 +1969,19 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			FP.P = P;
 			FP.aux = *aux->staged[field];
 			aux->stagedValid[field] = false;
-			dim3 gridA(grid.x, grid.y, grid.z + 1);
-			if (field == 0) k_half_step_aux<1><<<gridA, block, 0, gStream>>>(FP);
-			else k_half_step_aux<-1><<<gridA, block, 0, gStream>>>(FP);
-		} else if (field == 0) k_half_step<1><<<grid, block, 0, gStream>>>(P);
-		else k_half_step<-1><<<grid, block, 0, gStream>>>(P);
+			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
+			else launchHalfStep<-1>(v, grid, P, &FP, gStream);
+		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream);
+		else launchHalfStep<-1>(v, grid, P, 0, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 	}
 	ALIS_CUDA(cudaGetLastError());
+	if (timed) {
+		alisgpu_world::TyTuner &t = w->tune[field];
+		ALIS_CUDA(cudaEventRecord(t.b[t.seen], gStream));
+		t.variant[t.seen++] = v;
+	}
 	{
 		int rc = runStagedAux(s, field);
 		if (rc) return rc;
