@@ -1897,11 +1897,12 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		cudaStream_t st = gStream;
 		if (side) {
 			st = gSide;
-			if (gSideWaitsAll) {
+			if (gSideWaitsAll || !gMainRec[1 - field]) {
+				// (no record of the parent's last step of the other field: wait for everything)
 				ALIS_CUDA(cudaEventRecord(gEvJoin, gStream));
 				ALIS_CUDA(cudaStreamWaitEvent(gSide, gEvJoin, 0));
 				gSideWaitsAll = 0;
-			} else if (gMainRec[1 - field]) {
+			} else {
 				ALIS_CUDA(cudaStreamWaitEvent(gSide, gEvMainDone[1 - field], 0));
 			}
 		}
@@ -1938,14 +1939,16 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		if (side) {
 			ALIS_CUDA(cudaEventRecord(gEvAuxDone[field], gSide));
 			gAuxRec[field] = 1, gSideUsed = 1;
-		} else {
+		} else if (s->ntfsf > 0) {
 			ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
 			gMainRec[field] = 1;
+		} else {
+			gMainRec[field] = 0;
 		}
 		return ALISGPU_OK;
 	}
 	const int ni = g.iMAX - g.iMIN + 1;
-	bool timed = false;
+	bool timed = false, fused = false;
 	const int v = tunedShape(w, field, &timed);
 	const int ty = kTyChoice[v];
 	dim3 grid((g.kMAX - g.kMIN + TX * ALIS_KPT) / (TX * ALIS_KPT), (g.jMAX - g.jMIN + ty) / ty, ni);
@@ -1969,6 +1972,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			FP.P = P;
 			FP.aux = *aux->staged[field];
 			aux->stagedValid[field] = false;
+			fused = true;
 			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
 			else launchHalfStep<-1>(v, grid, P, &FP, gStream);
 		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream);
@@ -2025,8 +2029,14 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		if (rc) return rc;
 		w->hOps = gOps, w->hRecorded = true;
 	}
-	ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
-	gMainRec[field] = 1;
+	// an auxiliary world stepped on the side stream waits for this record;
+	// none is needed when there is no box or its column ran in this launch
+	if (s->ntfsf > 0 && !fused) {
+		ALIS_CUDA(cudaEventRecord(gEvMainDone[field], gStream));
+		gMainRec[field] = 1;
+	} else {
+		gMainRec[field] = 0;
+	}
 	return ALISGPU_OK;
 }
 
