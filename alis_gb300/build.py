@@ -108,22 +108,30 @@ def build_engine(force=False, verbose=False, nvcc_extra=()):
     return so
 
 
-def build_oracle(force=False):
-    """Compile the CPU oracle (host setup layer + restated stepper)."""
+FP64_HEADER = os.path.join(ORACLE, "fp64.h")
+
+
+def build_oracle(force=False, fp64=False):
+    """Compile the CPU oracle (host setup layer + restated stepper).
+    fp64: the same sources with float read as double (oracle/fp64.h), the
+    FP64 run against which the error of the FP32 arithmetic is stated."""
     os.makedirs(ORACLE_BUILD, exist_ok=True)
-    od = os.path.join(ORACLE_BUILD, "obj")
+    od = os.path.join(ORACLE_BUILD, "obj64" if fp64 else "obj")
     os.makedirs(od, exist_ok=True)
     headers = [os.path.join(INC, h) for h in os.listdir(INC)] + [os.path.join(HOST, "engine.h")]
+    flags = CFLAGS + (["-include", FP64_HEADER] if fp64 else [])
+    if fp64:
+        headers.append(FP64_HEADER)
     srcs = [os.path.join(HOST, s) for s in HOST_SOURCES] + [os.path.join(ORACLE, "cpu_step.c")]
     jobs, objs = [], []
     for src in srcs:
         obj = os.path.join(od, os.path.basename(src) + ".o")
         objs.append(obj)
         if force or _newer(obj, [src] + headers):
-            jobs.append(["gcc"] + CFLAGS + ["-c", src, "-o", obj])
+            jobs.append(["gcc"] + flags + ["-c", src, "-o", obj])
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(_run, jobs))
-    ar = os.path.join(ORACLE_BUILD, "liboracle_alis.a")
+    ar = os.path.join(ORACLE_BUILD, "liboracle_alis64.a" if fp64 else "liboracle_alis.a")
     if force or _newer(ar, objs):
         if os.path.exists(ar):
             os.remove(ar)
@@ -145,8 +153,8 @@ def build_reference(force=False):
 
 def link_program(source, out, against="engine", extra=()):
     """Compile a C program written against the ALiS API and link it with
-    the engine ("engine"), the oracle ("oracle") or the reference
-    ("reference")."""
+    the engine ("engine"), the oracle ("oracle"), the oracle's FP64 build
+    ("oracle64") or the reference ("reference")."""
     cuda = _cuda_home()
     os.makedirs(os.path.dirname(out), exist_ok=True)
     base = ["gcc", "-std=gnu99", "-O2", "-fopenmp", "-ffp-contract=off", "-w", source, "-o", out]
@@ -155,6 +163,9 @@ def link_program(source, out, against="engine", extra=()):
                                                     "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-lm"]
     elif against == "oracle":
         cmd = base[:1] + ["-I" + INC] + base[1:] + [os.path.join(ORACLE_BUILD, "liboracle_alis.a"), "-lm"]
+    elif against == "oracle64":
+        cmd = base[:1] + ["-include", FP64_HEADER, "-I" + INC] + base[1:] + \
+            [os.path.join(ORACLE_BUILD, "liboracle_alis64.a"), "-lm"]
     elif against == "reference":
         ref = os.environ.get("ALIS_REFERENCE", "/root/reference")
         cmd = ["gcc", "-std=c99", "-O2", "-fopenmp", "-ffp-contract=off", "-w", "-I" + os.path.join(ref, "src"),

@@ -11,7 +11,7 @@
 // every thread sums a strided share of the face cells in double, and a
 // block reduction combines them.  The accumulators themselves are the
 // float sums of the phaser kernels.  This file is built with FMA
-// contraction on: it is an FP64 computation judged by tolerance against
+// contraction on: it is an FP64 computation checked to a tolerance against
 // an FP64 restatement, not a bit-exact replica of the FP32 reference.
 #include <cstring>
 #include <vector>

@@ -20,6 +20,15 @@
 extern "C" {
 #endif
 
+/* Single precision, always: the type of the setup quantities that the
+ * reference computes in float and that decide integers (a waveform's peak
+ * step and length).  The FP64 build of the oracle reads `float` as double
+ * but defines this type as float beforehand, so both runs make the same
+ * decisions and differ only in the rounding of their arithmetic. */
+#ifndef ALIS_FP64
+typedef float alis_f32;
+#endif
+
 /* ---- hooks the host layer calls; every backend implements them ---- */
 
 /* W (a user world or a TFSF auxiliary world) was created; host arrays exist. */

@@ -16,15 +16,19 @@
 
 /* --- waveforms (reference src/source.c:11-49) ---
  * Each initialises its parameters on the first call (S->N == 0) and sets
- * S->N, the number of steps during which the source is active. */
+ * S->N, the number of steps during which the source is active.  The
+ * parameters are computed in single precision (alis_f32), as the
+ * reference computes them; the per-step values use the stored fields. */
 
 /* CW sine with a raised-cosine turn-on over `supplement` periods */
 float Sine(world W, source S, float t, float phase)
 {
 	if (!S->N) {
-		S->frequency = 2 * PI / S->wavelength;
-		S->peaktime = W->dt * floorf(S->wavelength * S->supplement / W->dt);
-		S->deviation = S->peaktime / PI;
+		alis_f32 lam = S->wavelength, sup = S->supplement, dt = W->dt;
+		alis_f32 peak = dt * floorf(lam * sup / dt);
+		S->frequency = (alis_f32)(2 * PI / lam);
+		S->peaktime = peak;
+		S->deviation = (alis_f32)(peak / PI);
 		S->N = -1;
 	}
 	if (t < S->peaktime)
@@ -36,10 +40,13 @@ float Sine(world W, source S, float t, float phase)
 float Pulse(world W, source S, float t, float phase)
 {
 	if (!S->N) {
-		S->frequency = 2 * PI / S->wavelength;
-		S->deviation = 2 * sq(S->wavelength) / (PI * S->supplement);
-		S->peaktime = W->dt * floorf(PI * S->deviation / W->dt);
-		S->N = 2 * floorf(PI * S->deviation / W->dt);
+		alis_f32 lam = S->wavelength, sup = S->supplement, dt = W->dt;
+		alis_f32 dev = 2 * sq(lam) / (PI * sup);
+		alis_f32 steps = floorf((alis_f32)(PI * dev) / dt);
+		S->frequency = (alis_f32)(2 * PI / lam);
+		S->deviation = dev;
+		S->peaktime = (alis_f32)(dt * steps);
+		S->N = 2 * steps;
 	}
 	return sinf(S->frequency * (t-S->peaktime) - phase) * expf(-sq((t-S->peaktime) / S->deviation));
 }
@@ -49,11 +56,15 @@ float Band(world W, source S, float t, float phase)
 {
 	(void)phase;
 	if (!S->N) {
-		S->resolution = S->supplement > S->wavelength ? ceilf(1.25 * S->supplement / S->wavelength + 0.5) : 2;
-		S->frequency = 2 * PI / S->wavelength;
-		S->deviation = 2 * PI / S->wavelength / (S->resolution - 0.5);
-		S->peaktime = floorf(S->wavelength * (S->resolution - 0.5) / W->dt) * W->dt;
-		S->N = 2 * S->wavelength * (S->resolution - 0.5) / W->dt;
+		alis_f32 lam = S->wavelength, sup = S->supplement, dt = W->dt;
+		/* the `0.5` and `1.25` literals are double: those steps are
+		 * double in the reference too, rounded to float where stored */
+		alis_f32 res = sup > lam ? (alis_f32)ceilf((alis_f32)(1.25 * sup / lam + 0.5)) : 2;
+		S->resolution = res;
+		S->frequency = (alis_f32)(2 * PI / lam);
+		S->deviation = (alis_f32)((alis_f32)(2 * PI / lam) / (res - 0.5));
+		S->peaktime = (alis_f32)((alis_f32)floorf((alis_f32)(lam * (res - 0.5) / dt)) * dt);
+		S->N = 2 * lam * (res - 0.5) / dt;
 	}
 	if (t == S->peaktime) return 0;
 	return 2 * (cosf((t-S->peaktime) * S->deviation * S->resolution) - cosf((t-S->peaktime) * S->deviation)) / ((t-S->peaktime) * S->deviation);

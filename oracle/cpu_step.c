@@ -305,7 +305,7 @@ void updateH(world W)
 /* FP64 accumulation (environment ALIS_ORACLE_DFT64=1): the same float
  * fields and float phase factors, summed in double complex in shadow
  * arrays; alis_be_sync_phasers_of rounds them into the face arrays.  The
- * GPU's compensated (Kahan) accumulation is judged against it. */
+ * GPU's compensated (Kahan) accumulation is checked against it. */
 typedef struct Shadow {
 	float complex ***A;
 	int i0, j0, k0, ni, nj, nk;
@@ -388,7 +388,7 @@ void updatePhaser(world W, phaser P)
 /* --- far-field face sums (reference src/farfld.c:248-459) ---
  * REAL is float for the reference-precision restatement and double for
  * the FP64 oracle (environment ALIS_ORACLE_FF64=1), against which the
- * GPU's FP64 projection is also judged. */
+ * GPU's FP64 projection is also checked. */
 
 #define DEFINE_FF(REAL, CPLX, CEXP, CONJ, NAME) \
 static CPLX NAME##X(phaser P, cfield S, int i, tfield T, REAL kx, REAL ky) \

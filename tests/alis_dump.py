@@ -1,11 +1,11 @@
 """Reader for the binary state dumps written by tests/drivers/dump.h.
 
-Record: char name[64]; int32 kind (0 float32, 1 complex64); int32 n0, n1,
-n2; then the elements in C order.
+Record: char name[64]; int32 kind (0 float32, 1 complex64, 2 float64,
+3 complex128); int32 n0, n1, n2; then the elements in C order.
 """
 import numpy as np
 
-_DT = {0: np.float32, 1: np.complex64}
+_DT = {0: np.float32, 1: np.complex64, 2: np.float64, 3: np.complex128}
 
 
 def read_dump(path):

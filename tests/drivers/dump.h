@@ -2,9 +2,10 @@
  * dump.h -- binary dump of ALiS state for the parity tests.
  *
  * Record format (little endian): char name[64]; int32 kind (0 float32,
- * 1 complex64); int32 n0, n1, n2; then n0*n1*n2 elements.  The same
- * driver source is compiled against the reference library, the oracle
- * and the GPU engine; tests/alis_dump.py reads the files.
+ * 1 complex64, 2 float64, 3 complex128); int32 n0, n1, n2; then n0*n1*n2
+ * elements.  The same driver source is compiled against the reference
+ * library, the oracle, the oracle's FP64 build (float read as double:
+ * kinds 2 and 3) and the GPU engine; tests/alis_dump.py reads the files.
  */
 #ifndef DUMP_H
 #define DUMP_H
@@ -16,6 +17,9 @@
 extern void alisSyncHost(world W) __attribute__((weak));
 
 static FILE *dumpFile;
+
+#define DUMP_REAL (sizeof(float) == 8 ? 2 : 0)
+#define DUMP_COMPLEX (sizeof(float) == 8 ? 3 : 1)
 
 static void dumpOpen(const char *path)
 {
@@ -36,7 +40,7 @@ static void dumpHeader(const char *name, int kind, int n0, int n1, int n2)
 static void dumpField(const char *name, float ***f, int i0, int i1, int j0, int j1, int k0, int k1)
 {
 	if (!f) return;
-	dumpHeader(name, 0, 1+i1-i0, 1+j1-j0, 1+k1-k0);
+	dumpHeader(name, DUMP_REAL, 1+i1-i0, 1+j1-j0, 1+k1-k0);
 	for (int i = i0; i <= i1; i++) for (int j = j0; j <= j1; j++)
 		fwrite(&f[i][j][k0], sizeof(float), 1+k1-k0, dumpFile);
 }
@@ -44,20 +48,20 @@ static void dumpField(const char *name, float ***f, int i0, int i1, int j0, int 
 static void dumpCField(const char *name, float complex ***f, int i0, int i1, int j0, int j1, int k0, int k1)
 {
 	if (!f) return;
-	dumpHeader(name, 1, 1+i1-i0, 1+j1-j0, 1+k1-k0);
+	dumpHeader(name, DUMP_COMPLEX, 1+i1-i0, 1+j1-j0, 1+k1-k0);
 	for (int i = i0; i <= i1; i++) for (int j = j0; j <= j1; j++)
 		fwrite(&f[i][j][k0], sizeof(float complex), 1+k1-k0, dumpFile);
 }
 
 static void dumpScalar(const char *name, float v)
 {
-	dumpHeader(name, 0, 1, 1, 1);
+	dumpHeader(name, DUMP_REAL, 1, 1, 1);
 	fwrite(&v, sizeof v, 1, dumpFile);
 }
 
 static void dumpCScalar(const char *name, float complex v)
 {
-	dumpHeader(name, 1, 1, 1, 1);
+	dumpHeader(name, DUMP_COMPLEX, 1, 1, 1);
 	fwrite(&v, sizeof v, 1, dumpFile);
 }
 

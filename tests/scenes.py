@@ -56,12 +56,17 @@ def binary(against):
         build.build_engine()
     elif against == "oracle":
         build.build_oracle()
+    elif against == "oracle64":
+        build.build_oracle(fp64=True)
     elif against == "reference":
         if build.build_reference() is None:
             return None
     deps = [DRIVER, os.path.join(ROOT, "tests", "drivers", "dump.h")]
+    if against == "oracle64":
+        deps.append(build.FP64_HEADER)
     lib = {"engine": os.path.join(build.LIB, "libalis_gb300.so"),
            "oracle": os.path.join(build.ORACLE_BUILD, "liboracle_alis.a"),
+           "oracle64": os.path.join(build.ORACLE_BUILD, "liboracle_alis64.a"),
            "reference": os.path.join(build.ORACLE, "_ref", "libalis_ref.a")}[against]
     if os.path.exists(lib):
         deps.append(lib)
