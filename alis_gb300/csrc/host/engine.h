@@ -22,7 +22,7 @@ extern "C" {
 
 /* Single precision, always: the type of the setup quantities that the
  * reference computes in float and that decide integers (a waveform's peak
- * step and length).  The FP64 build of the oracle reads `float` as double
+ * step and length, the phaser frequency grid).  The FP64 build of the oracle reads `float` as double
  * but defines this type as float beforehand, so both runs make the same
  * decisions and differ only in the rounding of their arithmetic. */
 #ifndef ALIS_FP64

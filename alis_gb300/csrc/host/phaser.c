@@ -68,16 +68,19 @@ static void setupPhaser(world W, phaser P, phaser p, source S, float xMin, float
 
 /* Frequencies f_n = (nMax-n)/(dL nMin nMax), n = 0..nMax-nMin: uniform in
  * frequency between 1/LMax and 1/LMin, in decreasing order, closed by an
- * f = 0 sentinel (reference src/phaser.c:21-66). */
+ * f = 0 sentinel (reference src/phaser.c:21-66).  The grid (its counts,
+ * accumulation length and frequencies) is computed in single precision
+ * (alis_f32), as the reference computes it. */
 phaser (createPhasers)(world W, float LMin, float LMax, float dL, float xMin, float xMax, float yMin, float yMax, float zMin, float zMax, ...)
 {
-	int nMin = floor(LMin/dL), nMax = ceil(LMax/dL);
+	alis_f32 lo = LMin, hi = LMax, step = dL, dt = W->dt;
+	int nMin = floor(lo/step), nMax = ceil(hi/step);
 	phaser P;
 	source S = alis_reference_source(W);
 	MALLOC(P, 0, 2-nMin+nMax);
 	for (int n = 0; n <= nMax-nMin; n++) {
-		P[n].N = nMin * nMax * dL / W->dt;
-		P[n].f = (nMax-n) / (dL * nMin * nMax);
+		P[n].N = nMin * nMax * step / dt;
+		P[n].f = (alis_f32)((nMax-n) / (step * nMin * nMax));
 		setupPhaser(W, P, P+n, S, xMin, xMax, yMin, yMax, zMin, zMax);
 	}
 	alis_be_phaser_created(P);
@@ -97,11 +100,11 @@ phaser createPhasersList(world W, int count, const float *wavelengths, float xMi
 	phaser P;
 	source S = alis_reference_source(W);
 	MALLOC(P, 0, count+1);
-	float Lmax = 0;
-	for (int n = 0; n < count; n++) Lmax = MAX(Lmax, wavelengths[n]);
+	alis_f32 Lmax = 0, dt = W->dt;
+	for (int n = 0; n < count; n++) Lmax = MAX(Lmax, (alis_f32)wavelengths[n]);
 	for (int n = 0; n < count; n++) {
-		P[n].N = Lmax / W->dt;
-		P[n].f = 1 / wavelengths[n];
+		P[n].N = Lmax / dt;
+		P[n].f = (alis_f32)(1 / (alis_f32)wavelengths[n]);
 		setupPhaser(W, P, P+n, S, xMin, xMax, yMin, yMax, zMin, zMax);
 	}
 	alis_be_phaser_created(P);

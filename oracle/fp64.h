@@ -12,12 +12,14 @@
  * recursions are the reference's formulas (src/update.c, src/world.c,
  * src/object.c, src/source.c, src/phaser.c, src/farfld.c), evaluated in
  * FP64.  Float literals (`0.5f`, the `PI` constant) keep their float
- * values, and the waveform parameters that decide integers (peak step,
- * active length) stay single precision through `alis_f32`, so both runs
- * solve the same discrete problem and differ only in the rounding of
- * their arithmetic.  (A Pulse of 600 nm and supplement 150 at dt = 5 puts
- * pi*deviation/dt at 959.9999 in float and 960.0 in double: without the
- * shared type its peak would move by one step.)
+ * values, and the setup quantities that decide integers (a waveform's
+ * peak step and length, the phaser frequency grid) stay single precision
+ * through `alis_f32`, so both runs solve the same discrete problem and
+ * differ only in the rounding of their arithmetic.  (A Pulse of 600 nm
+ * and supplement 150 at dt = 5 puts pi*deviation/dt at 959.9999 in float
+ * and 960.0 in double, which would move its peak by one step; phasers
+ * over 400-800 nm in steps of 400/63 number 64 in float and 65 in
+ * double.)
  *
  * The system headers come first, so that their own float declarations
  * keep their types; everything included after this file sees the macros.

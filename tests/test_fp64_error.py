@@ -149,3 +149,50 @@ def test_engine_error_against_fp64(builds, case):
         for cat, bound in BOUND.items():
             if cat in e:
                 assert e[cat][0] <= bound, (env, cat, e[cat])
+
+
+GOLD_C2 = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "c2_spectrum.json")
+
+
+def _band_error(flux, ref, floor):
+    """Largest relative flux error of `flux` against spectrum `ref` over the
+    frequencies where the source carries at least `floor` of its peak
+    spectral amplitude."""
+    weight = [1 / abs(a) for a in ref["A"]]
+    band = [i for i, w in enumerate(weight) if w >= floor * max(weight)]
+    return max(abs(flux[i] - ref["flux"][i]) / abs(ref["flux"][i]) for i in band)
+
+
+@pytest.mark.gpu
+def test_engine_benchmark_spectrum_against_fp64():
+    """The benchmark world at its full size (256^3 cells, 64 frequencies,
+    4000 steps) on the engine, against the spectra of the FP32 oracle and
+    of the FP64 build in tests/golden/c2_spectrum.json (made by
+    make_c2_spectrum.py on another host).  Plain phasers reproduce the
+    float reference within 1e-5 wherever the source carries 1e-2 of its
+    peak; against FP64 both modes stay within 1e-3 over the band of 1e-3
+    (the float reference itself is 3e-4 from FP64 there)."""
+    import json
+    import subprocess
+    import tempfile
+    from alis_gb300 import build
+    gold = json.load(open(GOLD_C2))
+    build.build_engine()
+    exe = build.link_program(os.path.join(os.path.dirname(scenes.DRIVER), "c2_spectrum.c"),
+                             os.path.join(scenes.BIN, "c2_spectrum_engine"), "engine")
+    ref32 = _band_error(gold["oracle"]["flux"], gold["oracle64"], IN_BAND)
+    for kahan in ("0", "1"):
+        env = dict(os.environ, ALISGPU_PHASER_KAHAN=kahan)
+        with tempfile.TemporaryDirectory() as d:
+            r = subprocess.run([exe, "230", str(gold["steps"])], cwd=d, env=env, capture_output=True,
+                               text=True, timeout=900)
+        assert r.returncode == 0, r.stderr[-2000:]
+        s = json.loads(r.stdout.strip().splitlines()[-1])
+        assert s["cells"] == gold["cells"] and s["f"] == gold["oracle"]["f"]
+        e64 = _band_error(s["flux"], gold["oracle64"], IN_BAND)
+        e32 = _band_error(s["flux"], gold["oracle"], 1e-2)
+        print("kahan=%s: flux error vs FP64 %.3e (float reference %.3e), vs FP32 reference %.3e"
+              % (kahan, e64, ref32, e32))
+        assert e64 <= 1e-3
+        if kahan == "0":
+            assert e32 <= 1e-5
