@@ -46,7 +46,7 @@ struct DevObj {
 	int i0, i1, j0, j1, k0, k1;          // box of maps and currents
 	int NJ, NK;
 	float a[3];
-	int cond;                             // any conductivity factor non-zero
+	int cond;                             // 0: no conductivity; 1: the reference's factor; 2: its compensated form
 	float JJ[ALIS_MAXPOLES][3], JK[ALIS_MAXPOLES][3], JE[ALIS_MAXPOLES][3];
 	float KJ[ALIS_MAXPOLES][3], KK[ALIS_MAXPOLES][3], KE[ALIS_MAXPOLES][3];
 	float *fill[3];                       // compact over the box

@@ -66,15 +66,36 @@ static void psiZ(vfield F, vfield G, coeffs *C, float ***Px, float ***Py, int Al
 /* --- curl half step with conduction, ADE currents and CPML
  * (reference src/update.c:87-125); Alt = +1 for E, -1 for H --- */
 
+/* Conduction factor q = (1 - a u) / (1 + a u) of a cell with fill u.
+ * The reference multiplies F by q, rounded to float, at every step: that
+ * rounding is the same each step, so over n steps the field of a
+ * conducting object drifts by n times it (2.85e-4 of the flux after 4000
+ * steps of the benchmark's gold block).  With
+ * ALIS_ORACLE_PRECISE_CONDUCTION=1 (the engine's
+ * ALISGPU_PRECISE_CONDUCTION=1) F loses F b instead, b = 2 a u / (1 + a u)
+ * = 1 - q: b's rounding moves the applied factor by b times as much.  Not
+ * the reference's arithmetic: an opt-in precision mode. */
+static int preciseConduction = -1;
+
 static void curlStep(world W, vfield F, vfield G, coeffs *C, int Alt)
 {
 	int i0 = W->iMIN, i1 = W->iMAX, j0 = W->jMIN, j1 = W->jMAX, k0 = W->kMIN, k1 = W->kMAX;
+	if (preciseConduction < 0) {
+		const char *e = getenv("ALIS_ORACLE_PRECISE_CONDUCTION");
+		preciseConduction = e && e[0] == '1';
+	}
 	for (int n = 0; n < C->N; n++) {
 		int a0 = MAX(i0, C->iMin[n]), a1 = MIN(i1, C->iMax[n]);
 		int b0 = MAX(j0, C->jMin[n]), b1 = MIN(j1, C->jMax[n]);
 		int c0 = MAX(k0, C->kMin[n]), c1 = MIN(k1, C->kMax[n]);
 		if (!(C->ax[n] || C->ay[n] || C->az[n])) continue;
-		LOOP3(i,a0,a1,j,b0,b1,k,c0,c1) {
+		if (preciseConduction) LOOP3(i,a0,a1,j,b0,b1,k,c0,c1) {
+			float px = C->ax[n] * C->Jx[n][i][j][k], py = C->ay[n] * C->Jy[n][i][j][k], pz = C->az[n] * C->Jz[n][i][j][k];
+			F.x[i][j][k] -= F.x[i][j][k] * (2 * px / (1 + px));
+			F.y[i][j][k] -= F.y[i][j][k] * (2 * py / (1 + py));
+			F.z[i][j][k] -= F.z[i][j][k] * (2 * pz / (1 + pz));
+		}
+		else LOOP3(i,a0,a1,j,b0,b1,k,c0,c1) {
 			F.x[i][j][k] *= (1 - C->ax[n] * C->Jx[n][i][j][k]) / (1 + C->ax[n] * C->Jx[n][i][j][k]);
 			F.y[i][j][k] *= (1 - C->ay[n] * C->Jy[n][i][j][k]) / (1 + C->ay[n] * C->Jy[n][i][j][k]);
 			F.z[i][j][k] *= (1 - C->az[n] * C->Jz[n][i][j][k]) / (1 + C->az[n] * C->Jz[n][i][j][k]);
