@@ -259,15 +259,53 @@ static void tfsfH(world W, tfsf S)
 
 #define GHOST(W, F, c, ...) (copyBoundary)(W->F[0].c, W->complexField ? W->F[1].c : 0, __VA_ARGS__)
 
+/* FP16 field storage, a study of the storage form (environment
+ * ALIS_ORACLE_FP16_STORAGE=1; not built in the engine): after each half
+ * step of a user world, every component of the updated field is stored
+ * as IEEE half with one power-of-two scale per x plane (the plane's
+ * largest magnitude maps into [0.5, 1)) and read back.  TFSF auxiliary
+ * columns, ADE currents and CPML psi stay float. */
+static int fp16Storage = -1, stepDepth;
+
+static void storeHalf(world W, vfield F)
+{
+	float ***c[3] = { F.x, F.y, F.z };
+	for (int q = 0; q < 3; q++) {
+		_Pragma("omp parallel for")
+		for (int i = W->iMIN; i <= W->iMAX; i++) {
+			double m = 0;
+			for (int j = W->jMIN; j <= W->jMAX; j++) for (int k = W->kMIN; k <= W->kMAX; k++)
+				if (fabs(c[q][i][j][k]) > m) m = fabs(c[q][i][j][k]);
+			if (m == 0) continue;
+			int e;
+			frexp(m, &e);
+			for (int j = W->jMIN; j <= W->jMAX; j++) for (int k = W->kMIN; k <= W->kMAX; k++)
+				c[q][i][j][k] = ldexp((double)(_Float16)ldexp(c[q][i][j][k], -e), e);
+		}
+	}
+}
+
+static void storeFields(world W, vfield *F)
+{
+	if (fp16Storage < 0) {
+		const char *e = getenv("ALIS_ORACLE_FP16_STORAGE");
+		fp16Storage = e && e[0] == '1';
+	}
+	if (fp16Storage && stepDepth == 1)
+		for (int m = 0; m <= W->complexField; m++) storeHalf(W, F[m]);
+}
+
 /* reference src/update.c:275-299 */
 void updateE(world W)
 {
+	stepDepth++;
 	for (int m = 0; m <= W->complexField; m++) {
 		curlStep(W, W->E[m], W->H[m], W->CE, 1);
 		currentStep(W, W->H[m], W->CH);
 	}
 	if (W->S) tfsfE(W, W->S);
 	if (W->SE) sourceStep(W, W->SE, W->H->t);
+	storeFields(W, W->E);
 	int iAlt = (W->xMinSur==PBC || W->xMinSur==BBC ? W->iNUM-1 : 1);
 	int jAlt = (W->yMinSur==PBC || W->yMinSur==BBC ? W->jNUM-1 : 1);
 	int kAlt = (W->zMinSur==PBC || W->zMinSur==BBC ? W->kNUM-1 : 1);
@@ -280,17 +318,20 @@ void updateE(world W)
 		GHOST(W, E, y, W->cosky, -W->sinky, W->iMIN, W->iMAX, W->jMAX+1, W->jMAX+1, W->kMIN, W->kMAX, 0, -jAlt, 0);
 	}
 	W->t = W->E->t = ++W->n * W->dt;
+	stepDepth--;
 }
 
 /* reference src/update.c:302-341 */
 void updateH(world W)
 {
+	stepDepth++;
 	for (int m = 0; m <= W->complexField; m++) {
 		curlStep(W, W->H[m], W->E[m], W->CH, -1);
 		currentStep(W, W->E[m], W->CE);
 	}
 	if (W->S) tfsfH(W, W->S);
 	if (W->SH) sourceStep(W, W->SH, W->E->t);
+	storeFields(W, W->H);
 	int iAlt = (W->xMinSur==PBC || W->xMinSur==BBC ? W->iNUM-1 : 1);
 	int jAlt = (W->yMinSur==PBC || W->yMinSur==BBC ? W->jNUM-1 : 1);
 	int kAlt = (W->zMinSur==PBC || W->zMinSur==BBC ? W->kNUM-1 : 1);
@@ -318,6 +359,7 @@ void updateH(world W)
 		GHOST(W, H, x, W->cosky, W->sinky, W->iMIN, W->iMAX+1, W->jMIN, W->jMIN, W->kMIN, W->kMAX+1, 0, jAlt, 0);
 	}
 	W->t = W->H->t = W->E->t + 0.5 * W->dt;
+	stepDepth--;
 }
 
 

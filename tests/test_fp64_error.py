@@ -246,3 +246,18 @@ def test_precise_conduction_acts_where_an_object_conducts(builds):
     assert not np.array_equal(ref["W.E0.x"], pre["W.E0.x"])
     ref, pre = scenes.run("oracle", "spheres", 1, 80), scenes.run("oracle", "spheres", 1, 80, env=PRECISE)
     assert not scenes.compare_exact(ref, pre)
+
+
+def test_fp16_storage_study(builds):
+    """FP16 field storage with one power-of-two scale per x plane
+    (ALIS_ORACLE_FP16_STORAGE=1; emulated in the oracle, not built in the
+    engine) against the FP64 run: the half's 11-bit mantissa, rounded at
+    every store, puts the sweep's unit cell 7.8e-4 from FP64 in band and
+    its fields 2.7e-2, against 1.8e-5 and 3.8e-6 for FP32 storage -- above
+    the 1e-4 spectral bound, which is why the engine stores FP32."""
+    b = scenes.run("oracle64", "unitcell", 1, 1500)
+    e32 = errors(scenes.run("oracle", "unitcell", 1, 1500), b)
+    e16 = errors(scenes.run("oracle", "unitcell", 1, 1500, env={"ALIS_ORACLE_FP16_STORAGE": "1"}), b)
+    print("unit cell, flux in band: FP32 storage %.2e, FP16 storage %.2e" % (e32["flux"][0], e16["flux"][0]))
+    assert e32["flux"][0] <= BOUND["flux"] < e16["flux"][0] < 1e-2
+    assert 1e-3 < e16["field"][0] < 1e-1
