@@ -14,9 +14,10 @@ a phaser face error is taken over all faces and components of one
 frequency; the far field over all samples of a scene.  A flux spectrum
 error is taken per frequency, over the band where the source carries at
 least 1e-3 of its peak spectral amplitude (1/A, src/phaser.c:38-45).
-Below that, the reference's float normalisation sum itself loses digits
-(up to 1e-1 at 1e-6 of the peak), which no change to the update can
-mend; those frequencies are reported, not bounded.
+Below that, the float rounding of the source's waveform values is as
+large as the waveform's spectrum itself (up to 1e-1 flux error at 1e-6 of
+the peak), which no change to the update can mend; those frequencies are
+reported, not bounded.
 """
 import os
 import sys
