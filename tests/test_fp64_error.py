@@ -118,9 +118,11 @@ def test_fp32_error_against_fp64(builds, case):
     for cat, bound in BOUND.items():
         if cat in e:
             assert e[cat][0] <= bound, (cat, e[cat])
-    # the discrete problem is the same: maps of filling fractions agree
+    # the discrete problem is the same: maps of filling fractions agree, and
+    # the phaser frequencies (computed in single precision by both builds)
+    # are the same numbers
     for k in a:
-        if ".fill" in k:
+        if ".fill" in k or (k.startswith("P.") and k.endswith(".f")):
             assert np.array_equal(a[k].astype(np.float64), b[k]), k
 
 
