@@ -33,6 +33,8 @@
  *           dispersive matter; 4^3 supersampling (shapespt: point
  *           samples, shapesedge: the edge rule)
  *   contour a height-map object, filled by the host loops
+ *   pec     a PEC mirror under silver and a lossy (nk) film, symmetry
+ *           planes and periodic walls, a single-wavelength phaser
  */
 #include <alis.h>
 #include "dump.h"
@@ -534,6 +536,29 @@ static void sceneContour(int steps)
 	dumpPhasers(P, "P");
 }
 
+/* a PEC mirror: z-min PEC under a silver layer and a lossy film (nk: a
+ * static conductivity and no poles), periodic x and y with symmetry
+ * planes at their lower ends, a dipole on both symmetry planes, a
+ * single-wavelength phaser plane */
+static void scenePEC(int steps)
+{
+	float a = 60 * scale;
+	dom D = {{a}, {a}, {-60, 240}};
+	res R = {5, {10}, {1240}};
+	sur S = {{SYM, PBC}, {SYM, PBC}, {PEC, PML}, {8}};
+	world W = createWorld(D, R, S, "");
+	matter Lossy = nk(2.2, 0.12, 1240/550);
+	object Film = {Box, {{-INF, INF}, {-INF, INF}, {20, 60}}};
+	object Mirror = {Box, {{-INF, INF}, {-INF, INF}, {-INF, 0}}};
+	putObjects(W, Lossy, Film, Ag, Mirror, Air);
+	pointDipole(W, Ex, 0, 0, 100, Pulse, 550, 60);
+	phaser P = createPhaser(W, 550, -INF, INF, -INF, INF, 200, 200);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Film));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -562,6 +587,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "shapespt")) sceneShapes(steps, 1);
 	else if (!strcmp(s, "shapesedge")) sceneShapes(steps, -1);
 	else if (!strcmp(s, "contour")) sceneContour(steps);
+	else if (!strcmp(s, "pec")) scenePEC(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

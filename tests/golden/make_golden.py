@@ -23,7 +23,7 @@ import scenes  # noqa: E402
 
 def main():
     out = {}
-    for scene, scale, steps in scenes.CASES:
+    for scene, scale, steps in scenes.PIN_CASES:
         d = scenes.run("reference", scene, scale, steps)
         if d is None:
             sys.exit("reference sources not available")

@@ -41,6 +41,7 @@ CASES = [
     ("nug", 1, 300),
     ("bowtie", 1, 300),
     ("beamtf", 1, 80),
+    ("pec", 1, 600),
 ]
 
 BOUND = {"field": 5e-5, "ade": 5e-5, "face": 5e-5, "far": 1e-5, "flux": 1e-4}

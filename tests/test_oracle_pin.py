@@ -38,7 +38,7 @@ def check_against_golden(dump, gold):
     return inexact
 
 
-@pytest.mark.parametrize("scene,scale,steps", scenes.CASES, ids=scenes.IDS)
+@pytest.mark.parametrize("scene,scale,steps", scenes.PIN_CASES, ids=scenes.PIN_IDS)
 def test_oracle_matches_reference(scene, scale, steps):
     dump = scenes.run("oracle", scene, scale, steps)
     inexact = check_against_golden(dump, GOLDEN["%s/%d/%d" % (scene, scale, steps)])
