@@ -35,6 +35,8 @@
  *   contour a height-map object, filled by the host loops
  *   pec     a PEC mirror under silver and a lossy (nk) film, symmetry
  *           planes and periodic walls, a single-wavelength phaser
+ *   aniso   an anisotropic Drude-Lorentz ball, box phasers, far-field
+ *           intensities and ring fluxes
  */
 #include <alis.h>
 #include "dump.h"
@@ -559,6 +561,35 @@ static void scenePEC(int steps)
 	dumpPhasers(P, "P");
 }
 
+/* an anisotropic dispersive ball (per-axis eps, one Drude and one Lorentz
+ * pole per axis) lit by a dipole in a CPML box; box phasers and the
+ * far-field aggregates: intensities per polarisation and ring fluxes */
+static void sceneAniso(int steps)
+{
+	float L = 100 * scale;
+	dom D = {{L}, {L}, {L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PML}};
+	world W = createWorld(D, R, S, "");
+	matter Aniso = {{2.0, 2.5, 3.0}, {{8.0, 0.1}, {7.5, 0.12}, {7.0, 0.15}, {3.0, 0.3, 1.5}, {3.2, 0.3, 1.2}, {3.4, 0.3, 1.0}}};
+	object Egg = {Ball, {{-40, 30}, {-30, 30}, {-20, 40}}};
+	putObjects(W, Aniso, Egg, Air);
+	pointDipole(W, Ey, 10, -50, 0, Pulse, 500, 120);
+	phaser P = createPhasers(W, 450, 750, 150, -L+20, L-20, -L+20, L-20, -L+20, L-20);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, Egg));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+	char nm[64];
+	float th[4] = { 0, 35, 90, 140 }, ph[4] = { 0, 60, 20, 250 };
+	tfield (*pol[3])(phaser, float, float) = { Ppol, Spol, Unpol };
+	for (int a = 0; a < 4; a++) for (int q = 0; q < 3; q++) {
+		snprintf(nm, 64, "FA.I.%d.%d", a, q); dumpScalar(nm, farFieldI(P + 1, pol[q], th[a], ph[a]));
+	}
+	dumpScalar("FA.flux.0", farFieldFlux(P + 1, Unpol, 0, 0, 30));
+	dumpScalar("FA.flux.1", farFieldFlux(P + 1, Ppol, 180, 0, 10, 40, 5));
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -588,6 +619,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "shapesedge")) sceneShapes(steps, -1);
 	else if (!strcmp(s, "contour")) sceneContour(steps);
 	else if (!strcmp(s, "pec")) scenePEC(steps);
+	else if (!strcmp(s, "aniso")) sceneAniso(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

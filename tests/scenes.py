@@ -50,8 +50,10 @@ IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
 # pinned against the reference on the CPU only (tests/test_oracle_pin.py);
 # not yet part of the GPU parity run: a PEC mirror under silver and a
-# lossy (nk) film, symmetry planes, a single-wavelength phaser
-PIN_CASES = CASES + [("pec", 1, 120)]
+# lossy (nk) film, symmetry planes, a single-wavelength phaser; an
+# anisotropic Drude-Lorentz ball with the far-field intensities and ring
+# fluxes
+PIN_CASES = CASES + [("pec", 1, 120), ("aniso", 1, 120)]
 PIN_IDS = ["%s-x%d" % (c[0], c[1]) for c in PIN_CASES]
 
 

@@ -42,6 +42,7 @@ CASES = [
     ("bowtie", 1, 300),
     ("beamtf", 1, 80),
     ("pec", 1, 600),
+    ("aniso", 1, 400),
 ]
 
 BOUND = {"field": 5e-5, "ade": 5e-5, "face": 5e-5, "far": 1e-5, "flux": 1e-4}
