@@ -37,6 +37,9 @@
  *           planes and periodic walls, a single-wavelength phaser
  *   aniso   an anisotropic Drude-Lorentz ball, box phasers, far-field
  *           intensities and ring fluxes
+ *   lattice a dipole array (symmetry planes and periodic walls) with a
+ *           phaser box over three periods: replicated phasers and the
+ *           far field's lattice factor
  */
 #include <alis.h>
 #include "dump.h"
@@ -590,6 +593,31 @@ static void sceneAniso(int steps)
 	dumpScalar("FA.flux.1", farFieldFlux(P + 1, Ppol, 180, 0, 10, 40, 5));
 }
 
+/* a dipole array: one cell with symmetry planes at its lower ends and
+ * periodic upper walls, a dielectric post; the phaser box spans three
+ * periods each way, so the phasers replicate over the lattice and the far
+ * field carries the lattice factor */
+static void sceneLattice(int steps)
+{
+	float a = 40 * scale;
+	dom D = {{a}, {a}, {150}};
+	res R = {5, {10}, {1240}};
+	sur S = {{SYM, PBC}, {SYM, PBC}, {PML}};
+	world W = createWorld(D, R, S, "");
+	object Post = {Box, {{-20, 20}, {-20, 20}, {-60, -20}}};
+	putObjects(W, n(2.0), Post, Air);
+	pointDipole(W, Ex, 0, 0, 20, Pulse, 550, 100);
+	phaser P = createPhasers(W, 450, 700, 125, -3*a, 3*a, -3*a, 3*a, -100, 100);
+	run(W, P, steps);
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+	char nm[64];
+	for (int q = 0; P[q].f; q++) {
+		snprintf(nm, 64, "FL.%d.num", q); dumpScalar(nm, P[q].xNUM * 1000 + P[q].yNUM);
+	}
+	farSamples(P + 1, "FL");
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -620,6 +648,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "contour")) sceneContour(steps);
 	else if (!strcmp(s, "pec")) scenePEC(steps);
 	else if (!strcmp(s, "aniso")) sceneAniso(steps);
+	else if (!strcmp(s, "lattice")) sceneLattice(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

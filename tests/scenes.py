@@ -52,8 +52,9 @@ IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 # not yet part of the GPU parity run: a PEC mirror under silver and a
 # lossy (nk) film, symmetry planes, a single-wavelength phaser; an
 # anisotropic Drude-Lorentz ball with the far-field intensities and ring
-# fluxes
-PIN_CASES = CASES + [("pec", 1, 120), ("aniso", 1, 120)]
+# fluxes; a dipole array whose phasers replicate over three periods, with
+# the far field's lattice factor
+PIN_CASES = CASES + [("pec", 1, 120), ("aniso", 1, 120), ("lattice", 1, 120)]
 PIN_IDS = ["%s-x%d" % (c[0], c[1]) for c in PIN_CASES]
 
 
