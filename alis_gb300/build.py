@@ -139,11 +139,20 @@ def build_oracle(force=False, fp64=False):
     return ar
 
 
+def reference_root():
+    """The reference checkout as oracle/build_ref.sh locates it (its
+    argument-free form: $ALIS_REFERENCE or the build container's
+    checkout), or None where there is none (the GPU machine)."""
+    r = subprocess.run(["sh", os.path.join(ORACLE, "build_ref.sh"), "--locate"], capture_output=True, text=True)
+    path = r.stdout.strip()
+    return path if r.returncode == 0 and os.path.isdir(os.path.join(path, "src")) else None
+
+
 def build_reference(force=False):
     """Build the reference library from its own sources (only where the
     reference checkout exists; used to pin the oracle)."""
-    ref = os.environ.get("ALIS_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src")):
+    ref = reference_root()
+    if ref is None:
         return None
     lib = os.path.join(ORACLE, "_ref", "libalis_ref.a")
     if force or not os.path.exists(lib):
@@ -167,7 +176,9 @@ def link_program(source, out, against="engine", extra=()):
         cmd = base[:1] + ["-include", FP64_HEADER, "-I" + INC] + base[1:] + \
             [os.path.join(ORACLE_BUILD, "liboracle_alis64.a"), "-lm"]
     elif against == "reference":
-        ref = os.environ.get("ALIS_REFERENCE", "/root/reference")
+        ref = reference_root()
+        if ref is None:
+            raise RuntimeError("no reference checkout (oracle/build_ref.sh --locate)")
         cmd = ["gcc", "-std=c99", "-O2", "-fopenmp", "-ffp-contract=off", "-w", "-I" + os.path.join(ref, "src"),
                source, "-o", out, os.path.join(ORACLE, "_ref", "libalis_ref.a"), "-lm"]
     else:

@@ -109,9 +109,12 @@ extern "C" int alisgpu__check(cudaError_t e, const char *what);
 // Device memory of worlds, phasers and their scratch comes from the
 // stream-ordered pool on the main stream of the world's group: freeing a
 // world that finished does not wait for the work of every other world.
+// An injected allocation failure (alisgpu_inject_alloc_failures) is taken here.
+extern "C" int alisgpu__alloc_denied(void);
 template <class T>
 static inline cudaError_t alisgpu__mallocAsync(T **p, size_t bytes)
 {
+	if (alisgpu__alloc_denied()) { *p = 0; return cudaErrorMemoryAllocation; }
 	return cudaMallocAsync((void **)p, bytes, alisgpu__stream());
 }
 static inline cudaError_t alisgpu__freeAsync(void *p)

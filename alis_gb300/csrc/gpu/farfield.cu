@@ -14,11 +14,13 @@
 // contraction on: it is an FP64 computation checked to a tolerance against
 // an FP64 restatement, not a bit-exact replica of the FP32 reference.
 #include <cstring>
+#include <mutex>
 #include <vector>
 #include "common.cuh"
 
 extern "C" const float2 *alisgpu__phaser_acc(alisgpu_phaser *p, int f, int face, long long *cells);
 extern "C" int alisgpu__phaser_nface(alisgpu_phaser *p);
+extern "C" int alisgpu__phaser_nfreq(alisgpu_phaser *p);
 extern "C" void alisgpu__bind_phaser(alisgpu_phaser *p);
 extern "C" const alisgpu_face *alisgpu__phaser_face(alisgpu_phaser *p, int face);
 
@@ -213,16 +215,19 @@ __global__ void __launch_bounds__(FF_THREADS) k_farfield(const FFParams P)
 	P.part[a * 6 + fidx] = out;
 }
 
-extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
-                                     const double *T, int nk, const unsigned char *present,
-                                     const double *kx, const double *ky, double *out)
+// Faces of the phaser in the kernel's form, and the largest shared-memory
+// weight table one of them needs.  Checks every index the kernel derives
+// from the arguments: the frequency, and for every face its i, j and k
+// ranges (k one beyond, for the half-cell H samples) against the lengths
+// of the line tables and of the test fields, mirror images included.
+static int ffFaces(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nk, FFParams &P, size_t &smem,
+                   const char *who)
 {
-	if (!p || !g || nA < 0 || !T || !present || !kx || !ky || !out) return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums: bad argument");
-	if (!nA) return ALISGPU_OK;
-	alisgpu__bind_phaser(p);
-	cudaStream_t st = alisgpu__stream();
-	FFParams P;
-	memset(&P, 0, sizeof P);
+	if (f < 0 || f >= alisgpu__phaser_nfreq(p))
+		return alisgpu__fail(ALISGPU_EINVAL, "%s: frequency %d outside [0, %d)", who, f, alisgpu__phaser_nfreq(p));
+	if (nk < 1 || g->zLen < 1 || g->xLen < 0 || g->yLen < 0)
+		return alisgpu__fail(ALISGPU_EINVAL, "%s: bad table lengths (nk %d, z %d)", who, nk, g->zLen);
+	const int kLen = nk < g->zLen ? nk : g->zLen;
 	P.nface = alisgpu__phaser_nface(p);
 	int maxn = 1;
 	for (int q = 0; q < P.nface; q++) {
@@ -230,58 +235,97 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 		FFFace &F = P.face[q];
 		F.axis = fc->axis;
 		F.i0 = fc->i0, F.i1 = fc->i1, F.j0 = fc->j0, F.j1 = fc->j1, F.k0 = fc->k0, F.k1 = fc->k1;
+		bool ok = F.i0 >= g->iMin && F.i1 < g->iMin + g->xLen && F.j0 >= g->jMin && F.j1 < g->jMin + g->yLen &&
+		          F.k0 >= g->kMIN && F.k1 + 1 < g->kMIN + kLen;
+		if (g->sym[2]) ok = ok && -F.k1 >= g->kMIN && 1 - F.k0 < g->kMIN + kLen;
+		if (!ok)
+			return alisgpu__fail(ALISGPU_EINVAL, "%s: face %d [%d,%d]x[%d,%d]x[%d,%d] outside the tables", who, q,
+			                     F.i0, F.i1, F.j0, F.j1, F.k0, F.k1);
 		long long cells;
 		F.acc = alisgpu__phaser_acc(p, f, q, &cells);
 		int n1 = F.axis == 0 ? 1 + F.j1 - F.j0 : 1 + F.i1 - F.i0;
 		int n2 = F.axis == 2 ? 1 + F.j1 - F.j0 : 1 + F.k1 - F.k0;
 		maxn = n1 + n2 > maxn ? n1 + n2 : maxn;
 	}
-	// device copies of the geometry tables and the direction batch
+	smem = (size_t)4 * maxn * sizeof(double2);
+	if (smem > 200 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "%s: face of %d cells per side too large", who, maxn);
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
+                                     const double *T, int nk, const unsigned char *present,
+                                     const double *kx, const double *ky, double *out)
+{
+	if (!p || !g || nA < 0 || nk < 0 || !T || !present || !kx || !ky || !out)
+		return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums: bad argument");
+	if (!nA) return ALISGPU_OK;
+	alisgpu__bind_phaser(p);
+	FFParams P;
+	memset(&P, 0, sizeof P);
+	size_t smem = 0;
+	int rc = ffFaces(p, f, g, nk, P, smem, "farfield_sums");
+	if (rc) return rc;
+	cudaStream_t st = alisgpu__stream();
+	// Device copies of the geometry tables and the direction batch.  Every
+	// allocation is made before anything is enqueued; any failure frees
+	// what was taken and returns before a copy or a launch.
 	std::vector<void *> tmp;
-	auto up = [&](const void *src, size_t bytes) -> void * {
+	bool failed = false;
+	auto take = [&](size_t bytes) -> void * {
 		void *d = 0;
-		if (alisgpu__mallocAsync(&d, bytes) != cudaSuccess) return 0;
-		cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, st);
+		if (alisgpu__mallocAsync(&d, bytes ? bytes : 1) != cudaSuccess) d = 0, failed = true;
 		tmp.push_back(d);
 		return d;
 	};
+	auto release = [&]() { for (void *q : tmp) if (q) alisgpu__freeAsync(q); tmp.clear(); };
+	const double *src[10] = { g->xE, g->xH, g->dxE, g->dxH, g->yE, g->yH, g->dyE, g->dyH, g->dzE, g->dzH };
+	size_t bytes[10];
+	for (int q = 0; q < 10; q++) bytes[q] = (size_t)(q < 4 ? g->xLen : q < 8 ? g->yLen : g->zLen) * sizeof(double);
+	void *dTab[10];
+	for (int q = 0; q < 10; q++) dTab[q] = take(bytes[q]);
+	const size_t tBytes = (size_t)nA * 6 * nk * sizeof(double2);
+	void *dT = take(tBytes), *dPr = take((size_t)nA * 6);
+	void *dKx = take(nA * sizeof(double)), *dKy = take(nA * sizeof(double));
+	double2 *part = (double2 *)take((size_t)nA * 6 * sizeof(double2));
+	if (failed) {
+		release();
+		return alisgpu__fail(ALISGPU_ENOMEM, "farfield_sums: allocation failed");
+	}
+	cudaError_t e = cudaSuccess;
+	for (int q = 0; q < 10 && e == cudaSuccess; q++)
+		if (bytes[q]) e = cudaMemcpyAsync(dTab[q], src[q], bytes[q], cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dT, T, tBytes, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dPr, present, (size_t)nA * 6, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dKx, kx, nA * sizeof(double), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(dKy, ky, nA * sizeof(double), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemsetAsync(part, 0, (size_t)nA * 6 * sizeof(double2), st);
 	P.g = *g;
-	P.g.xE = (const double *)up(g->xE, g->xLen * sizeof(double));
-	P.g.xH = (const double *)up(g->xH, g->xLen * sizeof(double));
-	P.g.dxE = (const double *)up(g->dxE, g->xLen * sizeof(double));
-	P.g.dxH = (const double *)up(g->dxH, g->xLen * sizeof(double));
-	P.g.yE = (const double *)up(g->yE, g->yLen * sizeof(double));
-	P.g.yH = (const double *)up(g->yH, g->yLen * sizeof(double));
-	P.g.dyE = (const double *)up(g->dyE, g->yLen * sizeof(double));
-	P.g.dyH = (const double *)up(g->dyH, g->yLen * sizeof(double));
-	P.g.dzE = (const double *)up(g->dzE, g->zLen * sizeof(double));
-	P.g.dzH = (const double *)up(g->dzH, g->zLen * sizeof(double));
+	P.g.xE = (const double *)dTab[0], P.g.xH = (const double *)dTab[1];
+	P.g.dxE = (const double *)dTab[2], P.g.dxH = (const double *)dTab[3];
+	P.g.yE = (const double *)dTab[4], P.g.yH = (const double *)dTab[5];
+	P.g.dyE = (const double *)dTab[6], P.g.dyH = (const double *)dTab[7];
+	P.g.dzE = (const double *)dTab[8], P.g.dzH = (const double *)dTab[9];
 	P.nk = nk;
-	P.T = (const double2 *)up(T, (size_t)nA * 6 * nk * sizeof(double2));
-	P.present = (const unsigned char *)up(present, (size_t)nA * 6);
-	P.kx = (const double *)up(kx, nA * sizeof(double));
-	P.ky = (const double *)up(ky, nA * sizeof(double));
-	double2 *part = 0;
-	ALIS_CUDA(alisgpu__mallocAsync(&part, (size_t)nA * 6 * sizeof(double2)));
-	tmp.push_back(part);
-	ALIS_CUDA(cudaMemsetAsync(part, 0, (size_t)nA * 6 * sizeof(double2), st));
+	P.T = (const double2 *)dT;
+	P.present = (const unsigned char *)dPr;
+	P.kx = (const double *)dKx, P.ky = (const double *)dKy;
 	P.part = part;
-	for (void *q : tmp) if (!q) return alisgpu__fail(ALISGPU_ENOMEM, "farfield_sums: allocation failed");
-	size_t smem = (size_t)4 * maxn * sizeof(double2);
-	if (smem > 200 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums: face of %d cells per side too large", maxn);
-	ALIS_CUDA(cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	if (P.nface) {
+	if (e == cudaSuccess) e = cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e == cudaSuccess && P.nface) {
 		dim3 grid(nA, P.nface);
 		int slot = alisgpu__prof_start();
 		k_farfield<<<grid, FF_THREADS, smem, st>>>(P);
 		alisgpu__prof_stop(slot, ALISGPU_K_FARFIELD);
 		alisgpu__count_launch();
-		ALIS_CUDA(cudaGetLastError());
+		e = cudaGetLastError();
 	}
 	std::vector<double2> h((size_t)nA * 6);
-	ALIS_CUDA(cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st));
-	ALIS_CUDA(cudaStreamSynchronize(st));
-	for (void *q : tmp) alisgpu__freeAsync(q);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double2), cudaMemcpyDeviceToHost, st);
+	// whatever was enqueued finishes before the buffers go back to the pool
+	cudaError_t es = cudaStreamSynchronize(st);
+	release();
+	if (e == cudaSuccess) e = es;
+	if (e != cudaSuccess) return alisgpu__check(e, "farfield_sums");
 	// faces in device order are min/max per axis as the host listed them;
 	// the host gives the sign per face through out[] layout: out[a*12 + 2*face]
 	for (int a = 0; a < nA; a++) for (int q = 0; q < 6; q++) {
@@ -298,11 +342,14 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
 // call made on it; make that first call before any stream capture starts.
 // Calls share the array, so overlapping calls (several host threads, or
 // a call issued while another is in flight) race; calls from one thread
-// are serialised by the synchronisation at the end of each call.
+// are serialised by the synchronisation at the end of each call, which
+// also runs when a call fails after enqueueing work.
 // ---------------------------------------------------------------------
 static __device__ __align__(256) unsigned char ffStaticScratch[ALISGPU_FF_STATIC_BYTES];
 #define FF_MAX_DEVICES 64
 static unsigned char *ffStaticBase[FF_MAX_DEVICES];
+static std::once_flag ffStaticOnce[FF_MAX_DEVICES];
+static cudaError_t ffStaticErr[FF_MAX_DEVICES];
 
 extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
                                             const double *T, int nk, const unsigned char *present,
@@ -311,14 +358,23 @@ extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alis
 	if (!p || !g || nA < 0 || !T || !present || !kx || !ky || !out || nk < 0)
 		return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums_static: bad argument");
 	if (!nA) return ALISGPU_OK;
+	alisgpu__bind_phaser(p);
+	FFParams P;
+	memset(&P, 0, sizeof P);
+	size_t smem = 0;
+	int rc = ffFaces(p, f, g, nk, P, smem, "farfield_sums_static");
+	if (rc) return rc;
 	int dev = 0;
 	ALIS_CUDA(cudaGetDevice(&dev));
 	if (dev < 0 || dev >= FF_MAX_DEVICES) return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: device %d beyond %d", dev, FF_MAX_DEVICES);
-	if (!ffStaticBase[dev]) {
+	// the device address of the array, looked up once per device with that
+	// device current (the host-side symbol is not a device address)
+	std::call_once(ffStaticOnce[dev], [dev]() {
 		void *base = 0;
-		ALIS_CUDA(cudaGetSymbolAddress(&base, ffStaticScratch));
-		ffStaticBase[dev] = (unsigned char *)base;
-	}
+		ffStaticErr[dev] = cudaGetSymbolAddress(&base, ffStaticScratch);
+		if (ffStaticErr[dev] == cudaSuccess) ffStaticBase[dev] = (unsigned char *)base;
+	});
+	if (ffStaticErr[dev] != cudaSuccess) return alisgpu__check(ffStaticErr[dev], "farfield_sums_static: cudaGetSymbolAddress");
 	// carve the scratch: tables, test fields, flags, wave numbers, partials
 	size_t off = 0;
 	auto take = [&](size_t bytes) -> size_t { size_t at = off; off += (bytes + 255) & ~(size_t)255; return at; };
@@ -334,59 +390,45 @@ extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alis
 	if (off > (size_t)ALISGPU_FF_STATIC_BYTES)
 		return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: %d directions need %zu bytes of scratch, the static buffer holds %u; "
 		                     "split the batch", nA, off, (unsigned)ALISGPU_FF_STATIC_BYTES);
-	alisgpu__bind_phaser(p);
 	cudaStream_t st = alisgpu__stream();
 	unsigned char *base = ffStaticBase[dev];
-	FFParams P;
-	memset(&P, 0, sizeof P);
-	P.nface = alisgpu__phaser_nface(p);
-	int maxn = 1;
-	for (int q = 0; q < P.nface; q++) {
-		const alisgpu_face *fc = alisgpu__phaser_face(p, q);
-		FFFace &F = P.face[q];
-		F.axis = fc->axis;
-		F.i0 = fc->i0, F.i1 = fc->i1, F.j0 = fc->j0, F.j1 = fc->j1, F.k0 = fc->k0, F.k1 = fc->k1;
-		long long cells;
-		F.acc = alisgpu__phaser_acc(p, f, q, &cells);
-		int n1 = F.axis == 0 ? 1 + F.j1 - F.j0 : 1 + F.i1 - F.i0;
-		int n2 = F.axis == 2 ? 1 + F.j1 - F.j0 : 1 + F.k1 - F.k0;
-		maxn = n1 + n2 > maxn ? n1 + n2 : maxn;
-	}
-	size_t smem = (size_t)4 * maxn * sizeof(double2);
-	if (smem > 200 * 1024) return alisgpu__fail(ALISGPU_ERANGE, "farfield_sums_static: face of %d cells per side too large", maxn);
 	const double *src[10] = { g->xE, g->xH, g->dxE, g->dxH, g->yE, g->yH, g->dyE, g->dyH, g->dzE, g->dzH };
 	const size_t len[10] = { xb, xb, xb, xb, yb, yb, yb, yb, zb, zb };
 	const double *dev10[10];
+	cudaError_t e = cudaSuccess;
 	for (int q = 0; q < 10; q++) {
 		dev10[q] = (const double *)(base + oTab[q]);
-		if (len[q]) ALIS_CUDA(cudaMemcpyAsync(base + oTab[q], src[q], len[q], cudaMemcpyHostToDevice, st));
+		if (len[q] && e == cudaSuccess) e = cudaMemcpyAsync(base + oTab[q], src[q], len[q], cudaMemcpyHostToDevice, st);
 	}
 	P.g = *g;
 	P.g.xE = dev10[0], P.g.xH = dev10[1], P.g.dxE = dev10[2], P.g.dxH = dev10[3];
 	P.g.yE = dev10[4], P.g.yH = dev10[5], P.g.dyE = dev10[6], P.g.dyH = dev10[7];
 	P.g.dzE = dev10[8], P.g.dzH = dev10[9];
 	P.nk = nk;
-	ALIS_CUDA(cudaMemcpyAsync(base + oT, T, (size_t)nA * 6 * nk * sizeof(double2), cudaMemcpyHostToDevice, st));
-	ALIS_CUDA(cudaMemcpyAsync(base + oPr, present, (size_t)nA * 6, cudaMemcpyHostToDevice, st));
-	ALIS_CUDA(cudaMemcpyAsync(base + oKx, kx, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st));
-	ALIS_CUDA(cudaMemcpyAsync(base + oKy, ky, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st));
+	if (e == cudaSuccess) e = cudaMemcpyAsync(base + oT, T, (size_t)nA * 6 * nk * sizeof(double2), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(base + oPr, present, (size_t)nA * 6, cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(base + oKx, kx, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(base + oKy, ky, (size_t)nA * sizeof(double), cudaMemcpyHostToDevice, st);
 	// the partials of missing faces must read as zero
-	ALIS_CUDA(cudaMemsetAsync(base + oPart, 0, (size_t)nA * 6 * sizeof(double2), st));
+	if (e == cudaSuccess) e = cudaMemsetAsync(base + oPart, 0, (size_t)nA * 6 * sizeof(double2), st);
 	P.T = (const double2 *)(base + oT);
 	P.present = base + oPr;
 	P.kx = (const double *)(base + oKx), P.ky = (const double *)(base + oKy);
 	P.part = (double2 *)(base + oPart);
-	ALIS_CUDA(cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	if (P.nface) {
+	if (e == cudaSuccess) e = cudaFuncSetAttribute(k_farfield, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+	if (e == cudaSuccess && P.nface) {
 		dim3 grid(nA, P.nface);
 		int slot = alisgpu__prof_start();
 		k_farfield<<<grid, FF_THREADS, smem, st>>>(P);
 		alisgpu__prof_stop(slot, ALISGPU_K_FARFIELD);
 		alisgpu__count_launch();
-		ALIS_CUDA(cudaGetLastError());
+		e = cudaGetLastError();
 	}
 	// out[(a*6 + face)*2 + re/im] has the layout of the double2 partials
-	ALIS_CUDA(cudaMemcpyAsync(out, base + oPart, (size_t)nA * 6 * sizeof(double2), cudaMemcpyDeviceToHost, st));
-	ALIS_CUDA(cudaStreamSynchronize(st));
+	if (e == cudaSuccess) e = cudaMemcpyAsync(out, base + oPart, (size_t)nA * 6 * sizeof(double2), cudaMemcpyDeviceToHost, st);
+	// on success and on failure alike, nothing of this call is left in flight
+	cudaError_t es = cudaStreamSynchronize(st);
+	if (e == cudaSuccess) e = es;
+	if (e != cudaSuccess) return alisgpu__check(e, "farfield_sums_static");
 	return ALISGPU_OK;
 }

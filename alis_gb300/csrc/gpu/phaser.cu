@@ -549,5 +549,6 @@ extern "C" const float2 *alisgpu__phaser_acc(alisgpu_phaser *p, int f, int face,
 	return p->acc + (size_t)f * p->cells * 4 + p->faceStart[face] * 4;
 }
 extern "C" int alisgpu__phaser_nface(alisgpu_phaser *p) { return p->nface; }
+extern "C" int alisgpu__phaser_nfreq(alisgpu_phaser *p) { return p->nfreq; }
 extern "C" void alisgpu__bind_phaser(alisgpu_phaser *p) { if (p) alisgpu__bind(p->w); }
 extern "C" const alisgpu_face *alisgpu__phaser_face(alisgpu_phaser *p, int face) { return &p->faces[face]; }

@@ -128,6 +128,14 @@ static void fullJoin(void)
 extern "C" const char *alisgpu_last_error(void) { return gErr; }
 extern "C" void alisgpu__count_launch(void) { gLaunches++, gOps++; }
 extern "C" unsigned long long alisgpu_launch_count(void) { return gLaunches; }
+static std::atomic<int> gDenyAllocs;
+extern "C" int alisgpu_inject_alloc_failures(int n) { return gDenyAllocs.exchange(n > 0 ? n : 0); }
+extern "C" int alisgpu__alloc_denied(void)
+{
+	int n = gDenyAllocs.load();
+	while (n > 0 && !gDenyAllocs.compare_exchange_weak(n, n - 1)) {}
+	return n > 0;
+}
 extern "C" cudaStream_t alisgpu__stream(void) { return gStream; }
 extern "C" void *alisgpu_stream(void) { return (void *)gDefaultGroup.main; }
 
@@ -1687,13 +1695,17 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 		GL.levStart[nlev] = GL.n;
 		GL.start[GL.n] = at;
 		GL.nlev = nlev;
-		static int blocksMax;
+		// resident blocks of the cooperative launch, computed once (host
+		// threads stepping several worlds may get here together)
+		static std::atomic<int> blocksMaxAt{0};
+		int blocksMax = blocksMaxAt.load();
 		if (!blocksMax) {
 			int dev = 0, sms = 0, per = 0;
 			ALIS_CUDA(cudaGetDevice(&dev));
 			ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 			ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_ghost_levels, 256, 0));
 			blocksMax = std::max(1, sms * per);
+			blocksMaxAt.store(blocksMax);
 		}
 		const int blocks = (int)std::min<long long>((total + 255) / 256, blocksMax);
 		void *args[] = { (void *)&GL };

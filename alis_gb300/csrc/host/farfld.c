@@ -14,7 +14,11 @@
 #include <string.h>
 #include "engine.h"
 
-/* --- projection maps (reference src/farfld.c:14-41) --- */
+/* --- projection maps (reference src/farfld.c:14-41) ---
+ * Pixel (x, y) of an X x Y image to a direction (theta, phi) in degrees;
+ * INF marks a pixel outside the map.  The arithmetic (double ratios,
+ * float square root and arc tangent) is the reference's, so the same
+ * pixel gives the same float angles. */
 
 void CylindericalMap(int x, int y, int X, int Y, float angle[2])
 {
@@ -22,24 +26,34 @@ void CylindericalMap(int x, int y, int X, int Y, float angle[2])
 	angle[1] = 360.0 * x / X;
 }
 
+/* one hemisphere seen from its pole: the polar angle grows with the
+ * distance from the image centre, 90 degrees at the inscribed circle */
+static void hemisphereMap(int x, int y, int X, int Y, int south, float angle[2])
+{
+	const double u = x / (X - 1.0) - 0.5, v = y / (Y - 1.0) - 0.5;
+	const float fromPole = 180 * sqrtf(u * u + v * v);
+	const float polar = south ? 180 - fromPole : fromPole;
+	angle[1] = 180 * atan2f(v, u) / PI;
+	angle[0] = (south ? polar < 90 : polar > 90) ? INF : polar;
+}
+
 void NorthernAzimuthalMap(int x, int y, int X, int Y, float angle[2])
 {
-	angle[0] = 180 * sqrtf(sq(x/(X-1.0)-0.5) + sq(y/(Y-1.0)-0.5));
-	angle[1] = 180 * atan2f(y/(Y-1.0)-0.5, x/(X-1.0)-0.5) / PI;
-	if (angle[0] > 90) angle[0] = INF;
+	hemisphereMap(x, y, X, Y, 0, angle);
 }
 
 void SouthernAzimuthalMap(int x, int y, int X, int Y, float angle[2])
 {
-	angle[0] = 180 - 180 * sqrtf(sq(x/(X-1.0)-0.5) + sq(y/(Y-1.0)-0.5));
-	angle[1] = 180 * atan2f(y/(Y-1.0)-0.5, x/(X-1.0)-0.5) / PI;
-	if (angle[0] < 90) angle[0] = INF;
+	hemisphereMap(x, y, X, Y, 1, angle);
 }
 
+/* the two hemispheres side by side; a middle column of an odd width
+ * belongs to both, the southern one written last */
 void AzimuthalMap(int x, int y, int X, int Y, float angle[2])
 {
-	if (x < (X+1)/2) NorthernAzimuthalMap(x, y, (X+1)/2, Y, angle);
-	if (x > X/2) SouthernAzimuthalMap(x-X/2, y, (X+1)/2, Y, angle);
+	const int half = (X + 1) / 2;
+	if (x < half) hemisphereMap(x, y, half, Y, 0, angle);
+	if (x > X / 2) hemisphereMap(x - X / 2, y, half, Y, 1, angle);
 }
 
 /* direction (a, b) rotated by theta about y (reference src/farfld.c:44-52) */
@@ -336,141 +350,210 @@ float farFieldI(phaser P, tfield pol(phaser,float,float), float theta, float phi
 	return conjf(f) * f;
 }
 
-/* Seven polarisation images (X, Y, CL, CR, P, S, unpolarised) of the far
- * field over an X x Y projection map (reference src/farfld.c:525-594).
- * All directions go to the backend as two batches. */
+/* The seven intensities of one direction from its P and S amplitudes:
+ * X and Y (the frame rotated by phi), circular left and right, P, S and
+ * unpolarised (reference src/farfld.c:563-580); log10 of each when asked. */
+enum { IMG_X, IMG_Y, IMG_CL, IMG_CR, IMG_P, IMG_S, IMG_UNPOL, IMG_COUNT };
+
+static void polarisations(float complex p, float complex s, float phi, int logScale, float v[IMG_COUNT])
+{
+	const float complex x = p*cosf(phi*PI/180)-s*sinf(phi*PI/180);
+	const float complex y = s*cosf(phi*PI/180)+p*sinf(phi*PI/180);
+	v[IMG_X] = conjf(x)*x;
+	v[IMG_Y] = conjf(y)*y;
+	v[IMG_CL] = sq(crealf(p)+cimagf(s))+sq(cimagf(p)-crealf(s));
+	v[IMG_CR] = sq(crealf(p)-cimagf(s))+sq(cimagf(p)+crealf(s));
+	v[IMG_P] = conjf(p)*p;
+	v[IMG_S] = conjf(s)*s;
+	if (!logScale) {
+		v[IMG_UNPOL] = v[IMG_P] + v[IMG_S];
+		return;
+	}
+	for (int q = 0; q < IMG_UNPOL; q++) v[q] = log10f(v[q]);
+	v[IMG_UNPOL] = log10f(conjf(p)*p+conjf(s)*s);
+}
+
+/* Where an image writer puts its files: W->ID followed by the caller's
+ * formatted name; a name starting with '/' puts them in the directory
+ * W->ID, and a full name ending with '/' is itself a directory. */
+static void outputName(world W, const char *name, char *full, size_t cap)
+{
+	snprintf(full, cap, "%s%s", W->ID, name);
+	if (name[0] == '/') mkdir(W->ID, 0755);
+	size_t n = strlen(full);
+	if (n && full[n-1] == '/') mkdir(full, 0755);
+}
+
+/* a one-plane slice of X x Y pixels, the shape the image writers take */
+static slice imageSlice(int X, int Y)
+{
+	slice S = calloc(1, sizeof *S);
+	S->jMax = S->jMAX = X - 1, S->jNUM = X;
+	S->kMax = S->kMAX = Y - 1, S->kNUM = Y;
+	return S;
+}
+
+/* Seven polarisation images of the far field over an X x Y projection
+ * map (reference src/farfld.c:525-594).  The variable arguments are the
+ * writer, its colour map and scale when it is png, and a printf-style
+ * file name; a name containing "Log" writes log10 intensities.  Every
+ * direction of the map goes to the backend in one batch per
+ * polarisation. */
 void farFieldProfile(world W, phaser P, projmap projMap, int X, int Y, ...)
 {
-	char *format, fieldname[4], filename[1024], fullname[1024];
 	va_list ap;
 	va_start(ap, Y);
-	method M = va_arg(ap, method);
-	unsigned long int *cmap = (M == png) ? va_arg(ap, unsigned long int *) : 0;
-	float Max = (M == png) ? va_arg(ap, double) : 1;
-	float max = 0, angle[2];
-	format = va_arg(ap, char*);
-	vsprintf(filename, format, ap);
+	const method M = va_arg(ap, method);
+	unsigned long int *cmap = 0;
+	float scale = 1;
+	if (M == png) {
+		cmap = va_arg(ap, unsigned long int *);
+		scale = va_arg(ap, double);
+	}
+	const char *format = va_arg(ap, const char *);
+	char name[1024], base[1024], file[1100];
+	vsnprintf(name, sizeof name, format, ap);
 	va_end(ap);
-	strcat(strcpy(fullname, W->ID), filename);
-	strcpy(fieldname, strstr(filename, "Log") ? "Log" : "");
-	if (filename[0]=='/') mkdir(W->ID, 0755);
-	if (fullname[strlen(fullname)-1]=='/') mkdir(fullname, 0755);
+	outputName(W, name, base, sizeof base);
+	char logTag[4] = "";
+	if (strstr(name, "Log")) strcpy(logTag, "Log");
 
-	slice S;
-	MALLOC(S, 0, 1);
-	*S = (struct slice) {0, 0, 0, X-1, 0, Y-1, 0, 0, 0, 0, X-1, X, 0, Y-1, Y};
-	float ***img[7];
-	for (int q = 0; q < 7; q++) img[q] = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
-	float ***Xp = img[0], ***Yp = img[1], ***Lp = img[2], ***Rp = img[3], ***Pp = img[4], ***Sp = img[5], ***Up = img[6];
+	const int pixels = X * Y;
+	float *theta = malloc(pixels * sizeof(float)), *phi = malloc(pixels * sizeof(float));
+	float complex *ampP = malloc(pixels * sizeof(float complex)), *ampS = malloc(pixels * sizeof(float complex));
+	/* pixels in the reference's order; a pixel the map leaves untouched
+	 * (the middle column of an even-width AzimuthalMap) repeats the
+	 * direction of the pixel before it */
+	float a[2] = { 0, 0 };
+	for (int q = 0; q < pixels; q++) {
+		projMap(q / Y, q % Y, X, Y, a);
+		theta[q] = a[0], phi[q] = a[1];
+	}
+	farFieldBatch(P, Ppol, pixels, theta, phi, ampP);
+	farFieldBatch(P, Spol, pixels, theta, phi, ampS);
 
-	int NA = X*Y;
-	float *th = calloc(NA, sizeof(float)), *ph = calloc(NA, sizeof(float));
-	float complex *pv = calloc(NA, sizeof(float complex)), *sv = calloc(NA, sizeof(float complex));
-	for (int x = 0; x < X; x++) for (int y = 0; y < Y; y++) {
-		projMap(x, y, X, Y, angle);
-		th[x*Y+y] = angle[0], ph[x*Y+y] = angle[1];
+	slice S = imageSlice(X, Y);
+	float ***img[IMG_COUNT];
+	for (int q = 0; q < IMG_COUNT; q++) img[q] = makeField(0, 0, 0, X-1, 0, Y-1);
+	float brightest = 0;
+	for (int q = 0; q < pixels; q++) {
+		float v[IMG_COUNT];
+		polarisations(ampP[q], ampS[q], phi[q], logTag[0] != 0, v);
+		for (int c = 0; c < IMG_COUNT; c++) img[c][0][q / Y][q % Y] = v[c];
+		brightest = MAX(brightest, v[IMG_UNPOL]);
 	}
-	printf("Performing Near-to-Far-Field Transformation.\n");
-	farFieldBatch(P, Ppol, NA, th, ph, pv);
-	farFieldBatch(P, Spol, NA, th, ph, sv);
-	int log = fieldname[0] != 0;
-	for (int x = 0; x < X; x++) for (int y = 0; y < Y; y++) {
-		float complex p = pv[x*Y+y], s = sv[x*Y+y];
-		float a1 = ph[x*Y+y];
-		float vx = conjf(p*cosf(a1*PI/180)-s*sinf(a1*PI/180))*(p*cosf(a1*PI/180)-s*sinf(a1*PI/180));
-		float vy = conjf(s*cosf(a1*PI/180)+p*sinf(a1*PI/180))*(s*cosf(a1*PI/180)+p*sinf(a1*PI/180));
-		float vl = sq(crealf(p)+cimagf(s))+sq(cimagf(p)-crealf(s));
-		float vr = sq(crealf(p)-cimagf(s))+sq(cimagf(p)+crealf(s));
-		float vp = conjf(p)*p, vs = conjf(s)*s;
-		if (log) {
-			Xp[0][x][y] = log10f(vx), Yp[0][x][y] = log10f(vy), Lp[0][x][y] = log10f(vl), Rp[0][x][y] = log10f(vr);
-			Pp[0][x][y] = log10f(vp), Sp[0][x][y] = log10f(vs), Up[0][x][y] = log10f(conjf(p)*p+conjf(s)*s);
-		} else {
-			Xp[0][x][y] = vx, Yp[0][x][y] = vy, Lp[0][x][y] = vl, Rp[0][x][y] = vr;
-			Pp[0][x][y] = vp, Sp[0][x][y] = vs, Up[0][x][y] = Pp[0][x][y]+Sp[0][x][y];
-		}
-		max = MAX(max, Up[0][x][y]);
-	}
-	free(th); free(ph); free(pv); free(sv);
-	if (Max <= 0) Max = max;
-	const char *tag[7] = { "X-pol", "Y-pol", "CL-pol", "CR-pol", "P-pol", "S-pol", "Unpol" };
-	for (int q = 0; q < 7; q++) {
-		S->F = img[q];
-		M(W, S, Max, fieldname, strcat(strcpy(filename, fullname), tag[q]), cmap);
-		if (q < 6) removeField(img[q], 0, 0, 0);
+	free(theta); free(phi); free(ampP); free(ampS);
+	if (scale <= 0) scale = brightest;
+	static const char *const suffix[IMG_COUNT] = { "X-pol", "Y-pol", "CL-pol", "CR-pol", "P-pol", "S-pol", "Unpol" };
+	for (int c = 0; c < IMG_COUNT; c++) {
+		snprintf(file, sizeof file, "%s%s", base, suffix[c]);
+		S->F = img[c];
+		M(W, S, scale, logTag, file, cmap);
+		if (c < IMG_UNPOL) removeField(img[c], 0, 0, 0);
 	}
 	deleteSlice(S);
 }
 
+/* A 360-degree cut through the far field, one degree apart: theta at
+ * fixed phi, or phi at fixed theta.  One row per degree: the angle, the
+ * unpolarised, P and S intensities (reference src/farfld.c:597-624). */
+static void farFieldCut(world W, phaser P, int alongTheta, float fixed, const char *name)
+{
+	float theta[360], phi[360];
+	float complex ampP[360], ampS[360];
+	for (int a = 0; a < 360; a++) {
+		theta[a] = alongTheta ? a : fixed;
+		phi[a] = alongTheta ? fixed : a;
+	}
+	farFieldBatch(P, Ppol, 360, theta, phi, ampP);
+	farFieldBatch(P, Spol, 360, theta, phi, ampS);
+	for (int a = 0; a < 360; a++) {
+		const float ip = sq(cabsf(ampP[a])), is = sq(cabsf(ampS[a]));
+		writeRow(W, (char *)name, (float)a, ip + is, ip, is);
+	}
+}
+
 void farFieldTheta(world W, phaser P, float phi, char *format, ...)
 {
-	char filename[1024];
+	char name[1024];
 	va_list ap;
 	va_start(ap, format);
-	vsprintf(filename, format, ap);
+	vsnprintf(name, sizeof name, format, ap);
 	va_end(ap);
-	float th[360], ph[360];
-	float complex p[360], s[360];
-	for (int a = 0; a < 360; a++) th[a] = a, ph[a] = phi;
-	farFieldBatch(P, Ppol, 360, th, ph, p);
-	farFieldBatch(P, Spol, 360, th, ph, s);
-	for (int a = 0; a < 360; a++)
-		writeRow(W, filename, th[a], sq(cabsf(p[a]))+sq(cabsf(s[a])), sq(cabsf(p[a])), sq(cabsf(s[a])));
+	farFieldCut(W, P, 1, phi, name);
 }
 
 void farFieldPhi(world W, phaser P, float theta, char *format, ...)
 {
-	char filename[1024];
+	char name[1024];
 	va_list ap;
 	va_start(ap, format);
-	vsprintf(filename, format, ap);
+	vsnprintf(name, sizeof name, format, ap);
 	va_end(ap);
-	float th[360], ph[360];
-	float complex p[360], s[360];
-	for (int a = 0; a < 360; a++) th[a] = theta, ph[a] = a;
-	farFieldBatch(P, Ppol, 360, th, ph, p);
-	farFieldBatch(P, Spol, 360, th, ph, s);
-	for (int a = 0; a < 360; a++)
-		writeRow(W, filename, ph[a], sq(cabsf(p[a]))+sq(cabsf(s[a])), sq(cabsf(p[a])), sq(cabsf(s[a])));
+	farFieldCut(W, P, 0, theta, name);
 }
 
-/* power into a cone of half-angle aMax (or a ring aMin..aMax) around
- * (theta, phi), integrated on rings of width delta with 6n samples
- * (reference src/farfld.c:627-662) */
+/* One ring of farFieldFlux: its index n around the axis, its sample
+ * count and its solid-angle weight (a difference of cosines). */
+typedef struct { int n, samples; float weight; } fluxRing;
+
+/* Power into a cone of half-angle aMax (a ring aMin..aMax when aMin > 0)
+ * around the direction (theta, phi), in the reference's quadrature
+ * (src/farfld.c:627-662): a polar cap below delta/2 from farFieldI, then
+ * rings of width delta with 6n samples each (at most 360 samples, from 60
+ * degrees on).  Every ring sample goes to the backend in one batch per
+ * polarisation; the float sum is formed in the reference's order. */
 float (farFieldFlux)(phaser P, tfield pol(phaser,float,float), float theta, float phi, float aMin, float aMax, float delta, ...)
 {
 	if (!delta) delta = 1;
 	if (!aMax) aMax = aMin, aMin = 0;
 	float Sum = 0;
-	int nMin = floor(aMin/delta+0.5);
-	int nMax = ceil(aMax/delta-0.5);
-	if (!nMin) {
+	int first = floor(aMin/delta+0.5);
+	const int last = ceil(aMax/delta-0.5);
+	if (!first) {
 		Sum = 2 * PI * (cosf(aMin*PI/180) - cosf(MIN(aMax,0.5*delta)*PI/180)) * farFieldI(P,pol,theta,phi);
 		aMin = 0.5 * delta;
-		nMin++;
+		first = 1;
 	}
-	if (!nMax) return Sum;
-	for (int n = nMin; n <= nMax; n++) {
-		int N = n<floor(60/delta+0.5) ? n*6 : floor(60/delta+0.5)*6;
-		float dth = cosf(MAX(aMin,delta*(n-0.5))*PI/180) - cosf(MIN(aMax,delta*(n+0.5))*PI/180);
-		float *a = calloc(N, sizeof(float)), *b = calloc(N, sizeof(float)), *c = calloc(N, sizeof(float));
-		float complex *pv = calloc(N, sizeof(float complex)), *sv = calloc(N, sizeof(float complex));
-		for (int m = 0; m < N; m++) {
-			a[m] = rotateA(theta, delta*n, 360.0*m/N);
-			b[m] = rotateB(theta, delta*n, 360.0*m/N)+phi;
-			c[m] = rotateB(-a[m], theta, phi-b[m])+180-360.0*m/N;
-		}
-		farFieldBatch(P, Ppol, N, a, b, pv);
-		farFieldBatch(P, Spol, N, a, b, sv);
-		for (int m = 0; m < N; m++) {
-			float complex p = pv[m], s = sv[m];
-			float pp = sq(cabsf((p * cosf(c[m]*PI/180) - s * sinf(c[m]*PI/180))));
-			float ss = sq(cabsf((s * cosf(c[m]*PI/180) + p * sinf(c[m]*PI/180))));
-			if (pol == Ppol) Sum += dth * (pp * (PI/N + sinf(PI/N)) + ss * (PI/N - sinf(PI/N)));
-			if (pol == Spol) Sum += dth * (pp * (PI/N - sinf(PI/N)) + ss * (PI/N + sinf(PI/N)));
-			if (pol == Unpol) Sum += 2 * PI/N * dth * (pp + ss);
-		}
-		free(a); free(b); free(c); free(pv); free(sv);
+	if (!last || last < first) return Sum;
+	const int rings = 1 + last - first;
+	const int widest = floor(60/delta+0.5);
+	fluxRing *ring = malloc(rings * sizeof *ring);
+	int total = 0;
+	for (int r = 0; r < rings; r++) {
+		const int n = first + r;
+		ring[r].n = n;
+		ring[r].samples = n < widest ? n*6 : widest*6;
+		ring[r].weight = cosf(MAX(aMin,delta*(n-0.5))*PI/180) - cosf(MIN(aMax,delta*(n+0.5))*PI/180);
+		total += ring[r].samples;
 	}
+	/* sample m of ring n: the direction at polar angle delta n and azimuth
+	 * 360 m / N about the axis, and the angle c that turns its P/S frame
+	 * into the frame of the axis */
+	float *a = malloc(total * sizeof(float)), *b = malloc(total * sizeof(float)), *c = malloc(total * sizeof(float));
+	float complex *ampP = malloc(total * sizeof(float complex)), *ampS = malloc(total * sizeof(float complex));
+	for (int r = 0, q = 0; r < rings; r++) {
+		const int n = ring[r].n, N = ring[r].samples;
+		for (int m = 0; m < N; m++, q++) {
+			a[q] = rotateA(theta, delta*n, 360.0*m/N);
+			b[q] = rotateB(theta, delta*n, 360.0*m/N)+phi;
+			c[q] = rotateB(-a[q], theta, phi-b[q])+180-360.0*m/N;
+		}
+	}
+	farFieldBatch(P, Ppol, total, a, b, ampP);
+	farFieldBatch(P, Spol, total, a, b, ampS);
+	for (int r = 0, q = 0; r < rings; r++) {
+		const int N = ring[r].samples;
+		const float dth = ring[r].weight, arc = PI/N, chord = sinf(PI/N);
+		for (int m = 0; m < N; m++, q++) {
+			const float complex p = ampP[q], s = ampS[q];
+			const float pp = sq(cabsf((p * cosf(c[q]*PI/180) - s * sinf(c[q]*PI/180))));
+			const float ss = sq(cabsf((s * cosf(c[q]*PI/180) + p * sinf(c[q]*PI/180))));
+			if (pol == Ppol) Sum += dth * (pp * (arc + chord) + ss * (arc - chord));
+			if (pol == Spol) Sum += dth * (pp * (arc - chord) + ss * (arc + chord));
+			if (pol == Unpol) Sum += 2 * arc * dth * (pp + ss);
+		}
+	}
+	free(ring); free(a); free(b); free(c); free(ampP); free(ampS);
 	return Sum;
 }

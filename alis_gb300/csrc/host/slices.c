@@ -14,77 +14,107 @@
 #include <stdint.h>
 #include "engine.h"
 
-/* --- graded-grid resampling (reference src/slices.c:25-64) --- */
+/* --- graded-grid resampling (reference src/slices.c:25-64) ---
+ * A slice of a graded grid is written on the uniform base grid: along
+ * each axis the slice spans (index range [lo, hi] of the graded grid ->
+ * range [LO, HI] of base-grid points), every base point n between graded
+ * cells c and c + 1 gets the linear interpolation of the two.  Axes are
+ * done in the order i, j, k; an axis done spans its base range in the
+ * passes after it.  The arithmetic is the reference's: float positions,
+ * float weights, one division per point. */
+
+static float gridPos(world W, int axis, int c)
+{
+	return axis == 0 ? W->itox(W, c) : axis == 1 ? W->jtoy(W, c) : W->ktoz(W, c);
+}
+
+static float gridStep(world W, int axis)
+{
+	return axis == 0 ? W->dx : axis == 1 ? W->dy : W->dz;
+}
 
 static float ***resample(world W, slice S, float ***F)
 {
-	float ***T, ***G = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
-	if (S->iMin != S->iMIN || S->iMax != S->iMAX) {
-		T = F, F = G, G = T;
-		for (int i = S->iMin; i < S->iMax; i++) {
-			float x0 = W->itox(W, i), x1 = W->itox(W, i+1);
-			int n0 = x0/W->dx+(i>0?1:0), n1 = x1/W->dx-(i<0?1:0);
-			for (int j = S->jMin; j <= S->jMax; j++) for (int n = n0; n <= n1; n++) for (int k = S->kMin; k <= S->kMax; k++)
-				F[n][j][k] = (G[i][j][k] * (x1 - n*W->dx) + G[i+1][j][k] * (n*W->dx - x0)) / (x1 - x0);
+	const int lo[3] = { S->iMin, S->jMin, S->kMin }, hi[3] = { S->iMax, S->jMax, S->kMax };
+	const int LO[3] = { S->iMIN, S->jMIN, S->kMIN }, HI[3] = { S->iMAX, S->jMAX, S->kMAX };
+	int from[3], to[3];             /* the current extent of the data per axis */
+	for (int a = 0; a < 3; a++) from[a] = lo[a], to[a] = hi[a];
+	float ***src = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX), ***dst = F;
+	for (int a = 0; a < 3; a++) {
+		if (lo[a] == LO[a] && hi[a] == HI[a]) continue;
+		float ***t = src; src = dst; dst = t;
+		const int b = (a + 1) % 3, c = (a + 2) % 3;
+		const float d = gridStep(W, a);
+		for (int g = lo[a]; g < hi[a]; g++) {
+			const float p0 = gridPos(W, a, g), p1 = gridPos(W, a, g+1);
+			const int n0 = p0/d+(g>0?1:0), n1 = p1/d-(g<0?1:0);
+			int at[3], next[3];
+			for (at[b] = from[b]; at[b] <= to[b]; at[b]++) for (at[c] = from[c]; at[c] <= to[c]; at[c]++) {
+				at[a] = g;
+				next[0] = at[0], next[1] = at[1], next[2] = at[2], next[a] = g+1;
+				const float v0 = src[at[0]][at[1]][at[2]], v1 = src[next[0]][next[1]][next[2]];
+				for (int n = n0; n <= n1; n++) {
+					at[a] = n;
+					dst[at[0]][at[1]][at[2]] = (v0 * (p1 - n*d) + v1 * (n*d - p0)) / (p1 - p0);
+				}
+			}
 		}
+		from[a] = LO[a], to[a] = HI[a];
 	}
-	if (S->jMin != S->jMIN || S->jMax != S->jMAX) {
-		T = F, F = G, G = T;
-		for (int j = S->jMin; j < S->jMax; j++) {
-			float y0 = W->jtoy(W, j), y1 = W->jtoy(W, j+1);
-			int n0 = y0/W->dy+(j>0?1:0), n1 = y1/W->dy-(j<0?1:0);
-			for (int i = S->iMIN; i <= S->iMAX; i++) for (int n = n0; n <= n1; n++) for (int k = S->kMin; k <= S->kMax; k++)
-				F[i][n][k] = (G[i][j][k] * (y1 - n*W->dy) + G[i][j+1][k] * (n*W->dy - y0)) / (y1 - y0);
-		}
-	}
-	if (S->kMin != S->kMIN || S->kMax != S->kMAX) {
-		T = F, F = G, G = T;
-		for (int k = S->kMin; k < S->kMax; k++) {
-			float z0 = W->ktoz(W, k), z1 = W->ktoz(W, k+1);
-			int n0 = z0/W->dz+(k>0?1:0), n1 = z1/W->dz-(k<0?1:0);
-			for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int n = n0; n <= n1; n++)
-				F[i][j][n] = (G[i][j][k] * (z1 - n*W->dz) + G[i][j][k+1] * (n*W->dz - z0)) / (z1 - z0);
-		}
-	}
-	removeField(G, S->iMIN, S->jMIN, S->kMIN);
-	return F;
+	removeField(src, S->iMIN, S->jMIN, S->kMIN);
+	return dst;
 }
 
-/* slice through the given box, clipped to the grid; 2-D slices of a
- * world with objects also carry a normalised index-contour overlay
- * (reference src/slices.c:67-117) */
+/* Index range of a slice along one axis: the box's ends as grid indices,
+ * clipped to the grid (to the mirror image of the grid below a symmetry
+ * plane), and the base-grid range the slice covers when it is resampled
+ * (reference src/slices.c:67-97). */
+static void sliceAxis(world W, int axis, float pMin, float pMax, int resampled, int r[4])
+{
+	const int MIN_[3] = { W->iMIN, W->jMIN, W->kMIN }, MAX_[3] = { W->iMAX, W->jMAX, W->kMAX };
+	const int sym = (axis == 0 ? W->xMinSur : axis == 1 ? W->yMinSur : W->zMinSur) == SYM;
+	int a = axis == 0 ? W->xtoi(W, pMin) : axis == 1 ? W->ytoj(W, pMin) : W->ztok(W, pMin);
+	int b = axis == 0 ? W->xtoi(W, pMax) : axis == 1 ? W->ytoj(W, pMax) : W->ztok(W, pMax);
+	if (b > MAX_[axis]) b = MAX_[axis];
+	const int floorIdx = sym ? -MAX_[axis] : MIN_[axis];
+	if (a < floorIdx) a = floorIdx;
+	r[0] = a, r[1] = b, r[2] = a, r[3] = b;
+	if (a != b && resampled) {
+		/* MIN / MAX of an index and a base-grid position, as float */
+		const float d = gridStep(W, axis), ea = gridPos(W, axis, a)/d, eb = gridPos(W, axis, b)/d;
+		r[2] = a < ea ? a : ea;
+		r[3] = b > eb ? b : eb;
+	}
+}
+
+/* A slice through the given box.  2-D slices of a world with eps^-1 maps
+ * carry the index contour of the objects, scaled to at most 0.5, for the
+ * image writers to overlay (reference src/slices.c:98-117). */
 slice createSlice(world W, float xMin, float xMax, float yMin, float yMax, float zMin, float zMax)
 {
-	slice S;
-	MALLOC(S, 0, 1);
-	*S = (struct slice) { W->xtoi(W, xMin), W->xtoi(W, xMax), W->ytoj(W, yMin), W->ytoj(W, yMax), W->ztok(W, zMin), W->ztok(W, zMax) };
-	if (W->Res.nug.x.m>1 || W->Res.nug.y.m>1 || W->Res.nug.z.m>1) S->interpolate = resample;
-	if (S->iMax > W->iMAX) S->iMax = W->iMAX;
-	if (S->jMax > W->jMAX) S->jMax = W->jMAX;
-	if (S->kMax > W->kMAX) S->kMax = W->kMAX;
-	if (S->iMin < W->iMIN && W->xMinSur!=SYM) S->iMin = W->iMIN;
-	if (S->jMin < W->jMIN && W->yMinSur!=SYM) S->jMin = W->jMIN;
-	if (S->kMin < W->kMIN && W->zMinSur!=SYM) S->kMin = W->kMIN;
-	if (S->iMin <-W->iMAX && W->xMinSur==SYM) S->iMin =-W->iMAX;
-	if (S->jMin <-W->jMAX && W->yMinSur==SYM) S->jMin =-W->jMAX;
-	if (S->kMin <-W->kMAX && W->zMinSur==SYM) S->kMin =-W->kMAX;
-	S->iMIN = (S->iMin==S->iMax || !S->interpolate) ? S->iMin : MIN(S->iMin, W->itox(W, S->iMin)/W->dx);
-	S->jMIN = (S->jMin==S->jMax || !S->interpolate) ? S->jMin : MIN(S->jMin, W->jtoy(W, S->jMin)/W->dy);
-	S->kMIN = (S->kMin==S->kMax || !S->interpolate) ? S->kMin : MIN(S->kMin, W->ktoz(W, S->kMin)/W->dz);
-	S->iMAX = (S->iMin==S->iMax || !S->interpolate) ? S->iMax : MAX(S->iMax, W->itox(W, S->iMax)/W->dx);
-	S->jMAX = (S->jMin==S->jMax || !S->interpolate) ? S->jMax : MAX(S->jMax, W->jtoy(W, S->jMax)/W->dy);
-	S->kMAX = (S->kMin==S->kMax || !S->interpolate) ? S->kMax : MAX(S->kMax, W->ktoz(W, S->kMax)/W->dz);
+	slice S = calloc(1, sizeof *S);
+	const int graded = W->Res.nug.x.m>1 || W->Res.nug.y.m>1 || W->Res.nug.z.m>1;
+	if (graded) S->interpolate = resample;
+	const float box[3][2] = { { xMin, xMax }, { yMin, yMax }, { zMin, zMax } };
+	int r[3][4];
+	for (int a = 0; a < 3; a++) sliceAxis(W, a, box[a][0], box[a][1], graded, r[a]);
+	S->iMin = r[0][0], S->iMax = r[0][1], S->iMIN = r[0][2], S->iMAX = r[0][3];
+	S->jMin = r[1][0], S->jMax = r[1][1], S->jMIN = r[1][2], S->jMAX = r[1][3];
+	S->kMin = r[2][0], S->kMax = r[2][1], S->kMIN = r[2][2], S->kMAX = r[2][3];
 	S->iNUM = 1-S->iMIN+S->iMAX;
 	S->jNUM = 1-S->jMIN+S->jMAX;
 	S->kNUM = 1-S->kMIN+S->kMAX;
 	S->F = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
-	if (!W->CE->x || !W->CE->y || !W->CE->z || (S->iMin!=S->iMax && S->jMin!=S->jMax && S->kMin!=S->kMax)) return S;
-	float Max = 0;
+	const int flat = S->iMin == S->iMax || S->jMin == S->jMax || S->kMin == S->kMax;
+	if (!W->CE->x || !W->CE->y || !W->CE->z || !flat) return S;
 	S->C = makeField(S->iMIN, S->iMAX, S->jMIN, S->jMAX, S->kMIN, S->kMAX);
-	for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++)
-		if (Max < (S->C[i][j][k] = ContourRI(W, i, j, k))) Max = S->C[i][j][k];
-	if (Max) for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++)
-		S->C[i][j][k] = 0.5*S->C[i][j][k]/Max;
+	float top = 0;
+	for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++) {
+		const float v = S->C[i][j][k] = ContourRI(W, i, j, k);
+		if (top < v) top = v;
+	}
+	if (top) for (int i = S->iMIN; i <= S->iMAX; i++) for (int j = S->jMIN; j <= S->jMAX; j++) for (int k = S->kMIN; k <= S->kMAX; k++)
+		S->C[i][j][k] = 0.5 * S->C[i][j][k] / top;
 	return S;
 }
 

@@ -46,6 +46,11 @@ int alisgpu_synchronize(void);
 void *alisgpu_stream(void);
 /* Kernel launches issued so far by this library (for launch accounting). */
 unsigned long long alisgpu_launch_count(void);
+/* Fault injection for the error paths, on the host: the next n
+ * stream-ordered allocations of the engine (world, phaser and far-field
+ * buffers) report an out-of-memory failure without allocating (n = 0
+ * clears it).  Returns the previous count. */
+int alisgpu_inject_alloc_failures(int n);
 
 /* Per-kernel timing with CUDA events recorded around each launch on the
  * engine stream (off by default; adds two event records per launch).
@@ -336,16 +341,21 @@ int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_farfield_geom 
                           const double *kx, const double *ky, double *out);
 
 /* Scratch-free variant of alisgpu_farfield_sums (no counterpart in the
- * reference): same arguments and results, but it allocates nothing --
- * its device buffers (tables, test fields, partial sums) live in one
- * static device array of ALISGPU_FF_STATIC_BYTES.  For callers that must
- * not allocate: code that captures the step into a CUDA graph (cudaMalloc
- * and cudaFree are not stream-ordered, and cudaFree synchronises the
- * device), and serving loops whose device memory is fully admitted to
- * jobs.  A batch whose buffers exceed the array is refused with
- * ALISGPU_ERANGE (about 650 directions of a 256-cell-high phaser box fit).
- * The first call on a device sets the array up; make it before any
- * stream capture.  Overlapping calls race on the shared array. */
+ * reference): same arguments and results, but it allocates no device
+ * memory -- its device buffers (tables, test fields, partial sums) live in
+ * one static device array of ALISGPU_FF_STATIC_BYTES that every GPU
+ * loading the library holds until exit.  For callers that cannot allocate:
+ * a serving loop whose device memory is fully admitted to resident jobs
+ * (a cudaMalloc there fails, or takes memory promised to a job), and hosts
+ * whose allocator policy forbids device allocation after start-up.  The
+ * call is synchronous: it returns after its own copies and kernel have
+ * finished, also when it fails.  A batch whose buffers exceed the array
+ * is refused with ALISGPU_ERANGE (about 650 directions of a 256-cell-high
+ * phaser box fit); a frequency or table length the phaser's faces do not
+ * fit is refused with ALISGPU_EINVAL.  The first call on a device looks up
+ * the array's device address; make that first call before any stream
+ * capture.  Calls share the array, which keeps the last call's contents:
+ * calls that overlap on the GPU (several host threads) race. */
 #define ALISGPU_FF_STATIC_BYTES (16u << 20)
 int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alisgpu_farfield_geom *g, int nA,
                                  const double *T, int nk, const unsigned char *present,

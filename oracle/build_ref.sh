@@ -1,12 +1,23 @@
 #!/bin/sh
 # Build the ALiS reference library from its own sources into oracle/_ref/
 # (checker only: pins the oracle restatement; never linked into the
-# engine).  Needs the read-only reference checkout; HDF5 and libpng are
-# replaced by the stand-in headers in oracle/stubs.  FMA contraction is
-# disabled so results do not depend on the host ISA.
-#   usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# engine).  HDF5 and libpng are replaced by the stand-in headers in
+# oracle/stubs.  FMA contraction is disabled so results do not depend on
+# the host ISA.
+#
+# This recipe is the one place that knows where the read-only reference
+# checkout lies: the first argument, else $ALIS_REFERENCE, else the
+# checkout of the build container (/root/reference).
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   build oracle/_ref/libalis_ref.a
+#          oracle/build_ref.sh --locate           print the checkout's path (exit 1: none)
 set -e
-REF=${1:-/root/reference}
+if [ "$1" = "--locate" ]; then
+  REF=${ALIS_REFERENCE:-/root/reference}
+  [ -d "$REF/src" ] || exit 1
+  echo "$REF"
+  exit 0
+fi
+REF=${1:-${ALIS_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/src" ] || { echo "reference sources not found at $REF/src" >&2; exit 1; }

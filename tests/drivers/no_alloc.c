@@ -9,11 +9,18 @@
  * largest difference relative to the largest sum, checks that a batch too
  * large for the static array is refused with ALISGPU_ERANGE, and exits 0
  * when the results agree within 1e-12.
+ *
+ * With the argument "errors" it checks the error paths of both entry
+ * points instead, each without a launch: an injected allocation failure
+ * (ALISGPU_ENOMEM), a frequency outside the phaser's and test fields
+ * shorter than the phaser box (ALISGPU_EINVAL); and that a call after
+ * them still gives the same sums.
  */
 #include <alisgpu.h>
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 
 static unsigned long long rng = 0x9e3779b97f4a7c15ULL;
 static double uni(void)                     /* [-1, 1) */
@@ -24,8 +31,9 @@ static double uni(void)                     /* [-1, 1) */
 
 #define CHECK(call) do { int rc_ = (call); if (rc_) { fprintf(stderr, "%s failed (%d): %s\n", #call, rc_, alisgpu_last_error()); return 2; } } while (0)
 
-int main(void)
+int main(int argc, char **argv)
 {
+	const int errors = argc > 1 && !strcmp(argv[1], "errors");
 	CHECK(alisgpu_init());
 	const int N = 24, L = 4, U = 19, NF = 3, NA = 5;
 	alisgpu_geometry geo = { 0, N-1, 0, N-1, 0, N-1, 0, N-1, 0, N-1, 0, N-1, 0, {0, 0, 0, 0, 0, 0} };
@@ -82,6 +90,29 @@ int main(void)
 	for (int q = 0; q < NA * 6 * nk * 2; q++) T[q] = uni();
 	for (int q = 0; q < NA * 6; q++) pr[q] = 1;
 	for (int a = 0; a < NA; a++) kx[a] = 0.02 * uni(), ky[a] = 0.02 * uni();
+
+	if (errors) {
+		double a[NA * 12], b[NA * 12];
+		CHECK(alisgpu_farfield_sums(p, 1, &g, NA, T, nk, pr, kx, ky, a));
+		unsigned long long before = alisgpu_launch_count();
+		alisgpu_inject_alloc_failures(3);
+		int oom = alisgpu_farfield_sums(p, 1, &g, NA, T, nk, pr, kx, ky, b);
+		alisgpu_inject_alloc_failures(0);
+		int badF = alisgpu_farfield_sums(p, NF, &g, NA, T, nk, pr, kx, ky, b);
+		int badFs = alisgpu_farfield_sums_static(p, -1, &g, NA, T, nk, pr, kx, ky, b);
+		int shortT = alisgpu_farfield_sums(p, 1, &g, NA, T, nk - 3, pr, kx, ky, b);
+		int shortTs = alisgpu_farfield_sums_static(p, 1, &g, NA, T, nk - 3, pr, kx, ky, b);
+		int launched = alisgpu_launch_count() != before;
+		CHECK(alisgpu_farfield_sums(p, 1, &g, NA, T, nk, pr, kx, ky, b));
+		int same = !memcmp(a, b, sizeof a);
+		printf("enomem %d einval_f %d %d einval_nk %d %d launched %d same_after %d\n",
+		       oom == ALISGPU_ENOMEM, badF == ALISGPU_EINVAL, badFs == ALISGPU_EINVAL,
+		       shortT == ALISGPU_EINVAL, shortTs == ALISGPU_EINVAL, launched, same);
+		alisgpu_phaser_destroy(p);
+		alisgpu_world_destroy(w);
+		return oom == ALISGPU_ENOMEM && badF == ALISGPU_EINVAL && badFs == ALISGPU_EINVAL && shortT == ALISGPU_EINVAL &&
+		       shortTs == ALISGPU_EINVAL && !launched && same ? 0 : 1;
+	}
 
 	double ref[2][NA * 12], got[2][NA * 12];
 	for (int rep = 0; rep < 2; rep++) {

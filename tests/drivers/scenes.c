@@ -40,6 +40,9 @@
  *   lattice a dipole array (symmetry planes and periodic walls) with a
  *           phaser box over three periods: replicated phasers and the
  *           far field's lattice factor
+ *   farmaps the dipole world's far-field maps: farFieldProfile images of
+ *           all seven polarisations over two projections (one of them
+ *           logarithmic) and the farFieldTheta / farFieldPhi cuts
  */
 #include <alis.h>
 #include "dump.h"
@@ -618,6 +621,63 @@ static void sceneLattice(int steps)
 	farSamples(P + 1, "FL");
 }
 
+/* an image writer for farFieldProfile: dumps the image and the scale it
+ * was given under the name of the file it would have written */
+static void dumpImage(world W, slice S, float Max, char *F, char *filename, unsigned long int *cmap)
+{
+	(void)W, (void)F, (void)cmap;
+	char nm[160];
+	snprintf(nm, sizeof nm, "FP.%s", filename);
+	dumpField(nm, S->F, S->iMin, S->iMax, S->jMin, S->jMax, S->kMin, S->kMax);
+	snprintf(nm, sizeof nm, "FP.%s.max", filename);
+	dumpScalar(nm, Max);
+}
+
+/* the rows farFieldTheta / farFieldPhi wrote to <name>.txt, as an
+ * n x 4 array (angle, unpolarised, P, S) */
+static void dumpRows(const char *name, const char *path)
+{
+	fflush(NULL);
+	FILE *f = fopen(path, "r");
+	if (!f) { perror(path); exit(2); }
+	float v[360][4];
+	int n = 0;
+	while (n < 360 && fscanf(f, "%f %f %f %f", &v[n][0], &v[n][1], &v[n][2], &v[n][3]) == 4) n++;
+	fclose(f);
+	dumpHeader(name, DUMP_REAL, n, 4, 1);
+	for (int r = 0; r < n; r++) for (int c = 0; c < 4; c++) fwrite(&v[r][c], sizeof(float), 1, dumpFile);
+}
+
+/* the far-field maps: a dispersive ball and a silver bar lit by two
+ * dipoles in a CPML box; polarisation images over a cylindrical and an
+ * azimuthal (logarithmic) projection, and the theta and phi cuts */
+static void sceneFarMaps(int steps)
+{
+	float L = 100 * scale;
+	dom D = {{L}, {L}, {L}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PML}};
+	world W = createWorld(D, R, S, "");
+	object Ball1 = {Ball, {{-60, 20}, {-40, 40}, {-30, 50}}};
+	object Bar = {Box, {{20, 70}, {-20, 20}, {-80, -40}}};
+	matter Ag1 = {{4.0323}, {{9.1864, 0.021}}};
+	putObjects(W, n(1.5), Ball1, Ag1, Bar, Air);
+	pointDipole(W, Ez, 5, 0, 0, Band, 400, 800);
+	pointDipole(W, Hx, -20, 10, 30, Pulse, 500, 100, 0.5, 30);
+	phaser P = createPhasers(W, 400, 800, 100, -L+20, L-20, -L+20, L-20, -L+20, L-20);
+	run(W, P, steps);
+	dumpPhasers(P, "P");
+	farFieldProfile(W, P + 1, CylindericalMap, 16, 9, dumpImage, "cyl");
+	farFieldProfile(W, P + 2, AzimuthalMap, 12, 7, dumpImage, "azLog");
+	farFieldTheta(W, P + 1, 30, "theta");
+	farFieldPhi(W, P + 2, 60, "phi");
+	char path[1100];
+	snprintf(path, sizeof path, "%stheta.txt", W->ID);
+	dumpRows("FT.theta", path);
+	snprintf(path, sizeof path, "%sphi.txt", W->ID);
+	dumpRows("FT.phi", path);
+}
+
 int main(int argc, char **argv)
 {
 	if (argc < 3) {
@@ -649,6 +709,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "pec")) scenePEC(steps);
 	else if (!strcmp(s, "aniso")) sceneAniso(steps);
 	else if (!strcmp(s, "lattice")) sceneLattice(steps);
+	else if (!strcmp(s, "farmaps")) sceneFarMaps(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

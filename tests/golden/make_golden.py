@@ -1,8 +1,8 @@
 """Generate tests/golden/scenes.json from the reference itself.
 
 Builds the ALiS reference library from its own sources (oracle/build_ref.sh,
-needs the read-only reference checkout, default /root/reference or
-$ALIS_REFERENCE), links tests/drivers/scenes.c against it, runs every
+which locates the read-only reference checkout: $ALIS_REFERENCE or the
+build container's checkout), links tests/drivers/scenes.c against it, runs every
 parity case with one OpenMP thread, and records per dumped array its
 shape, dtype, SHA-256 of the bytes and a few sums.  The fixture pins the
 oracle restatement (tests/test_oracle_pin.py) and the GPU engine

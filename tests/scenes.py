@@ -45,16 +45,21 @@ CASES = [
     ("shapespt", 1, 40),
     ("shapesedge", 1, 40),
     ("contour", 1, 40),
+    # a PEC mirror under silver and a lossy (nk) film, symmetry planes,
+    # a single-wavelength phaser; an anisotropic Drude-Lorentz ball with
+    # the far-field intensities and ring fluxes; a dipole array whose
+    # phasers replicate over three periods, with the far field's lattice
+    # factor; the far-field images and angular cuts
+    ("pec", 1, 120),
+    ("aniso", 1, 120),
+    ("lattice", 1, 120),
+    ("farmaps", 1, 120),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 
-# pinned against the reference on the CPU only (tests/test_oracle_pin.py);
-# not yet part of the GPU parity run: a PEC mirror under silver and a
-# lossy (nk) film, symmetry planes, a single-wavelength phaser; an
-# anisotropic Drude-Lorentz ball with the far-field intensities and ring
-# fluxes; a dipole array whose phasers replicate over three periods, with
-# the far field's lattice factor
-PIN_CASES = CASES + [("pec", 1, 120), ("aniso", 1, 120), ("lattice", 1, 120)]
+# every parity case is also pinned against the reference on the CPU
+# (tests/test_oracle_pin.py)
+PIN_CASES = list(CASES)
 PIN_IDS = ["%s-x%d" % (c[0], c[1]) for c in PIN_CASES]
 
 
@@ -135,3 +140,22 @@ def max_rel(a, b):
         scale = np.abs(y).max()
         out[k] = float(np.abs(x - y).max() / scale) if scale > 0 else float(np.abs(x).max())
     return out
+
+
+def check_against_golden(dump, gold):
+    """Names of the arrays of a dump that are not byte-identical to the
+    golden digests (the reference's output); those must still agree in L1
+    and in sum within 1e-5.  Shapes, types and the set of names must be
+    the same."""
+    assert sorted(dump) == sorted(gold), sorted(set(dump) ^ set(gold))
+    inexact = []
+    for name, g in gold.items():
+        s = summary(dump[name])
+        assert s["shape"] == g["shape"] and s["dtype"] == g["dtype"], name
+        if s["sha256"] == g["sha256"]:
+            continue
+        inexact.append(name)
+        scale = max(g["l1"], 1e-30)
+        assert abs(s["l1"] - g["l1"]) <= 1e-5 * scale, (name, s["l1"], g["l1"])
+        assert abs(complex(*s["sum"]) - complex(*g["sum"])) <= 1e-5 * scale, name
+    return inexact

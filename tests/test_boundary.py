@@ -67,7 +67,13 @@ def test_product_does_not_contain_oracle():
         assert sym not in out
 
 
-EXAMPLES = sorted(glob.glob(os.path.join(os.environ.get("ALIS_REFERENCE", "/root/reference"), "examples", "*.c")))
+def _examples():
+    from alis_gb300 import build
+    ref = build.reference_root()
+    return sorted(glob.glob(os.path.join(ref, "examples", "*.c"))) if ref else []
+
+
+EXAMPLES = _examples()
 
 
 @pytest.mark.skipif(not EXAMPLES, reason="reference examples not present on this machine")

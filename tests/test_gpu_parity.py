@@ -18,7 +18,41 @@ import pytest
 import scenes
 
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scenes.json")))
-FAR = ("F.ffP", "F.ffS")
+# far-field outputs: FP64 sums on the GPU, compared with the oracle's FP64
+# restatement (amplitudes F.ff* / FL.ff*, intensities and ring fluxes FA.*,
+# farFieldProfile images FP.*, farFieldTheta / farFieldPhi rows FT.*)
+FAR = ("F.", "FA.", "FL.ff", "FP.", "FT.")
+
+
+def _linear(key, a):
+    """A log10 image back to intensities (log10 of 0 is -inf: 0)."""
+    a = a.astype(np.complex128).reshape(-1)
+    if key.startswith("FP.") and "Log" in key and not key.endswith(".max"):
+        re = a.real
+        a = np.where(np.isfinite(re), np.power(10.0, np.where(np.isfinite(re), re, 0.0)), 0.0).astype(np.complex128)
+    return a
+
+
+def check_far_field(gpu, wide):
+    """Every far-field output within 1e-5 relative of the FP64 oracle, or of
+    1e-6 x the largest sample of its group for values whose exact value is
+    near zero.  A group is one image or one cut; the scalars of a scene
+    form one group.  The cuts are printed with 6 significant digits
+    (writeRow's %g), so they may differ by one unit in the last digit
+    more: 2.1e-5."""
+    far = sorted(k for k in gpu if k.startswith(FAR))
+    assert sorted(k for k in wide if k.startswith(FAR)) == far
+    scalars = [k for k in far if gpu[k].size == 1]
+    top_scalar = max((abs(_linear(k, wide[k])[0]) for k in scalars), default=0.0)
+    for k in far:
+        x, y = _linear(k, gpu[k]), _linear(k, wide[k])
+        finite = np.isfinite(y)
+        assert np.array_equal(np.isfinite(x), finite), k
+        top = top_scalar if y.size == 1 else float(np.abs(y[finite]).max(initial=0.0))
+        rel = 2.1e-5 if k.startswith("FT.") else 1e-5
+        tol = rel * np.maximum(np.maximum(np.abs(y[finite]), 1e-6 * top), 1e-30)
+        err = np.abs(x[finite] - y[finite])
+        assert (err <= tol).all(), (k, float((err / tol).max()))
 
 
 @pytest.mark.gpu
@@ -29,33 +63,27 @@ def test_engine_bit_identical_to_oracle(scene, scale, steps):
     near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
     bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith(FAR)})
     assert not bad, "differs from the oracle: %s" % bad[:10]
-    far = [k for k in gpu if k.startswith(FAR)]
-    if far:
-        # 1e-5 relative to the value, or to 1e-6 of the scene's largest
-        # far-field sample for directions whose exact value is near zero
-        wide = scenes.run("oracle", scene, scale, steps, env={"ALIS_ORACLE_FF64": "1"})
-        top = max(abs(complex(wide[k].reshape(-1)[0])) for k in far)
-        for k in far:
-            x, y = complex(gpu[k].reshape(-1)[0]), complex(wide[k].reshape(-1)[0])
-            assert abs(x - y) <= 1e-5 * max(abs(y), 1e-6 * top, 1e-30), (k, x, y)
+    if any(k.startswith(FAR) for k in gpu):
+        check_far_field(gpu, scenes.run("oracle", scene, scale, steps, env={"ALIS_ORACLE_FF64": "1"}))
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scene,scale,steps", scenes.CASES[:2], ids=scenes.IDS[:2])
+@pytest.mark.parametrize("scene,scale,steps", scenes.CASES, ids=scenes.IDS)
 def test_engine_matches_reference_fixture(scene, scale, steps):
+    """The engine against the reference's own output, recorded as golden
+    digests on an x86-64 host: every near-field array identical byte for
+    byte or, where the host C library's float transcendentals (waveforms,
+    phase factors: computed on this host) round differently in the last
+    bit, within 1e-5 in L1 and in sum.  The byte-identical share is
+    printed; the eps^-1 maps, which no transcendental function touches,
+    must all be identical."""
     gpu = scenes.run("engine", scene, scale, steps)
-    gold = GOLDEN["%s/%d/%d" % (scene, scale, steps)]
-    exact = 0
-    for name, g in gold.items():
-        if name.startswith(FAR):
-            continue
-        s = scenes.summary(gpu[name])
-        if s["sha256"] == g["sha256"]:
-            exact += 1
-            continue
-        scale_ = max(g["l1"], 1e-30)
-        assert abs(s["l1"] - g["l1"]) <= 1e-5 * scale_, (name, s["l1"], g["l1"])
-    assert exact > 0
+    gold = {k: v for k, v in GOLDEN["%s/%d/%d" % (scene, scale, steps)].items() if not k.startswith(FAR)}
+    near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
+    inexact = scenes.check_against_golden(near, gold)
+    print("%s: %d of %d arrays byte-identical to the reference" % (scene, len(gold) - len(inexact), len(gold)))
+    static = [k for k in inexact if k.split(".")[1].startswith("CE")]
+    assert not static, static
 
 
 def _rel_l1(a, b, keys):

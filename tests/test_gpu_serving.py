@@ -4,8 +4,10 @@ photonic-crystal k-point runs with complex fields -- admitted by device
 footprint and stepped in turn, each world on streams of its own so that
 their work overlaps on the device.  Every request's result (its outgoing
 phaser flux summed over frequencies and k-points) must be bit-identical
-in the mix, run one after another on the default streams, and run alone.
-Prints the throughput of the served and the sequential runs and the
+in the mix, run one after another on the default streams, and run alone,
+and the same as the oracle's result for that request: the request loop
+built against the oracle runs the same seeded stream one request after
+another on the host cores.  Prints the throughput of the served and the sequential runs and the
 served latency percentiles."""
 import json
 import os
@@ -14,6 +16,13 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _oracle_serve():
+    from alis_gb300 import build
+    build.build_oracle()
+    return build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                              os.path.join(ROOT, "tests", "drivers", "bin", "serve_oracle"), "oracle", extra=["-lm"])
 
 
 def _run(exe, args, env=None):
@@ -50,6 +59,11 @@ def test_served_results_equal_alone_and_sequential():
     for kind, q in sorted(kinds.items()):
         alone, _ = _run(exe, ["alone", n, 2000, seed, "small", q])
         assert alone[q] == served[q], (q, alone[q], served[q])
+    # the oracle, the same stream one request after another
+    oracle, _ = _run(_oracle_serve(), ["sequential", n, 2000, seed, "small"])
+    assert len(oracle) == n
+    for q in range(n):
+        assert oracle[q] == served[q], (q, oracle[q], served[q])
     print("served %.2f Gcell/s (p50 %.1f ms, p99 %.1f ms), sequential %.2f Gcell/s" %
           (s1["gcell_per_s"], s1["latency_ms"]["p50"], s1["latency_ms"]["p99"], s2["gcell_per_s"]))
 
@@ -57,7 +71,8 @@ def test_served_results_equal_alone_and_sequential():
 @pytest.mark.gpu
 def test_served_unit_cell_sweep_equals_sequential():
     """The metasurface sweep mix (periodic unit cells with a TFSF pulse and
-    a transmission plane), shortened to 400 steps per cell."""
+    a transmission plane), shortened to 400 steps per cell: served,
+    sequential and the oracle's results identical per request."""
     from alis_gb300 import build
     build.build_engine()
     exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
@@ -67,4 +82,6 @@ def test_served_unit_cell_sweep_equals_sequential():
     seq, s2 = _run(exe, ["sequential", 12, 2000, 7, "sweep"], env)
     assert len(served) == 12 and served == seq
     assert any(int(v[1], 16) for v in served.values())
+    oracle, _ = _run(_oracle_serve(), ["sequential", 12, 2000, 7, "sweep"], env)
+    assert oracle == served
     print("sweep: served %.2f Gcell/s, sequential %.2f Gcell/s" % (s1["gcell_per_s"], s2["gcell_per_s"]))

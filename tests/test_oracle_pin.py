@@ -23,25 +23,10 @@ GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "scene
 EXACT_HOST = platform.machine() == "x86_64"
 
 
-def check_against_golden(dump, gold):
-    assert sorted(dump) == sorted(gold), sorted(set(dump) ^ set(gold))
-    inexact = []
-    for name, g in gold.items():
-        s = scenes.summary(dump[name])
-        assert s["shape"] == g["shape"] and s["dtype"] == g["dtype"], name
-        if s["sha256"] == g["sha256"]:
-            continue
-        inexact.append(name)
-        scale = max(g["l1"], 1e-30)
-        assert abs(s["l1"] - g["l1"]) <= 1e-5 * scale, (name, s["l1"], g["l1"])
-        assert abs(complex(*s["sum"]) - complex(*g["sum"])) <= 1e-5 * scale, name
-    return inexact
-
-
 @pytest.mark.parametrize("scene,scale,steps", scenes.PIN_CASES, ids=scenes.PIN_IDS)
 def test_oracle_matches_reference(scene, scale, steps):
     dump = scenes.run("oracle", scene, scale, steps)
-    inexact = check_against_golden(dump, GOLDEN["%s/%d/%d" % (scene, scale, steps)])
+    inexact = scenes.check_against_golden(dump, GOLDEN["%s/%d/%d" % (scene, scale, steps)])
     if EXACT_HOST:
         assert not inexact, "not bit-identical: %s" % inexact[:10]
 
@@ -53,7 +38,7 @@ def test_reference_build_agrees_with_fixture():
         pytest.skip("reference sources not present on this machine")
     scene, scale, steps = scenes.CASES[1]
     dump = scenes.run("reference", scene, scale, steps)
-    inexact = check_against_golden(dump, GOLDEN["%s/%d/%d" % (scene, scale, steps)])
+    inexact = scenes.check_against_golden(dump, GOLDEN["%s/%d/%d" % (scene, scale, steps)])
     if EXACT_HOST:
         assert not inexact
 
