@@ -17,6 +17,7 @@
 #include <mutex>
 #include <vector>
 #include "common.cuh"
+#include "batch.cuh"
 
 extern "C" const float2 *alisgpu__phaser_acc(alisgpu_phaser *p, int f, int face, long long *cells);
 extern "C" int alisgpu__phaser_nface(alisgpu_phaser *p);
@@ -256,6 +257,7 @@ extern "C" int alisgpu_farfield_sums(alisgpu_phaser *p, int f, const alisgpu_far
                                      const double *T, int nk, const unsigned char *present,
                                      const double *kx, const double *ky, double *out)
 {
+	ALIS_BATCH_GUARD();
 	if (!p || !g || nA < 0 || nk < 0 || !T || !present || !kx || !ky || !out)
 		return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums: bad argument");
 	if (!nA) return ALISGPU_OK;
@@ -355,6 +357,7 @@ extern "C" int alisgpu_farfield_sums_static(alisgpu_phaser *p, int f, const alis
                                             const double *T, int nk, const unsigned char *present,
                                             const double *kx, const double *ky, double *out)
 {
+	ALIS_BATCH_GUARD();
 	if (!p || !g || nA < 0 || !T || !present || !kx || !ky || !out || nk < 0)
 		return alisgpu__fail(ALISGPU_EINVAL, "farfield_sums_static: bad argument");
 	if (!nA) return ALISGPU_OK;

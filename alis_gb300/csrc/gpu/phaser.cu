@@ -21,6 +21,7 @@
 #include <mutex>
 #include <vector>
 #include "common.cuh"
+#include "batch.cuh"
 
 struct alisgpu_phaser {
 	alisgpu_world *w;
@@ -60,9 +61,8 @@ extern "C" cudaStream_t alisgpu__gather_begin(alisgpu_world *w, const int (*box)
 extern "C" void alisgpu__bind(alisgpu_world *w);
 extern "C" int alisgpu__gather_end(alisgpu_world *w, cudaStream_t st);
 
-__global__ void k_phaser_gather(const GatherParams P)
+__device__ __forceinline__ void gatherCell(const GatherParams &P, long long t)
 {
-	long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= P.start[P.nface]) return;
 	int f = 0;
 	while (t >= P.start[f + 1]) f++;
@@ -84,6 +84,11 @@ __global__ void k_phaser_gather(const GatherParams P)
 	reinterpret_cast<float4 *>(P.out)[t] = v;
 }
 
+__global__ void k_phaser_gather(const GatherParams P)
+{
+	gatherCell(P, (long long)blockIdx.x * blockDim.x + threadIdx.x);
+}
+
 // fl(a + p * 0.5) with the rounding of the reference's double expression
 // (float)((double)a + (double)p * 0.5): p * 0.5 is exact in double and
 // the double sum of two floats rounds innocuously to float, so the result
@@ -100,18 +105,17 @@ __device__ __forceinline__ float addHalf(float a, float p)
 
 // thread = one (face cell, component); loops over a chunk of frequencies
 template <bool KAHAN>
-__global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
-                                                                long long n4, int nfreq, int steps)
+__device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
+                                           long long n4, int nfreq, int steps, long long bx, int by, float2 *sph)
 {
-	extern __shared__ float2 sph[];                 // [steps][FLUSH_FREQ][2]
-	const int f0 = blockIdx.y * FLUSH_FREQ;
+	const int f0 = by * FLUSH_FREQ;
 	const int nf = min(FLUSH_FREQ, nfreq - f0);
 	for (int q = threadIdx.x; q < steps * FLUSH_FREQ * 2; q += blockDim.x) {
 		int s = q / (FLUSH_FREQ * 2), r = q % (FLUSH_FREQ * 2), ff = r / 2, h = r % 2;
 		sph[q] = ff < nf ? phase[((long long)s * nfreq + f0 + ff) * 2 + h] : make_float2(0, 0);
 	}
 	__syncthreads();
-	long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	long long t = bx * blockDim.x + threadIdx.x;
 	if (t >= n4) return;
 	const bool isH = (t & 3) >= 2;
 	float2 a[FLUSH_FREQ], cc[FLUSH_FREQ];
@@ -169,6 +173,56 @@ __global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf
 			if (KAHAN) comp[(long long)(f0 + ff) * n4 + t] = cc[ff];
 		}
 	}
+}
+
+template <bool KAHAN>
+__global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
+                                                                long long n4, int nfreq, int steps)
+{
+	extern __shared__ float2 sph[];                 // [steps][FLUSH_FREQ][2]
+	flushBlock<KAHAN>(buf, acc, comp, phase, n4, nfreq, steps, blockIdx.x, blockIdx.y, sph);
+}
+
+// ---- batched phaser work (batch.cuh): every recorded phaser's flush in
+// one launch, then every phaser's gather in one launch ----
+struct FlushItem {
+	const float *buf;
+	float2 *acc, *comp;
+	const float2 *phase;
+	long long n4;
+	int nfreq, steps, kahan;
+	int bx, blocks;                       // cell blocks; blocks of the item (bx x frequency groups)
+	int start;                            // its first block in the launch
+};
+struct GatherItem {
+	const GatherParams *G;
+	long long start;                      // its first thread in the launch
+};
+
+__global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush_batch(const FlushItem *T, int n)
+{
+	extern __shared__ float2 sph[];
+	int lo = 0, hi = n - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (T[mid].start <= (int)blockIdx.x) lo = mid; else hi = mid - 1;
+	}
+	const FlushItem &F = T[lo];
+	const int b = (int)blockIdx.x - F.start;
+	if (F.kahan) flushBlock<true>(F.buf, F.acc, F.comp, F.phase, F.n4, F.nfreq, F.steps, b % F.bx, b / F.bx, sph);
+	else flushBlock<false>(F.buf, F.acc, F.comp, F.phase, F.n4, F.nfreq, F.steps, b % F.bx, b / F.bx, sph);
+}
+
+__global__ void k_phaser_gather_batch(const GatherItem *T, int n, long long total)
+{
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= total) return;
+	int lo = 0, hi = n - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (T[mid].start <= t) lo = mid; else hi = mid - 1;
+	}
+	gatherCell(*T[lo].G, t - T[lo].start);
 }
 
 extern "C" int alisgpu_phaser_create(alisgpu_world *w, int nfreq, int nface, const alisgpu_face *faces, int ring, int kahan, alisgpu_phaser **out)
@@ -229,6 +283,7 @@ static void pinnedRelease(float2 *b, size_t n)
 
 extern "C" int alisgpu_phaser_destroy(alisgpu_phaser *p)
 {
+	ALIS_BATCH_GUARD();
 	if (p) alisgpu__bind(p->w);
 	if (!p) return ALISGPU_OK;
 	cudaStreamSynchronize(alisgpu__stream());
@@ -243,11 +298,10 @@ extern "C" int alisgpu_phaser_destroy(alisgpu_phaser *p)
 	return ALISGPU_OK;
 }
 
-extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
+// the phase factors of the buffered steps to the device, through pinned
+// staging (two buffers in turn)
+static int uploadPhases(alisgpu_phaser *p)
 {
-	if (p) alisgpu__bind(p->w);
-	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_flush: null phaser");
-	if (!p->used || !p->cells) { p->used = 0; p->hostPhase.clear(); return ALISGPU_OK; }
 	cudaStream_t st = alisgpu__stream();
 	const size_t nph = p->hostPhase.size();
 	if (nph > p->pinnedCap) {
@@ -272,6 +326,19 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 	memcpy(p->pinned[b], p->hostPhase.data(), nph * sizeof(float2));
 	ALIS_CUDA(cudaMemcpyAsync(p->phase, p->pinned[b], nph * sizeof(float2), cudaMemcpyHostToDevice, st));
 	ALIS_CUDA(cudaEventRecord(p->pinnedFree[b], st));
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
+{
+	if (p) alisgpu__bind(p->w);
+	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_flush: null phaser");
+	if (!p->used || !p->cells) { p->used = 0; p->hostPhase.clear(); return ALISGPU_OK; }
+	// a batch's recorded gathers into the ring come first
+	int rc = alisgpu__batch_flush();
+	if (rc) return rc;
+	if ((rc = uploadPhases(p))) return rc;
+	cudaStream_t st = alisgpu__stream();
 	long long n4 = p->cells * 4;
 	dim3 grid((unsigned)((n4 + FLUSH_THREADS - 1) / FLUSH_THREADS), (p->nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ);
 	size_t smem = (size_t)p->used * FLUSH_FREQ * 2 * sizeof(float2);
@@ -286,10 +353,122 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 	return ALISGPU_OK;
 }
 
+static thread_local std::vector<FlushItem> gBatchFlush;
+static thread_local std::vector<GatherParams> gBatchGather;
+
+extern "C" void alisgpu__phaser_batch_clear(void)
+{
+	gBatchFlush.clear();
+	gBatchGather.clear();
+}
+
+// the face samples of the current fields into ring slot `used`
+static void gatherParams(alisgpu_phaser *p, GatherParams &G)
+{
+	memset(&G, 0, sizeof G);
+	alisgpu__world_fields(p->w, 0, G.E, G.H, &G.L);
+	G.nface = p->nface;
+	for (int f = 0; f <= p->nface; f++) G.start[f] = p->faceStart[f];
+	for (int f = 0; f < p->nface; f++) {
+		const alisgpu_face &a = p->faces[f];
+		int b[7] = { a.axis, a.i0, a.i1, a.j0, a.j1, a.k0, a.k1 };
+		memcpy(G.box[f], b, sizeof b);
+	}
+	G.out = p->buf + (size_t)p->used * p->cells * 4;
+}
+
+// a phaser's step in the open batch group: its ring flush when the ring
+// is full, then its gather
+static int recordPhaser(alisgpu_phaser *p, const float *phaseE, const float *phaseH)
+{
+	if (p->used == p->ring) {
+		if (p->cells) {
+			int rc = uploadPhases(p);
+			if (rc) return rc;
+			FlushItem F;
+			memset(&F, 0, sizeof F);
+			F.buf = p->buf, F.acc = p->acc, F.comp = p->comp, F.phase = p->phase;
+			F.n4 = p->cells * 4, F.nfreq = p->nfreq, F.steps = p->used, F.kahan = p->kahan;
+			F.bx = (int)((F.n4 + FLUSH_THREADS - 1) / FLUSH_THREADS);
+			F.blocks = F.bx * ((p->nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ);
+			if (F.blocks > 0) gBatchFlush.push_back(F);
+		}
+		p->used = 0;
+		p->hostPhase.clear();
+	}
+	if (p->cells) {
+		GatherParams G;
+		gatherParams(p, G);
+		gBatchGather.push_back(G);
+	}
+	for (int f = 0; f < p->nfreq; f++) {
+		p->hostPhase.push_back(make_float2(phaseE[2 * f], phaseE[2 * f + 1]));
+		p->hostPhase.push_back(make_float2(phaseH[2 * f], phaseH[2 * f + 1]));
+	}
+	p->used++;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu__phaser_batch_launch(void)
+{
+	auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+	std::vector<FlushItem> &F = gBatchFlush;
+	std::vector<GatherParams> &G = gBatchGather;
+	if (F.empty() && G.empty()) return ALISGPU_OK;
+	int blocks = 0, steps = 0;
+	for (FlushItem &f : F) {
+		f.start = blocks;
+		if ((long long)blocks + f.blocks >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: flush blocks exceed 2^31");
+		blocks += f.blocks;
+		steps = std::max(steps, f.steps);
+	}
+	const size_t oF = 0, oG = al(F.size() * sizeof(FlushItem)), oI = oG + al(G.size() * sizeof(GatherParams));
+	const size_t total = oI + G.size() * sizeof(GatherItem);
+	void *hv = 0;
+	const void *dv = 0;
+	int rc = alisgpu__blob_take(total, &hv, &dv);
+	if (rc) return rc;
+	unsigned char *h = (unsigned char *)hv;
+	const unsigned char *d = (const unsigned char *)dv;
+	if (!F.empty()) memcpy(h + oF, F.data(), F.size() * sizeof(FlushItem));
+	if (!G.empty()) memcpy(h + oG, G.data(), G.size() * sizeof(GatherParams));
+	long long threads = 0;
+	GatherItem *items = (GatherItem *)(h + oI);
+	for (size_t q = 0; q < G.size(); q++) {
+		items[q].G = (const GatherParams *)(d + oG) + q;
+		items[q].start = threads;
+		threads += G[q].start[G[q].nface];
+	}
+	if ((rc = alisgpu__blob_send())) return rc;
+	cudaStream_t st = alisgpu__stream();
+	if (blocks) {
+		const size_t smem = (size_t)steps * FLUSH_FREQ * 2 * sizeof(float2);
+		int slot = alisgpu__prof_start();
+		k_phaser_flush_batch<<<(unsigned)blocks, FLUSH_THREADS, smem, st>>>((const FlushItem *)(d + oF), (int)F.size());
+		alisgpu__prof_stop(slot, ALISGPU_K_FLUSH);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	if (threads) {
+		int slot = alisgpu__prof_start();
+		k_phaser_gather_batch<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>((const GatherItem *)(d + oI), (int)G.size(), threads);
+		alisgpu__prof_stop(slot, ALISGPU_K_GATHER);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	F.clear(), G.clear();
+	return alisgpu__blob_done();
+}
+
 extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, const float *phaseH)
 {
 	if (p) alisgpu__bind(p->w);
 	if (!p || !phaseE || !phaseH) return alisgpu__fail(ALISGPU_EINVAL, "phaser_record: bad argument");
+	{
+		const int rec = alisgpu__batch_enter(BATCH_PHASER, p->w);
+		if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "phaser_record: batch launch failed");
+		if (rec) return recordPhaser(p, phaseE, phaseH);
+	}
 	if (p->used == p->ring) {
 		int rc = alisgpu_phaser_flush(p);
 		if (rc) return rc;
@@ -334,6 +513,7 @@ extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, con
 
 extern "C" int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q, float *host)
 {
+	ALIS_BATCH_GUARD();
 	if (p) alisgpu__bind(p->w);
 	if (!p || !host || f < 0 || f >= p->nfreq || face < 0 || face >= p->nface || q < 0 || q > 3)
 		return alisgpu__fail(ALISGPU_EINVAL, "phaser_download: bad argument");
@@ -347,6 +527,7 @@ extern "C" int alisgpu_phaser_download(alisgpu_phaser *p, int f, int face, int q
 
 extern "C" int alisgpu_phaser_zero(alisgpu_phaser *p)
 {
+	ALIS_BATCH_GUARD();
 	if (p) alisgpu__bind(p->w);
 	if (!p) return alisgpu__fail(ALISGPU_EINVAL, "phaser_zero: null phaser");
 	p->used = 0;
@@ -453,6 +634,7 @@ __global__ void k_phaser_flux_outer(const FluxParams P)
 extern "C" int alisgpu_phaser_face_flux(alisgpu_phaser *p, const float *const wE[3], const float *const wH[3],
                                         const int lo[3], const int hi[3], float *out)
 {
+	ALIS_BATCH_GUARD();
 	if (p) alisgpu__bind(p->w);
 	if (!p || !wE || !wH || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "phaser_face_flux: bad argument");
 	int rc = alisgpu_phaser_flush(p);

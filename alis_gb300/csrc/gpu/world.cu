@@ -23,6 +23,7 @@
 #include <mutex>
 #include <cooperative_groups.h>
 #include "common.cuh"
+#include "batch.cuh"
 namespace cg = cooperative_groups;
 
 // ---------------------------------------------------------------------
@@ -220,6 +221,7 @@ extern "C" int alisgpu_profile_read(int kind, double *ms, unsigned long long *la
 
 extern "C" int alisgpu_synchronize(void)
 {
+	ALIS_BATCH_GUARD();
 	if (!gInit) return ALISGPU_OK;
 	std::lock_guard<std::mutex> lock(gGroupsLock);
 	for (size_t q = 0; q <= gOwnGroups.size(); q++) {
@@ -269,8 +271,8 @@ struct alisgpu_world {
 	// ALIS_TUNE_STEPS launches, then fixed
 	struct TyTuner {
 		int choice = -1, seen = 0;
-		cudaEvent_t a[9], b[9];
-		int variant[9];
+		cudaEvent_t a[15], b[15];
+		int variant[15];
 	} tune[2];
 	// an auxiliary world's half step waiting to run inside its parent's
 	// launch of the same field
@@ -288,6 +290,13 @@ struct alisgpu_world {
 	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
 	unsigned char *matIdx;                 // eps^-1 triple index per cell (few distinct triples)
 	float4 *matTab;
+	// batched stepping: device copies of the half-step parameters per field
+	// and m, of a one-block step, of the source patches and of the ghost
+	// copies; the values of an auxiliary step staged for the parent's
+	// batched launch; the batch group the world last joined
+	ParamSlot bP[2][2], bS[2], bSrc[2], bG[2];
+	std::vector<float> stagedVals[2];
+	unsigned long long batchStamp;
 };
 
 static inline void bindWorld(const alisgpu_world *w)
@@ -384,6 +393,7 @@ static void freeObjects(alisgpu_world *w)
 
 extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w) return ALISGPU_OK;
@@ -484,6 +494,7 @@ extern "C" void *alisgpu_world_stream(const alisgpu_world *w)
 
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	gOps++;
 	fullJoin();
@@ -523,6 +534,7 @@ static int upload1D(alisgpu_world *w, float **dst, const float *src, int n)
 
 extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *const dtd[3], const float *const cpml[9])
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w || grid < 0 || grid > 1 || !dtd) return alisgpu__fail(ALISGPU_EINVAL, "set_line_tables: bad argument");
@@ -535,6 +547,7 @@ extern "C" int alisgpu_set_line_tables(alisgpu_world *w, int grid, const float *
 
 extern "C" int alisgpu_set_spacing(alisgpu_world *w, const float *const dE[3], const float *const dH[3])
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w || !dE || !dH) return alisgpu__fail(ALISGPU_EINVAL, "set_spacing: bad argument");
@@ -562,6 +575,7 @@ static int uploadBoxToLayout(alisgpu_world *w, float *dev, const float *host, in
 
 extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *cy, const float *cz)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "set_eps: null world");
@@ -634,6 +648,7 @@ static bool preciseConduction()
 
 extern "C" int alisgpu_set_dispersive(alisgpu_world *w, int n, const alisgpu_dispersive *objs)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w || n < 0 || (n && !objs)) return alisgpu__fail(ALISGPU_EINVAL, "set_dispersive: bad argument");
@@ -694,6 +709,7 @@ static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
 
 extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (w) {
@@ -711,6 +727,7 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 
 extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp, const float *host)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	gOps++;
 	fullJoin();
@@ -737,6 +754,7 @@ __global__ void k_current_gather(const CurGather P)
 
 extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *host)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w || !host || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_currents_download: bad argument");
@@ -769,6 +787,7 @@ extern "C" int alisgpu_object_currents_download(alisgpu_world *w, int n, float *
 
 extern "C" int alisgpu_current_download(alisgpu_world *w, int n, int m, int p, int comp, int isK, float *host)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	fullJoin();
 	if (!w || !host || n < 0 || n >= (int)w->objs.size() || m < 0 || m > w->g.complexField || comp < 0 || comp > 2)
@@ -1039,7 +1058,6 @@ __device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int
 // steps (32 x 4 measured best on the 256^3 dispersive world).
 #define ALIS_TY_CHOICES 3
 static const int kTyChoice[ALIS_TY_CHOICES] = { 2, 4, 8 };
-#define ALIS_TY_DEFAULT 1
 #define STEP_MINB(TY) (2048 / (TX * (TY)))
 // The lean tiers for NC cells k, k + TX, ... of one row, all in range and
 // none of them hard: the loads of every cell first, then the updates, so
@@ -1202,7 +1220,8 @@ struct SourceParams {
 	float v[ALIS_MAXSRCV];
 };
 
-__global__ void k_sources(const SourceParams P)
+// the patches of one world by one block; vals: the values (null: those of P)
+__device__ __forceinline__ void sourcesBlock(const SourceParams &P, const float *vals)
 {
 	for (int q = 0; q < P.n; q++) {
 		const alisgpu_source_patch &s = P.p[q];
@@ -1211,7 +1230,7 @@ __global__ void k_sources(const SourceParams P)
 		float *F = P.F[s.m][s.comp];
 		for (int t = threadIdx.x; t < cells; t += blockDim.x) {
 			int kk = t % nk, jj = (t / nk) % nj, ii = t / (nk * nj);
-			float v = P.vdev ? P.vdev[s.voff + t] : P.v[s.voff + t];
+			float v = vals ? vals[s.voff + t] : P.vdev ? P.vdev[s.voff + t] : P.v[s.voff + t];
 			int i = s.i0 + ii, j = s.j0 + jj, k = s.k0 + kk;
 			if (i < P.L.i0 || i >= P.L.i0 + P.L.ni || j < P.L.j0 || j >= P.L.j0 + P.L.nj || k < P.L.k0 || k >= P.L.k0 + P.L.nk) {
 				atomicOr(P.err, 4u);
@@ -1221,6 +1240,11 @@ __global__ void k_sources(const SourceParams P)
 		}
 		__syncthreads();
 	}
+}
+
+__global__ void k_sources(const SourceParams P)
+{
+	sourcesBlock(P, 0);
 }
 
 // one group of independent ghost copies (reference src/update.c:182-191)
@@ -1329,9 +1353,8 @@ __device__ __forceinline__ bool inCopy(const alisgpu_ghost_copy &c, int i, int j
 }
 
 template <bool CHECK>
-__global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ GhostLevels P, unsigned int *flag)
+__device__ __forceinline__ void ghostChainCell(const GhostLevels &P, int t, unsigned int *flag)
 {
-	const int t = blockIdx.x * blockDim.x + threadIdx.x;
 	if (t >= P.start[P.n]) return;
 	int q = 0;
 	while (t >= P.start[q + 1]) q++;
@@ -1392,6 +1415,12 @@ __global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ Gho
 	}
 }
 
+template <bool CHECK>
+__global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ GhostLevels P, unsigned int *flag)
+{
+	ghostChainCell<CHECK>(P, blockIdx.x * blockDim.x + threadIdx.x, flag);
+}
+
 // Small worlds (the TFSF auxiliary columns, tiny test worlds): the whole
 // half step -- every cell of every m, then the source patches in list
 // order, then the ghost copies one after another -- in one block, with a
@@ -1418,7 +1447,7 @@ struct SmallStepParams {
 #define SMALL_THREADS 128
 // the whole half step of a small world by the threads tid = 0..nth-1 of one block
 template <int ALT>
-__device__ __noinline__ void smallStepBlock(const SmallStepParams &S, int tid, int nth)
+__device__ __noinline__ void smallStepBlock(const SmallStepParams &S, int tid, int nth, const float *vals = 0)
 {
 	const Layout &L = S.P[0].L;
 	for (int m = 0; m < S.nm; m++) {
@@ -1440,7 +1469,7 @@ __device__ __noinline__ void smallStepBlock(const SmallStepParams &S, int tid, i
 				atomicOr(S.P[0].err, 4u);
 				continue;
 			}
-			F[L.at(i, j, k)] += S.vdev ? S.vdev[p.voff + t] : S.v[p.voff + t];
+			F[L.at(i, j, k)] += vals ? vals[p.voff + t] : S.vdev ? S.vdev[p.voff + t] : S.v[p.voff + t];
 		}
 		__syncthreads();
 	}
@@ -1479,10 +1508,13 @@ static void freeStaged(alisgpu_world *w)
 
 // an auxiliary step handed over for a launch that did not take it runs on its own
 template <int ALT> __global__ void k_small_step(const __grid_constant__ SmallStepParams S);
+static int recordStaged(alisgpu_world *aux, int field);
+static bool batchRecording(void);
 static int runStagedAux(const alisgpu_half_step *s, int field)
 {
 	alisgpu_world *aux = s->ntfsf == 1 ? s->tfsf[0].aux : 0;
 	if (!aux || !aux->stagedValid[field]) return ALISGPU_OK;
+	if (batchRecording() && !aux->group) return recordStaged(aux, field);
 	aux->stagedValid[field] = false;
 	if (field == 0) k_small_step<1><<<1, SMALL_THREADS, 0, gStream>>>(*aux->staged[field]);
 	else k_small_step<-1><<<1, SMALL_THREADS, 0, gStream>>>(*aux->staged[field]);
@@ -1519,6 +1551,206 @@ __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const 
 	halfStepBlock<ALT, TY>(F.P, (int)blockIdx.z - 1);
 }
 
+// ---------------------------------------------------------------------
+// Marching form of the half step.  A warp owns a tile of 32 cells along k
+// and RJ rows along j and walks a chunk of i planes in the direction in
+// which the i neighbour it reads was the plane before: E (neighbour
+// i + 1) walks down, H (neighbour i - 1) walks up.  The i neighbour's two
+// components stay in registers from the plane before, the j neighbours of
+// all but the edge row are the next row's registers, and the line tables
+// and class bits of j and k are read once per tile.  So a plain cell
+// loads its three G components, its three F components and its
+// material index from DRAM, the two k neighbours from L1, and nothing
+// else.  Cells with CPML or TFSF k-plane bits add their face updates
+// inline; TFSF i/j planes and dispersive cells run the full sequence out
+// of line (hardCell), which reads everything itself.  The arithmetic of
+// every cell is that of stepCell, term for term.
+//
+// Work items are (i chunk, j tile, k tile) triples, k tile fastest, the
+// i chunks in the marching direction; the grid holds one wave of resident
+// blocks and each block takes items blockIdx.x, blockIdx.x + nblocks, ...
+// A fused launch adds one block (the last) that runs the TFSF auxiliary
+// column's half step.
+// ---------------------------------------------------------------------
+#define MARCH_WARPS 4
+#define MARCH_THREADS (32 * MARCH_WARPS)
+#ifndef MARCH_MINB
+#define MARCH_MINB 4
+#endif
+
+struct MarchShape {
+	int nkt, njt, nic;                  // k tiles, j tiles, i chunks
+	int ni;                             // planes per i chunk
+	int nblocks;                        // blocks taking items (the grid, less a fused auxiliary block)
+};
+
+template <int ALT, int RJ>
+__device__ __forceinline__ void marchItem(const HalfStepParams &P, const MarchShape &M, int item, int *tileList, int *nlist)
+{
+	const int kt = item % M.nkt, jt = (item / M.nkt) % M.njt, ic = item / (M.nkt * M.njt);
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int k = P.kMIN + kt * 32 + lane;
+	const int j0 = P.jMIN + (jt * MARCH_WARPS + warp) * RJ;
+	// planes of the chunk: chunk 0 is where the march of this field starts
+	const int ni = P.iMAX - P.iMIN + 1;
+	const int lo = ALT == 1 ? max(ni - (ic + 1) * M.ni, 0) : ic * M.ni;
+	const int hi = ALT == 1 ? ni - ic * M.ni - 1 : min((ic + 1) * M.ni, ni) - 1;
+	const int iFirst = ALT == 1 ? P.iMIN + hi : P.iMIN + lo, iLast = ALT == 1 ? P.iMIN + lo : P.iMIN + hi;
+	const bool manyObj = P.nobj > 8;
+	if (manyObj) {
+		// objects whose box meets this item's cells, in list order (warp 0)
+		__syncthreads();
+		if (warp == 0) {
+			const int ti0 = min(iFirst, iLast), ti1 = max(iFirst, iLast);
+			const int tj0 = P.jMIN + jt * MARCH_WARPS * RJ, tj1 = min(tj0 + MARCH_WARPS * RJ - 1, P.jMAX);
+			const int tk0 = P.kMIN + kt * 32, tk1 = min(tk0 + 31, P.kMAX);
+			int cnt = 0;
+			for (int base = 0; base < P.nobj; base += 32) {
+				const int n = base + lane;
+				bool hit = false;
+				if (n < P.nobj) {
+					const DevObj &o = P.obj[n];
+					hit = ti1 >= o.i0 && ti0 <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
+				}
+				const unsigned bal = __ballot_sync(0xffffffffu, hit);
+				if (hit) {
+					const int pos = cnt + __popc(bal & ((1u << lane) - 1));
+					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
+				}
+				cnt += __popc(bal);
+			}
+			if (lane == 0) *nlist = cnt;
+		}
+		__syncthreads();
+	}
+	if (k > P.kMAX || j0 > P.jMAX) return;
+	const int *list = 0;
+	int nIter = P.nobj;
+	if (manyObj && *nlist <= ALIS_TILE_OBJ) list = tileList, nIter = *nlist;
+
+	const int sj = (int)P.L.sj, si = (int)P.L.si;
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	float *Fx = P.F[0], *Fy = P.F[1], *Fz = P.F[2];
+	const bool hasC = P.C[0] != 0;
+	// per tile: rows in range, their class bits and dt/dy; the lane's k bits and dt/dz
+	const unsigned bk = __ldg(P.cls[2] + (k - P.kMIN));
+	const float dz = __ldg(P.dtd[2] + (k - P.kMIN));
+	unsigned bj[RJ];
+	float dy[RJ];
+	bool row[RJ];
+#pragma unroll
+	for (int r = 0; r < RJ; r++) {
+		row[r] = j0 + r <= P.jMAX;
+		bj[r] = row[r] ? __ldg(P.cls[1] + (j0 + r - P.jMIN)) : 0u;
+		dy[r] = row[r] ? __ldg(P.dtd[1] + (j0 + r - P.jMIN)) : 0.f;
+	}
+	// the i neighbour (z and y components) of the first plane
+	int c = (iFirst - P.L.i0) * si + (j0 - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
+	float nz[RJ], ny[RJ];
+#pragma unroll
+	for (int r = 0; r < RJ; r++) if (row[r]) nz[r] = __ldg(Gz + c + r * sj + ALT * si), ny[r] = __ldg(Gy + c + r * sj + ALT * si);
+	for (int i = iFirst;; i -= ALT, c -= ALT * si) {
+		const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN));
+		const float dx = __ldg(P.dtd[0] + (i - P.iMIN));
+		float gx[RJ], gy[RJ], gz[RJ], gxk[RJ], gyk[RJ], fx[RJ], fy[RJ], fz[RJ], cx[RJ], cy[RJ], cz[RJ];
+#pragma unroll
+		for (int r = 0; r < RJ; r++) {
+			if (!row[r]) continue;
+			const int cr = c + r * sj;
+			gx[r] = __ldg(Gx + cr), gy[r] = __ldg(Gy + cr), gz[r] = __ldg(Gz + cr);
+			gxk[r] = __ldg(Gx + cr + ALT), gyk[r] = __ldg(Gy + cr + ALT);
+			fx[r] = Fx[cr], fy[r] = Fy[cr], fz[r] = Fz[cr];
+			cx[r] = 1, cy[r] = 1, cz[r] = 1;
+			if (hasC) {
+				if (P.matIdx) {
+					const float4 t = __ldg(P.matTab + __ldg(P.matIdx + cr));
+					cx[r] = t.x, cy[r] = t.y, cz[r] = t.z;
+				} else {
+					cx[r] = __ldg(P.C[0] + cr), cy[r] = __ldg(P.C[1] + cr), cz[r] = __ldg(P.C[2] + cr);
+				}
+			}
+		}
+		// j neighbours: the adjacent row's registers, the edge row's from memory
+		float gzj[RJ], gxj[RJ];
+#pragma unroll
+		for (int r = 0; r < RJ; r++) {
+			if (!row[r]) continue;
+			const int q = r + ALT;
+			if (q >= 0 && q < RJ && row[q]) gzj[r] = gz[q], gxj[r] = gx[q];
+			else gzj[r] = __ldg(Gz + c + r * sj + ALT * sj), gxj[r] = __ldg(Gx + c + r * sj + ALT * sj);
+		}
+		unsigned hard = 0;
+#pragma unroll
+		for (int r = 0; r < RJ; r++) {
+			if (!row[r]) continue;
+			const int j = j0 + r, cr = c + r * sj;
+			if (((bi | bj[r]) & CLS_TFSF) || (bi & bj[r] & bk & 0x1FFu)) {
+				hard |= 1u << r;
+			} else {
+				float ex = fx[r], ey = fy[r], ez = fz[r];
+				const float gzi = nz[r], gyi = ny[r];
+				// curl (reference src/update.c:109-118)
+				if (hasC) {
+					ex += (dz * (gy[r] - gyk[r]) + dy[r] * (gzj[r] - gz[r])) * cx[r];
+					ey += (dx * (gz[r] - gzi) + dz * (gxk[r] - gx[r])) * cy[r];
+					ez += (dy[r] * (gx[r] - gxj[r]) + dx * (gyi - gy[r])) * cz[r];
+				} else {
+					ex += (dz * (gy[r] - gyk[r]) + dy[r] * (gzj[r] - gz[r]));
+					ey += (dx * (gz[r] - gzi) + dz * (gxk[r] - gx[r]));
+					ez += (dy[r] * (gx[r] - gxj[r]) + dx * (gyi - gy[r]));
+				}
+				// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
+				if ((bi | bj[r] | bk) & (CLS_PML_LO | CLS_PML_HI)) {
+#define PML_ARGS P, i, j, k, ex, ey, ez, gx[r], gy[r], gz[r], gyk[r], gxk[r], gzj[r], gxj[r], gzi, gyi, hasC, cx[r], cy[r], cz[r]
+					if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
+					if (bj[r] & CLS_PML_LO) pmlFace<1>(PML_ARGS);
+					if (bk & CLS_PML_LO) pmlFace<2>(PML_ARGS);
+					if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
+					if (bj[r] & CLS_PML_HI) pmlFace<4>(PML_ARGS);
+					if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
+#undef PML_ARGS
+				}
+				// TFSF k face planes (cells on an i or j face plane are hard)
+				if (bk & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, k, ex, ey, ez, hasC, cx[r], cy[r], cz[r]);
+				Fx[cr] = ex, Fy[cr] = ey, Fz[cr] = ez;
+			}
+			nz[r] = gz[r], ny[r] = gy[r];
+		}
+		// hard cells after the plane's lean ones: only the carried state is
+		// live across the out-of-line calls
+		if (hard) {
+#pragma unroll
+			for (int r = 0; r < RJ; r++) if ((hard >> r) & 1u) hardCell<ALT>(P, i, j0 + r, k, list, nIter);
+		}
+		if (i == iLast) break;
+	}
+}
+
+template <int ALT, int RJ>
+__device__ __forceinline__ void marchBlock(const HalfStepParams &P, const MarchShape &M)
+{
+	__shared__ int tileList[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	const int items = M.nkt * M.njt * M.nic;
+	for (int item = blockIdx.x; item < items; item += M.nblocks) marchItem<ALT, RJ>(P, M, item, tileList, &nlist);
+}
+
+template <int ALT, int RJ>
+__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march(const __grid_constant__ HalfStepParams P, const MarchShape M)
+{
+	marchBlock<ALT, RJ>(P, M);
+}
+
+template <int ALT, int RJ>
+__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march_aux(const __grid_constant__ FusedStepParams F, const MarchShape M)
+{
+	if (blockIdx.x == M.nblocks) {
+		smallStepBlock<ALT>(F.aux, threadIdx.x, blockDim.x);
+		return;
+	}
+	marchBlock<ALT, RJ>(F.P, M);
+}
+
 // one half-step launch with block height kTyChoice[v] (v a runtime choice)
 template <int ALT>
 static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
@@ -1531,6 +1763,414 @@ static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const Fuse
 	else if (ty == 8) ALIS_LAUNCH(8);
 	else ALIS_LAUNCH(4);
 #undef ALIS_LAUNCH
+}
+
+// ---------------------------------------------------------------------
+// Batched launches over many worlds (batch.cuh)
+// ---------------------------------------------------------------------
+struct BatchEntry {                    // the cells of one world (one m) in a batched march
+	const HalfStepParams *P;           // its device slot
+	MarchShape M;
+	int itemStart;                     // its first item in the launch
+};
+struct BatchBlock {                    // a half step run by one block (auxiliary column, tiny world)
+	const SmallStepParams *S;          // its device slot
+	int voff;                          // its source values in the group's values, or -1
+};
+struct BatchSource {                   // the source patches of one world
+	const SourceParams *S;
+	int voff;
+};
+struct BatchGhost {                    // the ghost copies of one world
+	const GhostLevels *G;
+	int start;                         // its first thread in the launch
+};
+struct BatchMarch {
+	const BatchEntry *E;
+	int nE, nitems, per;               // entries, items, items per block
+	const BatchBlock *blk;
+	int nblk;                          // one-block steps: the first nblk blocks
+	const float *vals;
+};
+
+// One launch over every world of a group: the first blocks run the
+// one-block steps, the others take `per` consecutive items each of the
+// concatenated marches, the world's parameters copied to shared memory
+// whenever an item belongs to another entry than the block's last one.
+template <int ALT, int RJ>
+__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march_batch(const BatchMarch B)
+{
+	__shared__ HalfStepParams sP;
+	__shared__ int tileList[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	if ((int)blockIdx.x < B.nblk) {
+		const BatchBlock &b = B.blk[blockIdx.x];
+		smallStepBlock<ALT>(*b.S, threadIdx.x, blockDim.x, b.voff >= 0 ? B.vals + b.voff : 0);
+		return;
+	}
+	const int g0 = ((int)blockIdx.x - B.nblk) * B.per, g1 = min(g0 + B.per, B.nitems);
+	int cur = -1;
+	for (int g = g0; g < g1; g++) {
+		int lo = 0, hi = B.nE - 1;
+		while (lo < hi) {
+			const int mid = (lo + hi + 1) >> 1;
+			if (B.E[mid].itemStart <= g) lo = mid; else hi = mid - 1;
+		}
+		if (lo != cur) {
+			__syncthreads();
+			const long long *src = reinterpret_cast<const long long *>(B.E[lo].P);
+			long long *dst = reinterpret_cast<long long *>(&sP);
+			for (int q = threadIdx.x; q < (int)(sizeof(HalfStepParams) / sizeof(long long)); q += blockDim.x) dst[q] = src[q];
+			__syncthreads();
+			cur = lo;
+		}
+		marchItem<ALT, RJ>(sP, B.E[lo].M, g - B.E[lo].itemStart, tileList, &nlist);
+	}
+}
+
+__global__ void k_sources_batch(const BatchSource *T, const float *vals)
+{
+	const BatchSource &b = T[blockIdx.x];
+	sourcesBlock(*b.S, b.voff >= 0 ? vals + b.voff : 0);
+}
+
+__global__ void __launch_bounds__(256) k_ghost_batch(const BatchGhost *T, int n, int total)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= total) return;
+	int lo = 0, hi = n - 1;
+	while (lo < hi) {
+		const int mid = (lo + hi + 1) >> 1;
+		if (T[mid].start <= t) lo = mid; else hi = mid - 1;
+	}
+	ghostChainCell<false>(*T[lo].G, t - T[lo].start, 0);
+}
+
+// the group a host thread is recording
+struct SlotUpdate {
+	void *dst;
+	size_t off, bytes;                 // in the staged update bytes
+};
+struct Recorder {
+	bool on = false;
+	int kind = BATCH_NONE;
+	unsigned long long stamp = 1;
+	std::vector<BatchEntry> entries;
+	std::vector<BatchBlock> blocks;
+	std::vector<BatchSource> sources;
+	std::vector<BatchGhost> ghosts;
+	int nitems = 0, ghostTotal = 0;
+	std::vector<float> values;
+	std::vector<unsigned char> updates;        // new bytes of changed slots
+	std::vector<SlotUpdate> updateList;
+	void clear() {
+		kind = BATCH_NONE;
+		stamp++;
+		entries.clear(), blocks.clear(), sources.clear(), ghosts.clear();
+		nitems = 0, ghostTotal = 0;
+		values.clear(), updates.clear(), updateList.clear();
+	}
+};
+static thread_local Recorder gRec;
+static bool batchRecording(void) { return gRec.on; }
+
+// the staging blob: pinned host and device buffers in turn, each reused
+// once the launches that read its last contents have finished
+#define BLOB_RING 4
+struct Blob {
+	unsigned char *pin[BLOB_RING] = {};
+	unsigned char *dev[BLOB_RING] = {};
+	size_t cap[BLOB_RING] = {};
+	cudaEvent_t done[BLOB_RING] = {};
+	bool pending[BLOB_RING] = {};
+	int cur = 0;
+	size_t bytes = 0;
+	bool open = false;
+};
+static thread_local Blob gBlob;
+
+extern "C" int alisgpu__blob_take(size_t bytes, void **host, const void **dev)
+{
+	Blob &b = gBlob;
+	if (b.open) return alisgpu__fail(ALISGPU_EINVAL, "batch: blob taken twice");
+	const int q = b.cur;
+	if (b.pending[q]) {
+		ALIS_CUDA(cudaEventSynchronize(b.done[q]));
+		b.pending[q] = false;
+	}
+	if (!b.done[q]) ALIS_CUDA(cudaEventCreateWithFlags(&b.done[q], cudaEventDisableTiming));
+	if (bytes > b.cap[q]) {
+		if (b.pin[q]) cudaFreeHost(b.pin[q]), b.pin[q] = 0;
+		if (b.dev[q]) alisgpu__freeAsync(b.dev[q]), b.dev[q] = 0;
+		b.cap[q] = 0;
+		const size_t cap = std::max(bytes + bytes / 2, (size_t)1 << 16);
+		ALIS_CUDA(cudaMallocHost(&b.pin[q], cap));
+		ALIS_CUDA(alisgpu__mallocAsync(&b.dev[q], cap));
+		b.cap[q] = cap;
+	}
+	b.bytes = bytes, b.open = true;
+	*host = b.pin[q], *dev = b.dev[q];
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu__blob_send(void)
+{
+	Blob &b = gBlob;
+	if (!b.open) return alisgpu__fail(ALISGPU_EINVAL, "batch: no blob taken");
+	if (b.bytes) ALIS_CUDA(cudaMemcpyAsync(b.dev[b.cur], b.pin[b.cur], b.bytes, cudaMemcpyHostToDevice, gStream));
+	return ALISGPU_OK;
+}
+
+// the launches reading the blob are issued: the next group takes the next buffer
+extern "C" int alisgpu__blob_done(void)
+{
+	Blob &b = gBlob;
+	if (!b.open) return ALISGPU_OK;
+	ALIS_CUDA(cudaEventRecord(b.done[b.cur], gStream));
+	b.pending[b.cur] = true;
+	b.open = false;
+	b.cur = (b.cur + 1) % BLOB_RING;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu__slot_sync(ParamSlot *s, const void *src, size_t bytes, const void **dev)
+{
+	if (!s->dev || s->host.size() != bytes) {
+		if (s->dev) alisgpu__freeAsync(s->dev), s->dev = nullptr;
+		s->host.clear();
+		ALIS_CUDA(alisgpu__mallocAsync((unsigned char **)&s->dev, bytes));
+	}
+	if (s->host.size() != bytes || memcmp(s->host.data(), src, bytes)) {
+		s->host.assign((const unsigned char *)src, (const unsigned char *)src + bytes);
+		// uploaded with the group, before its launches
+		const size_t off = (gRec.updates.size() + 255) & ~(size_t)255;
+		gRec.updates.resize(off + bytes);
+		memcpy(gRec.updates.data() + off, src, bytes);
+		gRec.updateList.push_back(SlotUpdate{ s->dev, off, bytes });
+	}
+	*dev = s->dev;
+	return ALISGPU_OK;
+}
+
+extern "C" void alisgpu__slot_free(ParamSlot *s)
+{
+	if (s->dev) alisgpu__freeAsync(s->dev);
+	s->dev = nullptr;
+	s->host.clear();
+}
+
+// march rows and shape of a batched entry: chunks of up to 16 planes (the
+// worlds of a group fill the GPU together)
+static int batchRows(void)
+{
+	static int rows = 0;
+	if (!rows) {
+		const char *e = getenv("ALISGPU_BATCH_ROWS");
+		rows = e && atoi(e) == 2 ? 2 : 4;
+	}
+	return rows;
+}
+
+static MarchShape batchShape(const alisgpu_geometry &g, int rows)
+{
+	MarchShape M;
+	const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
+	M.nkt = (nk + 31) / 32;
+	M.njt = (nj + MARCH_WARPS * rows - 1) / (MARCH_WARPS * rows);
+	M.ni = std::min(ni, 16);
+	M.nic = (ni + M.ni - 1) / M.ni;
+	M.nblocks = 0;
+	return M;
+}
+
+template <int ALT, int RJ>
+static int launchMarchBatch(const BatchMarch &B0, cudaStream_t st)
+{
+	static std::atomic<int> residentAt{0};
+	int resident = residentAt.load();
+	if (!resident) {
+		int dev = 0, sms = 0, per = 0;
+		ALIS_CUDA(cudaGetDevice(&dev));
+		ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_march_batch<ALT, RJ>, MARCH_THREADS, 0));
+		resident = std::max(1, sms * per);
+		residentAt.store(resident);
+	}
+	BatchMarch B = B0;
+	B.per = std::max(1, (B.nitems + resident - 1) / resident);
+	const unsigned blocks = (unsigned)B.nblk + (unsigned)((B.nitems + B.per - 1) / B.per);
+	if (blocks) k_march_batch<ALT, RJ><<<blocks, MARCH_THREADS, 0, st>>>(B);
+	return ALISGPU_OK;
+}
+
+// launch the open half-step group: its tables and the changed slots go up
+// in one copy, then the march, the sources and the ghost copies of every
+// world, each one launch
+static int launchHalfGroup(int field)
+{
+	Recorder &R = gRec;
+	auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+	const size_t oE = 0, oB = oE + al(R.entries.size() * sizeof(BatchEntry));
+	const size_t oS = oB + al(R.blocks.size() * sizeof(BatchBlock));
+	const size_t oG = oS + al(R.sources.size() * sizeof(BatchSource));
+	const size_t oV = oG + al(R.ghosts.size() * sizeof(BatchGhost));
+	const size_t oU = oV + al(R.values.size() * sizeof(float));
+	const size_t total = oU + R.updates.size();
+	void *hv = 0;
+	const void *dv = 0;
+	int rc = alisgpu__blob_take(total, &hv, &dv);
+	if (rc) return rc;
+	unsigned char *h = (unsigned char *)hv;
+	const unsigned char *d = (const unsigned char *)dv;
+	if (!R.entries.empty()) memcpy(h + oE, R.entries.data(), R.entries.size() * sizeof(BatchEntry));
+	if (!R.blocks.empty()) memcpy(h + oB, R.blocks.data(), R.blocks.size() * sizeof(BatchBlock));
+	if (!R.sources.empty()) memcpy(h + oS, R.sources.data(), R.sources.size() * sizeof(BatchSource));
+	if (!R.ghosts.empty()) memcpy(h + oG, R.ghosts.data(), R.ghosts.size() * sizeof(BatchGhost));
+	if (!R.values.empty()) memcpy(h + oV, R.values.data(), R.values.size() * sizeof(float));
+	if (!R.updates.empty()) memcpy(h + oU, R.updates.data(), R.updates.size());
+	if ((rc = alisgpu__blob_send())) return rc;
+	for (const SlotUpdate &u : R.updateList)
+		ALIS_CUDA(cudaMemcpyAsync(u.dst, d + oU + u.off, u.bytes, cudaMemcpyDeviceToDevice, gStream));
+	const float *vals = (const float *)(d + oV);
+	if (!R.entries.empty() || !R.blocks.empty()) {
+		BatchMarch B;
+		B.E = (const BatchEntry *)(d + oE), B.nE = (int)R.entries.size(), B.nitems = R.nitems, B.per = 1;
+		B.blk = (const BatchBlock *)(d + oB), B.nblk = (int)R.blocks.size();
+		B.vals = vals;
+		int slot = alisgpu__prof_start();
+		const int rows = batchRows();
+		if (field == 0) rc = rows == 2 ? launchMarchBatch<1, 2>(B, gStream) : launchMarchBatch<1, 4>(B, gStream);
+		else rc = rows == 2 ? launchMarchBatch<-1, 2>(B, gStream) : launchMarchBatch<-1, 4>(B, gStream);
+		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
+		alisgpu__count_launch();
+		if (rc) return rc;
+		ALIS_CUDA(cudaGetLastError());
+	}
+	if (!R.sources.empty()) {
+		int slot = alisgpu__prof_start();
+		k_sources_batch<<<(unsigned)R.sources.size(), 256, 0, gStream>>>((const BatchSource *)(d + oS), vals);
+		alisgpu__prof_stop(slot, ALISGPU_K_SOURCE);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	if (!R.ghosts.empty() && R.ghostTotal) {
+		int slot = alisgpu__prof_start();
+		k_ghost_batch<<<(unsigned)((R.ghostTotal + 255) / 256), 256, 0, gStream>>>((const BatchGhost *)(d + oG),
+		                                                                        (int)R.ghosts.size(), R.ghostTotal);
+		alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+	}
+	return alisgpu__blob_done();
+}
+
+// launch the open group, whatever its kind
+static int batchLaunch(void)
+{
+	Recorder &R = gRec;
+	int rc = ALISGPU_OK;
+	const bool updates = !R.updateList.empty();
+	if (R.kind == BATCH_E || R.kind == BATCH_H) rc = launchHalfGroup(R.kind == BATCH_E ? 0 : 1);
+	else if (R.kind == BATCH_PHASER) rc = alisgpu__phaser_batch_launch();
+	else if (updates) rc = launchHalfGroup(0);
+	R.clear();
+	return rc;
+}
+
+extern "C" int alisgpu__batch_enter(int kind, const void *world)
+{
+	Recorder &R = gRec;
+	if (!R.on) return 0;
+	const alisgpu_world *w = (const alisgpu_world *)world;
+	if (w && w->group) return 0;                      // worlds on streams of their own step as usual
+	if (kind == BATCH_NONE) return 1;
+	if (R.kind != kind || (w && w->batchStamp == R.stamp)) {
+		if (batchLaunch()) return -1;
+		R.kind = kind;
+	}
+	if (w) const_cast<alisgpu_world *>(w)->batchStamp = R.stamp;
+	return 1;
+}
+
+extern "C" int alisgpu_batch_begin(void)
+{
+	int rc = alisgpu_init();
+	if (rc) return rc;
+	if (gRec.on) return alisgpu__fail(ALISGPU_EINVAL, "batch_begin: a batch is open already");
+	bindWorld(0);
+	fullJoin();
+	gRec.clear();
+	gRec.on = true;
+	return ALISGPU_OK;
+}
+
+extern "C" int alisgpu_batch_end(void)
+{
+	if (!gRec.on) return ALISGPU_OK;
+	bindWorld(0);
+	const int rc = batchLaunch();
+	gRec.on = false;
+	if (rc) alisgpu__phaser_batch_clear();
+	return rc;
+}
+
+extern "C" int alisgpu__batch_flush(void)
+{
+	if (!gRec.on || gRec.kind == BATCH_NONE) return ALISGPU_OK;
+	return batchLaunch();
+}
+
+// Launch shapes of the half step the tuner picks from: k_half_step with
+// blocks of 32 x 2, 32 x 4 or 32 x 8 threads over one plane, or k_march
+// with warps of 2 or 4 rows.
+#define ALIS_SHAPES 5
+#define ALIS_SHAPE_MARCH0 3
+static const int kMarchRows[2] = { 2, 4 };
+
+// Items and blocks of a march over a world: k tiles x j tiles x i chunks
+// of at most 8 planes (fewer when the tiles alone do not fill the
+// resident blocks), and as many blocks as give every block the same
+// number of items, within one wave of resident blocks.
+template <int ALT, int RJ>
+static int marchShape(const alisgpu_geometry &g, MarchShape &M)
+{
+	static std::atomic<int> residentAt{0};
+	int resident = residentAt.load();
+	if (!resident) {
+		int dev = 0, sms = 0, per = 0;
+		ALIS_CUDA(cudaGetDevice(&dev));
+		ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_march<ALT, RJ>, MARCH_THREADS, 0));
+		resident = std::max(1, sms * per);
+		residentAt.store(resident);
+	}
+	const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
+	M.nkt = (nk + 31) / 32;
+	M.njt = (nj + MARCH_WARPS * RJ - 1) / (MARCH_WARPS * RJ);
+	const long long tiles = (long long)M.nkt * M.njt;
+	M.ni = (int)std::max(1LL, std::min(8LL, tiles * ni / (4LL * resident)));
+	M.nic = (ni + M.ni - 1) / M.ni;
+	const long long items = tiles * M.nic;
+	const long long per = (items + resident - 1) / resident;
+	M.nblocks = (int)((items + per - 1) / per);
+	return ALISGPU_OK;
+}
+
+template <int ALT>
+static int launchMarch(int rows, const alisgpu_geometry &g, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
+{
+	MarchShape M;
+	int rc = rows == 2 ? marchShape<ALT, 2>(g, M) : marchShape<ALT, 4>(g, M);
+	if (rc) return rc;
+	const unsigned blocks = (unsigned)M.nblocks + (F ? 1u : 0u);
+	if (rows == 2) {
+		if (F) k_march_aux<ALT, 2><<<blocks, MARCH_THREADS, 0, st>>>(*F, M);
+		else k_march<ALT, 2><<<blocks, MARCH_THREADS, 0, st>>>(P, M);
+	} else {
+		if (F) k_march_aux<ALT, 4><<<blocks, MARCH_THREADS, 0, st>>>(*F, M);
+		else k_march<ALT, 4><<<blocks, MARCH_THREADS, 0, st>>>(P, M);
+	}
+	return ALISGPU_OK;
 }
 
 // ---------------------------------------------------------------------
@@ -1591,7 +2231,12 @@ static bool boxesMeet(const int a[6], const int b[6])
 	return a[0] <= b[1] && b[0] <= a[1] && a[2] <= b[3] && b[2] <= a[3] && a[4] <= b[5] && b[4] <= a[5];
 }
 
-static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, int n)
+static int recordGhosts(alisgpu_world *w, int field, const GhostLevels &GL, long long total);
+
+// The ghost copies of a half step.  With record set (a batch records the
+// world's half step) the one-launch form joins the batch group; the other
+// forms launch the group first and then run on their own.
+static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, int n, bool record = false)
 {
 	const alisgpu_geometry &g = w->g;
 	if (n <= 0) return ALISGPU_OK;
@@ -1670,6 +2315,7 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 				alisgpu__freeAsync(flag);
 				w->ghostChain[field] = h == 0;
 			}
+			if (w->ghostChain[field] && record) return recordGhosts(w, field, GL, total);
 			if (w->ghostChain[field]) {
 				int slot = alisgpu__prof_start();
 				k_ghost_chain<false><<<blocks, 256, 0, gStream>>>(GL, nullptr);
@@ -1681,6 +2327,10 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 			memset(GL.c, 0, sizeof GL.c);
 			memset(GL.start, 0, sizeof GL.start);
 			GL.n = 0;
+		}
+		if (record) {
+			int rc = alisgpu__batch_flush();
+			if (rc) return rc;
 		}
 		int at = 0;
 		for (int l = 0; l < nlev; l++) {
@@ -1714,6 +2364,10 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 		alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
 		alisgpu__count_launch();
 		return ALISGPU_OK;
+	}
+	if (record) {
+		int rc = alisgpu__batch_flush();
+		if (rc) return rc;
 	}
 	int q = 0;
 	while (q < n) {
@@ -1763,7 +2417,8 @@ static int applyPendingGhosts(alisgpu_world *w)
 // half steps of the field cycle through the shapes with events around
 // them; once every one of them has completed, the shape with the least
 // time (each shape's fastest run) stays.  ALISGPU_TUNE=0 keeps 32 x 4.
-#define ALIS_TUNE_STEPS 9
+#define ALIS_TUNE_STEPS 15
+#define ALIS_SHAPE_DEFAULT 4
 static int tunedShape(alisgpu_world *w, int field, bool *timed)
 {
 	alisgpu_world::TyTuner &t = w->tune[field];
@@ -1774,24 +2429,30 @@ static int tunedShape(alisgpu_world *w, int field, bool *timed)
 		const char *e = getenv("ALISGPU_TUNE");
 		enabled = !(e && e[0] == '0');
 	}
-	if (!enabled) return t.choice = ALIS_TY_DEFAULT;
-	if (gProfOn) return ALIS_TY_DEFAULT;
+	static int forced = -2;
+	if (forced == -2) {
+		const char *e = getenv("ALISGPU_STEP_SHAPE");
+		forced = e && atoi(e) >= 0 && atoi(e) < ALIS_SHAPES ? atoi(e) : -1;
+	}
+	if (forced >= 0) return t.choice = forced;
+	if (!enabled) return t.choice = ALIS_SHAPE_DEFAULT;
+	if (gProfOn) return ALIS_SHAPE_DEFAULT;
 	if (t.seen < ALIS_TUNE_STEPS) {
 		if (cudaEventCreate(&t.a[t.seen]) != cudaSuccess || cudaEventCreate(&t.b[t.seen]) != cudaSuccess)
-			return t.choice = ALIS_TY_DEFAULT;
+			return t.choice = ALIS_SHAPE_DEFAULT;
 		*timed = true;
-		return t.seen % ALIS_TY_CHOICES;
+		return t.seen % ALIS_SHAPES;
 	}
-	for (int q = 0; q < ALIS_TUNE_STEPS; q++) if (cudaEventQuery(t.b[q]) != cudaSuccess) return ALIS_TY_DEFAULT;
-	float best[ALIS_TY_CHOICES];
-	for (int c = 0; c < ALIS_TY_CHOICES; c++) best[c] = 1e30f;
+	for (int q = 0; q < ALIS_TUNE_STEPS; q++) if (cudaEventQuery(t.b[q]) != cudaSuccess) return ALIS_SHAPE_DEFAULT;
+	float best[ALIS_SHAPES];
+	for (int c = 0; c < ALIS_SHAPES; c++) best[c] = 1e30f;
 	for (int q = 0; q < ALIS_TUNE_STEPS; q++) {
 		float ms = 0;
 		if (cudaEventElapsedTime(&ms, t.a[q], t.b[q]) == cudaSuccess && ms < best[t.variant[q]]) best[t.variant[q]] = ms;
 		cudaEventDestroy(t.a[q]), cudaEventDestroy(t.b[q]);
 	}
-	int c = ALIS_TY_DEFAULT;
-	for (int q = 0; q < ALIS_TY_CHOICES; q++) if (best[q] < best[c]) c = q;
+	int c = ALIS_SHAPE_DEFAULT;
+	for (int q = 0; q < ALIS_SHAPES; q++) if (best[q] < best[c]) c = q;
 	return t.choice = c;
 }
 
@@ -1828,6 +2489,92 @@ static int stageValues(alisgpu_world *w, const float *vals, int n, cudaStream_t 
 	ALIS_CUDA(cudaMemcpyAsync(w->vbuf, w->vpin[b], n * sizeof(float), cudaMemcpyHostToDevice, st));
 	ALIS_CUDA(cudaEventRecord(w->vpinFree[b], st));
 	*dev = w->vbuf;
+	return ALISGPU_OK;
+}
+
+// ---- recording a half step into the open batch group ----
+static int recordStaged(alisgpu_world *aux, int field)
+{
+	aux->stagedValid[field] = false;
+	const void *dS = 0;
+	int rc = alisgpu__slot_sync(&aux->bS[field], aux->staged[field], sizeof(SmallStepParams), &dS);
+	if (rc) return rc;
+	const std::vector<float> &v = aux->stagedVals[field];
+	const int voff = v.empty() ? -1 : (int)gRec.values.size();
+	gRec.values.insert(gRec.values.end(), v.begin(), v.end());
+	gRec.blocks.push_back(BatchBlock{ (const SmallStepParams *)dS, voff });
+	return ALISGPU_OK;
+}
+
+static int recordGhosts(alisgpu_world *w, int field, const GhostLevels &GL, long long total)
+{
+	const void *dG = 0;
+	int rc = alisgpu__slot_sync(&w->bG[field], &GL, sizeof GL, &dG);
+	if (rc) return rc;
+	if (gRec.ghostTotal + total >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: ghost copies exceed 32-bit indexing");
+	gRec.ghosts.push_back(BatchGhost{ (const GhostLevels *)dG, gRec.ghostTotal });
+	gRec.ghostTotal += (int)total;
+	return ALISGPU_OK;
+}
+
+// A large world's half step in the open batch group: a march entry per
+// field set m, the TFSF auxiliary column's staged step as a one-block
+// entry, the source patches and the ghost copies (H; E's wait for the
+// next host read as usual).  P: the step's parameters with the per-world
+// parts filled in.
+static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStepParams &P)
+{
+	const alisgpu_geometry &g = w->g;
+	const int field = s->field;
+	const int rows = batchRows();
+	for (int m = 0; m <= g.complexField; m++) {
+		P.m = m;
+		for (int c = 0; c < 3; c++) {
+			P.F[c] = field == 0 ? w->E[m][c] : w->H[m][c];
+			P.G[c] = field == 0 ? w->H[m][c] : w->E[m][c];
+			P.C[c] = field == 0 ? w->C[c] : 0;
+			P.Fother[c] = w->E[m][c];
+		}
+		P.matIdx = field == 0 ? w->matIdx : 0;
+		P.matTab = field == 0 ? w->matTab : 0;
+		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
+		const void *dP = 0;
+		int rc = alisgpu__slot_sync(&w->bP[field][m], &P, sizeof P, &dP);
+		if (rc) return rc;
+		const MarchShape M = batchShape(g, rows);
+		gRec.entries.push_back(BatchEntry{ (const HalfStepParams *)dP, M, gRec.nitems });
+		const long long items = (long long)gRec.nitems + (long long)M.nkt * M.njt * M.nic;
+		if (items >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: too many items");
+		gRec.nitems = (int)items;
+	}
+	int rc = runStagedAux(s, field);
+	if (rc) return rc;
+	if (s->nsrc > 0) {
+		if (s->nsrc > ALIS_MAXSRC) return alisgpu__fail(ALISGPU_ERANGE, "half_step: %d source patches (max %d)", s->nsrc, ALIS_MAXSRC);
+		static thread_local SourceParams SP;
+		memset(&SP, 0, sizeof SP);
+		SP.n = s->nsrc;
+		SP.L = w->L;
+		for (int m = 0; m < 2; m++) for (int c = 0; c < 3; c++) {
+			int mm = m <= g.complexField ? m : 0;
+			SP.F[m][c] = field == 0 ? w->E[mm][c] : w->H[mm][c];
+		}
+		memcpy(SP.p, s->src, s->nsrc * sizeof(alisgpu_source_patch));
+		SP.err = gErrWord;
+		const void *dS = 0;
+		if ((rc = alisgpu__slot_sync(&w->bSrc[field], &SP, sizeof SP, &dS))) return rc;
+		const int voff = s->nvalues ? (int)gRec.values.size() : -1;
+		gRec.values.insert(gRec.values.end(), s->values, s->values + s->nvalues);
+		gRec.sources.push_back(BatchSource{ (const SourceParams *)dS, voff });
+	}
+	if (field == 0) {
+		w->pendingE.assign(s->ghost, s->ghost + s->nghost);
+	} else {
+		w->hGhosts.assign(s->ghost, s->ghost + s->nghost);
+		if ((rc = runGhosts(w, 1, s->ghost, s->nghost, true))) return rc;
+	}
+	w->hRecorded = false;
+	gMainRec[field] = 0;
 	return ALISGPU_OK;
 }
 
@@ -1926,6 +2673,32 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		S.nsrc = s->nsrc, S.nghost = s->nghost;
 		if (s->nsrc) memcpy(S.src, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		if (s->nghost) memcpy(S.ghost, s->ghost, s->nghost * sizeof(alisgpu_ghost_copy));
+		// recorded by a batch: staged for the parent's entry, or an entry of its own
+		const int rec = alisgpu__batch_enter(s->concurrent ? BATCH_NONE : (field == 0 ? BATCH_E : BATCH_H), w);
+		if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
+		if (rec) {
+			S.vdev = 0;
+			memset(S.v, 0, sizeof S.v);
+			if (s->attach && s->concurrent) {
+				if (!w->staged[field]) w->staged[field] = new SmallStepParams();
+				*w->staged[field] = S;
+				w->stagedValid[field] = true;
+				w->stagedVals[field].assign(s->values, s->values + s->nvalues);
+				return ALISGPU_OK;
+			}
+			if (!s->concurrent) {
+				int rc = runStagedAux(s, field);
+				if (rc) return rc;
+			}
+			const void *dS = 0;
+			int rc = alisgpu__slot_sync(&w->bS[field], &S, sizeof S, &dS);
+			if (rc) return rc;
+			const int voff = s->nvalues ? (int)gRec.values.size() : -1;
+			gRec.values.insert(gRec.values.end(), s->values, s->values + s->nvalues);
+			gRec.blocks.push_back(BatchBlock{ (const SmallStepParams *)dS, voff });
+			gMainRec[field] = 0;
+			return ALISGPU_OK;
+		}
 		// on the side stream: after the parent's last step of the other
 		// field, or after everything when a join asked for that
 		cudaStream_t st = gStream;
@@ -1981,10 +2754,16 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		}
 		return ALISGPU_OK;
 	}
+	{
+		const int rec = alisgpu__batch_enter(field == 0 ? BATCH_E : BATCH_H, w);
+		if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
+		if (rec) return recordHalfStep(w, s, P);
+	}
 	const int ni = g.iMAX - g.iMIN + 1;
 	bool timed = false, fused = false;
 	const int v = tunedShape(w, field, &timed);
-	const int ty = kTyChoice[v];
+	const bool march = v >= ALIS_SHAPE_MARCH0;
+	const int ty = march ? 4 : kTyChoice[v], rows = march ? kMarchRows[v - ALIS_SHAPE_MARCH0] : 0;
 	dim3 grid((g.kMAX - g.kMIN + TX * ALIS_KPT) / (TX * ALIS_KPT), (g.jMAX - g.jMIN + ty) / ty, ni);
 	if (timed) ALIS_CUDA(cudaEventRecord(w->tune[field].a[w->tune[field].seen], gStream));
 	for (int m = 0; m <= g.complexField; m++) {
@@ -2007,8 +2786,14 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			FP.aux = *aux->staged[field];
 			aux->stagedValid[field] = false;
 			fused = true;
-			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
+			if (march) {
+				int rc = field == 0 ? launchMarch<1>(rows, g, P, &FP, gStream) : launchMarch<-1>(rows, g, P, &FP, gStream);
+				if (rc) return rc;
+			} else if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
 			else launchHalfStep<-1>(v, grid, P, &FP, gStream);
+		} else if (march) {
+			int rc = field == 0 ? launchMarch<1>(rows, g, P, 0, gStream) : launchMarch<-1>(rows, g, P, 0, gStream);
+			if (rc) return rc;
 		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream);
 		else launchHalfStep<-1>(v, grid, P, 0, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
@@ -2173,6 +2958,7 @@ __global__ void __launch_bounds__(256) k_plane_total(const PlaneParams P)
 
 extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int lo[2], const int hi[2], float *out)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	if (!w || axis < 0 || axis > 2 || !lo || !hi || !out) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: bad argument");
 	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "plane_flux: spacing tables not set");
@@ -2250,6 +3036,7 @@ __global__ void k_box_gather(const BoxGatherParams P)
 
 extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1, int k0, int k1, float *host)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	if (!w || !host || i1 < i0 || j1 < j0 || k1 < k0) return alisgpu__fail(ALISGPU_EINVAL, "field_box_download: bad argument");
 	const Layout &L = w->L;
@@ -2359,6 +3146,7 @@ extern "C" int alisgpu_slice_dft_create(alisgpu_world *w, const int box[6], alis
 extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int comp, int avg, const int sym[3], const float par[3],
                                      float re, float im)
 {
+	ALIS_BATCH_GUARD();
 	if (d) bindWorld(d->w);
 	if (!d || field < 0 || field > 1 || m < 0 || m > 1 || comp < 0 || comp > 2 || avg < 0 || avg > 1 || !sym || !par)
 		return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_add: bad argument");
@@ -2413,6 +3201,7 @@ extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int
 
 extern "C" int alisgpu_slice_dft_download(alisgpu_slice_dft *d, float *F, float *G)
 {
+	ALIS_BATCH_GUARD();
 	if (d) bindWorld(d->w);
 	if (!d || !F || !G) return alisgpu__fail(ALISGPU_EINVAL, "slice_dft_download: bad argument");
 	const size_t cells = (size_t)(1 + d->i1 - d->i0) * (1 + d->j1 - d->j0) * (1 + d->k1 - d->k0);
@@ -2538,6 +3327,7 @@ __global__ void __launch_bounds__(256) k_absorb_total(const AbsorbParams P)
 
 extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 {
+	ALIS_BATCH_GUARD();
 	bindWorld(w);
 	if (!w || !out || n < 0 || n >= (int)w->objs.size()) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: bad argument");
 	if (!w->sp[0][0]) return alisgpu__fail(ALISGPU_EINVAL, "object_absorption: spacing tables not set");
@@ -2677,6 +3467,7 @@ static int crossGroup(const alisgpu_world *ws, const alisgpu_world *wp, bool pum
 extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1, const alisgpu_world *wp2, int n, int m,
                                      const float d[3][6], float Alt)
 {
+	ALIS_BATCH_GUARD();
 	if (!ws || !wp1 || !wp2 || !d || n < 0 || n >= (int)ws->objs.size() || m < 0 || m > ws->g.complexField ||
 	    m > wp1->g.complexField || m > wp2->g.complexField)
 		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: bad argument");

@@ -106,6 +106,17 @@ def run(against, scene, scale, steps, env=None):
         return read_dump(out)
 
 
+_CACHE = {}
+
+
+def run_cached(against, scene, scale, steps):
+    """run() of a case without extra environment, kept for the session."""
+    key = (against, scene, scale, steps)
+    if key not in _CACHE:
+        _CACHE[key] = run(against, scene, scale, steps)
+    return _CACHE[key]
+
+
 def digest(arr):
     return hashlib.sha256(np.ascontiguousarray(arr).tobytes()).hexdigest()
 
