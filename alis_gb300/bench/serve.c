@@ -13,6 +13,13 @@
  * mode sequential: the same requests one after another, each run to its
  *                  end alone on the default streams (the plain path).
  * mode alone <id>: request <id> by itself (its result, for comparison).
+ * mode batched:    the requests in waves -- as many as fit the budget and
+ *                  the slots, in arrival order -- whose worlds step
+ *                  together: every step's updateE, updateH and
+ *                  updatePhaser calls of the wave's worlds are recorded
+ *                  between alisBatchBegin and alisBatchEnd and run as a
+ *                  few launches over all of them; SERVE_THREADS host
+ *                  threads record a share of the wave each.
  *
  * The mix follows the served-stream workload in miniature: half vacuum
  * with a dielectric ball, three tenths a Drude bowtie antenna with a gap
@@ -37,6 +44,7 @@
 #include <time.h>
 #include <stdint.h>
 #include <unistd.h>
+#include <omp.h>
 
 #define MAXREQ 4096
 #define MAXK 16
@@ -250,7 +258,7 @@ static int cmpd(const void *a, const void *b)
 int main(int argc, char **argv)
 {
 	if (argc < 6) {
-		fprintf(stderr, "usage: %s served|sequential|alone requests rate seed small|large [slots|id] [budget GB]\n", argv[0]);
+		fprintf(stderr, "usage: %s served|sequential|alone|batched requests rate seed small|large|sweep [slots|id] [budget GB]\n", argv[0]);
 		return 2;
 	}
 	const char *mode = argv[1];
@@ -298,6 +306,47 @@ int main(int argc, char **argv)
 			R[q].arrival = 0;
 			cellSteps += (double)R[q].cells * R[q].steps;
 			finished++;
+		}
+	} else if (!strcmp(mode, "batched")) {
+		int next = 0, wave[MAXREQ];
+		while (next < nreq) {
+			int n = 0, longest = 0;
+			double used = 0;
+			while (next < nreq && n < slots && (n == 0 || used + footprint(next) <= budget)) {
+				setupRequest(next, 0);
+				R[next].start = now();
+				used += footprint(next);
+				if (R[next].steps > longest) longest = R[next].steps;
+				wave[n++] = next++;
+			}
+			/* each host thread records the steps of its share of the wave */
+			double ts = now();
+			const int nth = threads < n ? threads : n;
+			#pragma omp parallel num_threads(nth)
+			{
+				const int me = omp_get_thread_num();
+				const int a0 = n * me / nth, a1 = n * (me + 1) / nth;
+				for (int s = 0; s < longest; s++) {
+					alisBatchBegin();
+					for (int a = a0; a < a1; a++) if (R[wave[a]].done < R[wave[a]].steps)
+						for (int k = 0; k < R[wave[a]].nk; k++) updateE(R[wave[a]].W[k]);
+					for (int a = a0; a < a1; a++) if (R[wave[a]].done < R[wave[a]].steps)
+						for (int k = 0; k < R[wave[a]].nk; k++) updateH(R[wave[a]].W[k]);
+					for (int a = a0; a < a1; a++) if (R[wave[a]].done < R[wave[a]].steps)
+						for (int k = 0; k < R[wave[a]].nk; k++) updatePhaser(R[wave[a]].W[k], R[wave[a]].P[k]);
+					alisBatchEnd();
+					for (int a = a0; a < a1; a++) if (R[wave[a]].done < R[wave[a]].steps) R[wave[a]].done++;
+				}
+			}
+			tStep += now() - ts;
+			for (int a = 0; a < n; a++) {
+				const int q = wave[a];
+				finishRequest(q);
+				R[q].finish -= t0;
+				R[q].arrival = 0;
+				cellSteps += (double)R[q].cells * R[q].steps;
+				finished++;
+			}
 		}
 	} else {
 		int active[MAXREQ], nact = 0, next = 0;
@@ -354,6 +403,6 @@ int main(int argc, char **argv)
 	       "\"host_s\": {\"setup\": %.4f, \"step\": %.4f, \"finish\": %.4f}, \"threads\": %d}\n",
 	       mode, finished, rate, argv[4], argv[5], slots, budget / 1e9, wall, cellSteps,
 	       cellSteps / wall / 1e9, 1e3 * p50, 1e3 * p99, 1e3 * lat[nl - 1], finished / wall, tSetup, tStep, tFinish,
-	       strcmp(mode, "served") ? 1 : threads);
+	       strcmp(mode, "served") && strcmp(mode, "batched") ? 1 : threads);
 	return 0;
 }

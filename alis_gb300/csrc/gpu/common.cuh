@@ -73,8 +73,9 @@ struct HalfStepParams {
 	float *F[3];
 	const float *G[3];
 	const float *C[3];                    // eps^-1 maps (E half step) or null
-	const unsigned char *matIdx;          // per cell index into matTab (or null): the
+	const void *matIdx;                   // per cell index into matTab (or null): the
 	const float4 *matTab;                 // distinct (C[0], C[1], C[2]) triples
+	int matWide;                          // index of 16 bits (else 8)
 	const float *dtd[3];                  // dt/ds tables indexed from MIN
 	const float *cp[9];                   // CPML b/c tables (xP,xPy,xPz,yP,yPz,yPx,zP,zPx,zPy)
 	int slabOn[6];                        // xMin,yMin,zMin,xMax,yMax,zMax
@@ -95,6 +96,14 @@ struct HalfStepParams {
 #define CLS_PML_LO 0x2000u
 #define CLS_PML_HI 0x4000u
 #define CLS_TFSF 0x8000u
+
+// the eps^-1 triple of cell c from the material index
+__device__ __forceinline__ float4 matTriple(const HalfStepParams &P, int c)
+{
+	const unsigned q = P.matWide ? (unsigned)__ldg((const unsigned short *)P.matIdx + c)
+	                             : (unsigned)__ldg((const unsigned char *)P.matIdx + c);
+	return __ldg(P.matTab + q);
+}
 
 // ---- launch bookkeeping ----
 extern "C" void alisgpu__count_launch(void);

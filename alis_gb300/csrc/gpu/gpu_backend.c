@@ -466,6 +466,8 @@ static void halfStep(world W, int field) { halfStepAs(W, field, 0); }
  * launch (measured on 32 periodic unit cells: 11.6 against 9.4 Gcell/s
  * one after another, 25.4 against 21.3 served).  ALISGPU_AUX_ATTACH=0
  * turns it off, =2 turns it on for every world. */
+static __thread int batchOn;
+
 static int attachAux(world W)
 {
 	static int enabled = -1;
@@ -475,7 +477,20 @@ static int attachAux(world W)
 	}
 	if (!enabled || !W->S || W->S->S || !W->S->W || W->S->W->S || !findWorld(W->S->W)) return 0;
 	devWorld *d = findWorld(W);
-	return d && (enabled == 2 || d->ownStreams || (long)W->iNUM * W->jNUM * W->kNUM >= (1L << 22));
+	return d && (enabled == 2 || batchOn || d->ownStreams || (long)W->iNUM * W->jNUM * W->kNUM >= (1L << 22));
+}
+
+/* batched launches over the worlds this thread steps (alisBatchBegin):
+ * their TFSF auxiliary columns always ride in the parent's entry */
+void alis_be_batch(int begin)
+{
+	if (begin) {
+		CHECK("batch_begin", alisgpu_batch_begin());
+		batchOn = 1;
+	} else {
+		batchOn = 0;
+		CHECK("batch_end", alisgpu_batch_end());
+	}
 }
 
 /* reference src/update.c:275-299 */

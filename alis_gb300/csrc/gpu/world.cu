@@ -20,6 +20,7 @@
 #include <vector>
 #include <algorithm>
 #include <atomic>
+#include <unordered_map>
 #include <mutex>
 #include <cooperative_groups.h>
 #include "common.cuh"
@@ -271,8 +272,8 @@ struct alisgpu_world {
 	// ALIS_TUNE_STEPS launches, then fixed
 	struct TyTuner {
 		int choice = -1, seen = 0;
-		cudaEvent_t a[15], b[15];
-		int variant[15];
+		cudaEvent_t a[9], b[9];
+		int variant[9];
 	} tune[2];
 	// an auxiliary world's half step waiting to run inside its parent's
 	// launch of the same field
@@ -288,15 +289,24 @@ struct alisgpu_world {
 	float *planeTab;                       // scratch of the observer kernels
 	size_t planeTabFloats;
 	float *sp[2][3];                       // cell spacings (CE, CH) per axis, indexed from MIN
-	unsigned char *matIdx;                 // eps^-1 triple index per cell (few distinct triples)
+	void *matIdx;                          // eps^-1 triple index per cell (few distinct triples)
 	float4 *matTab;
+	int matWide;                           // the index has 16 bits (else 8)
 	// batched stepping: device copies of the half-step parameters per field
 	// and m, of a one-block step, of the source patches and of the ghost
 	// copies; the values of an auxiliary step staged for the parent's
 	// batched launch; the batch group the world last joined
 	ParamSlot bP[2][2], bS[2], bSrc[2], bG[2];
+	long long ghostCells[2];                // cells of the ghost copies in bG
 	std::vector<float> stagedVals[2];
 	unsigned long long batchStamp;
+	// the device form of its TFSF boxes (tfsfFor)
+	struct TfsfCache { const alisgpu_tfsf *key; int field; DevTfsf T; };
+	std::vector<TfsfCache> tfCache;
+	unsigned long long tfEpoch;
+	// what the cell-class tables of each field were made from: the CPML
+	// slabs, the TFSF boxes and the object boxes
+	std::vector<int> clsKey[2];
 };
 
 static inline void bindWorld(const alisgpu_world *w)
@@ -593,36 +603,57 @@ extern "C" int alisgpu_set_eps(alisgpu_world *w, const float *cx, const float *c
 	}
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
 	// the E half step reads (C[0], C[1], C[2]) at the cells of [MIN, MAX]^3:
-	// with at most 256 distinct triples it reads a byte per cell instead
+	// with at most 256 distinct triples it reads a byte per cell instead,
+	// with at most 65536 two bytes (supersampled object edges)
 	if (w->matIdx) { alisgpu__freeAsync(w->matIdx); w->matIdx = 0; }
 	if (w->matTab) { alisgpu__freeAsync(w->matTab); w->matTab = 0; }
+	w->matWide = 0;
 	if (cx && cy && cz) {
 		const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
-		std::vector<unsigned char> idx(w->L.elems(), 0);
+		std::vector<unsigned short> idx(w->L.elems(), 0);
 		std::vector<float4> tab;
-		std::vector<unsigned> bits;                 // 3 words per entry
-		int last = -1;
+		// distinct triples by their bits, numbered in first-seen order
+		struct Key { unsigned b[3]; bool operator==(const Key &o) const { return !memcmp(b, o.b, sizeof b); } };
+		struct KeyHash {
+			size_t operator()(const Key &k) const {
+				unsigned long long h = 0x9e3779b97f4a7c15ull;
+				for (int a = 0; a < 3; a++) h = (h ^ k.b[a]) * 0x100000001b3ull;
+				return (size_t)(h ^ (h >> 29));
+			}
+		};
+		std::unordered_map<Key, int, KeyHash> seen;
+		Key last = { { 0, 0, 0 } };
+		int lastQ = -1;
 		bool ok = true;
 		for (int i = 0; i < ni && ok; i++) for (int j = 0; j < nj && ok; j++) for (int k = 0; k < nk; k++) {
 			const float v[3] = { cx[((size_t)i * nj + j) * nk + k], cy[((size_t)i * (nj + 1) + j) * nk + k],
 			                     cz[((size_t)i * nj + j) * (nk + 1) + k] };
-			unsigned b[3];
-			memcpy(b, v, sizeof b);
-			int q = -1;
-			if (last >= 0 && !memcmp(&bits[3 * last], b, sizeof b)) q = last;
-			for (int e = 0; q < 0 && e < (int)tab.size(); e++) if (!memcmp(&bits[3 * e], b, sizeof b)) q = e;
-			if (q < 0) {
-				if (tab.size() == 256) { ok = false; break; }
-				q = (int)tab.size();
-				tab.push_back(make_float4(v[0], v[1], v[2], 0.0f));
-				bits.insert(bits.end(), b, b + 3);
+			Key key;
+			memcpy(key.b, v, sizeof key.b);
+			int q = lastQ;
+			if (q < 0 || !(key == last)) {
+				auto it = seen.find(key);
+				if (it != seen.end()) q = it->second;
+				else {
+					if (tab.size() == 65536) { ok = false; break; }
+					q = (int)tab.size();
+					seen.emplace(key, q);
+					tab.push_back(make_float4(v[0], v[1], v[2], 0.0f));
+				}
+				last = key, lastQ = q;
 			}
-			last = q;
-			idx[w->L.at(g.iMIN + i, g.jMIN + j, g.kMIN + k)] = (unsigned char)q;
+			idx[w->L.at(g.iMIN + i, g.jMIN + j, g.kMIN + k)] = (unsigned short)q;
 		}
 		if (ok) {
-			ALIS_CUDA(alisgpu__mallocAsync(&w->matIdx, idx.size()));
-			ALIS_CUDA(orderedCopy(w->matIdx, idx.data(), idx.size(), cudaMemcpyHostToDevice));
+			w->matWide = tab.size() > 256;
+			if (w->matWide) {
+				ALIS_CUDA(alisgpu__mallocAsync((unsigned short **)&w->matIdx, idx.size() * sizeof(unsigned short)));
+				ALIS_CUDA(orderedCopy(w->matIdx, idx.data(), idx.size() * sizeof(unsigned short), cudaMemcpyHostToDevice));
+			} else {
+				std::vector<unsigned char> narrow(idx.begin(), idx.end());
+				ALIS_CUDA(alisgpu__mallocAsync((unsigned char **)&w->matIdx, narrow.size()));
+				ALIS_CUDA(orderedCopy(w->matIdx, narrow.data(), narrow.size(), cudaMemcpyHostToDevice));
+			}
 			ALIS_CUDA(alisgpu__mallocAsync(&w->matTab, tab.size() * sizeof(float4)));
 			ALIS_CUDA(orderedCopy(w->matTab, tab.data(), tab.size() * sizeof(float4), cudaMemcpyHostToDevice));
 		}
@@ -1084,7 +1115,7 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 		if (hasC) {
 			if (P.matIdx) {
 				// the same floats from the table of distinct triples
-				const float4 t = __ldg(P.matTab + __ldg(P.matIdx + c));
+				const float4 t = matTriple(P, c);
 				cx[q] = t.x, cy[q] = t.y, cz[q] = t.z;
 			} else {
 				cx[q] = __ldg(P.C[0] + c), cy[q] = __ldg(P.C[1] + c), cz[q] = __ldg(P.C[2] + c);
@@ -1122,34 +1153,64 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 	}
 }
 
-// Fused half step of a large world, one thread per ALIS_KPT cells of a
-// row (k, k + TX, ...), one i plane per block of TX x TY threads.  Tiers
-// by the cell's class bits: plain cells take the curl only; CPML cells
-// and cells on TFSF k face planes add their face updates, all inline;
-// cells on TFSF i or j face planes (whole blocks or warps) and dispersive
-// cells go to hardCell.  Index arithmetic is 32-bit (at most 2^31
-// elements per array, checked on the host).  Worlds with more than 8
-// objects add a per-block list of the objects that meet the tile.
-#ifndef ALIS_KPT
-#define ALIS_KPT 1
-#endif
-template <int ALT, int TY_>
-__device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int plane)
+// A cell with no class bits: the curl alone (reference
+// src/update.c:109-118), with the loads and arithmetic of leanCells.
+template <int ALT>
+__device__ __forceinline__ void plainCell(const HalfStepParams &P, int i, int j, int k)
 {
-	constexpr int KW = TX * ALIS_KPT;
-	__shared__ int tileList[ALIS_TILE_OBJ];
-	__shared__ int nlist;
-	const int k = P.kMIN + blockIdx.x * KW + threadIdx.x;
-	const int j = P.jMIN + blockIdx.y * TY_ + threadIdx.y;
+	const int sj = (int)P.L.sj, si = (int)P.L.si;
+	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
+	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
+	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
+	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
+	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
+	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
+	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
+	if (P.C[0]) {
+		float cx, cy, cz;
+		if (P.matIdx) {
+			const float4 t = matTriple(P, c);
+			cx = t.x, cy = t.y, cz = t.z;
+		} else {
+			cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
+		}
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0)) * cx;
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0)) * cy;
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0)) * cz;
+	} else {
+		fx += (dz * (gy0 - gyk) + dy * (gzj - gz0));
+		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
+		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
+	}
+	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+}
+
+// Fused half step of a large world over one tile: one thread per cell,
+// TX cells of a row along k per warp, TY_ rows, one i plane.  Tiers by
+// the cell's class bits: a warp whose cells have none takes the curl
+// alone on a path without further tests; otherwise plain cells take the
+// curl, CPML cells and cells on TFSF k face planes add their face updates,
+// all inline, and cells on TFSF i or j face planes (whole blocks or
+// warps) and dispersive cells go to hardCell.  Index arithmetic is 32-bit
+// (at most 2^31 elements per array, checked on the host).  Worlds with
+// more than 8 objects add a per-tile list of the objects that meet it
+// (tileList/nlist in shared memory, one block's).
+template <int ALT, int TY_>
+__device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, int by, int plane, int *tileList, int *nlist)
+{
+	const int k = P.kMIN + bx * TX + threadIdx.x;
+	const int j = P.jMIN + by * TY_ + threadIdx.y;
 	// E sweeps i downwards, H upwards: each starts on the planes the other
 	// touched last, which are still in L2
 	const int i = ALT == 1 ? P.iMAX - plane : P.iMIN + plane;
 	const bool manyObj = P.nobj > 8;
 	if (manyObj) {
 		// objects whose box meets this tile, in list order (one warp)
+		__syncthreads();
 		if (threadIdx.y == 0) {
-			const int tj0 = P.jMIN + blockIdx.y * TY_, tj1 = min(tj0 + TY_ - 1, P.jMAX);
-			const int tk0 = P.kMIN + blockIdx.x * KW, tk1 = min(tk0 + KW - 1, P.kMAX);
+			const int tj0 = P.jMIN + by * TY_, tj1 = min(tj0 + TY_ - 1, P.jMAX);
+			const int tk0 = P.kMIN + bx * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
 			int cnt = 0;
 			for (int base = 0; base < P.nobj; base += 32) {
 				int n = base + threadIdx.x;
@@ -1165,42 +1226,37 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int plane
 				}
 				cnt += __popc(bal);
 			}
-			if (threadIdx.x == 0) nlist = cnt;
+			if (threadIdx.x == 0) *nlist = cnt;
 		}
 		__syncthreads();
 	}
-	if (k > P.kMAX || j > P.jMAX) return;
-	const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN));
-	unsigned bk[ALIS_KPT];
-	bool lean = !((bi | bj) & CLS_TFSF);
-#pragma unroll
-	for (int q = 0; q < ALIS_KPT; q++) {
-		const int kq = k + q * TX;
-		bk[q] = kq <= P.kMAX ? __ldg(P.cls[2] + (kq - P.kMIN)) : 0u;
-		if (kq > P.kMAX || (bi & bj & bk[q] & 0x1FFu)) lean = false;
-	}
-	if (lean) {
-		leanCells<ALT, ALIS_KPT>(P, i, j, k, bi, bj, bk);
+	const bool inRange = k <= P.kMAX && j <= P.jMAX;
+	unsigned bi = 0, bj = 0, bk = 0;
+	if (inRange) bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
+	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI | CLS_TFSF)) && !(bi & bj & bk & 0x1FFu);
+	if (__all_sync(0xffffffffu, plain)) {
+		plainCell<ALT>(P, i, j, k);
 		return;
 	}
-	// one cell at a time: hard cells run the full sequence out of line
-	// (object loops: the tile's list, or all objects filtered by class bits)
+	if (!inRange) return;
+	if (!((bi | bj) & CLS_TFSF) && !(bi & bj & bk & 0x1FFu)) {
+		leanCells<ALT, 1>(P, i, j, k, bi, bj, &bk);
+		return;
+	}
+	// hard cells run the full sequence out of line (object loops: the
+	// tile's list, or all objects filtered by class bits)
 	const int *list = 0;
 	int nIter = P.nobj;
-	if (manyObj && nlist <= ALIS_TILE_OBJ) list = tileList, nIter = nlist;
-#pragma unroll
-	for (int q = 0; q < ALIS_KPT; q++) {
-		const int kq = k + q * TX;
-		if (kq > P.kMAX) break;
-		if (((bi | bj) & CLS_TFSF) || (bi & bj & bk[q] & 0x1FFu)) hardCell<ALT>(P, i, j, kq, list, nIter);
-		else leanCells<ALT, 1>(P, i, j, kq, bi, bj, bk + q);
-	}
+	if (manyObj && *nlist <= ALIS_TILE_OBJ) list = tileList, nIter = *nlist;
+	hardCell<ALT>(P, i, j, k, list, nIter);
 }
 
 template <int ALT, int TY>
 __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
-	halfStepBlock<ALT, TY>(P, (int)blockIdx.z);
+	__shared__ int tileList[ALIS_TILE_OBJ];
+	__shared__ int nlist;
+	halfStepBlock<ALT, TY>(P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, tileList, &nlist);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1548,207 +1604,9 @@ __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const 
 		if (blockIdx.x == 0 && blockIdx.y == 0) smallStepBlock<ALT>(F.aux, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
 		return;
 	}
-	halfStepBlock<ALT, TY>(F.P, (int)blockIdx.z - 1);
-}
-
-// ---------------------------------------------------------------------
-// Marching form of the half step.  A warp owns a tile of 32 cells along k
-// and RJ rows along j and walks a chunk of i planes in the direction in
-// which the i neighbour it reads was the plane before: E (neighbour
-// i + 1) walks down, H (neighbour i - 1) walks up.  The i neighbour's two
-// components stay in registers from the plane before, the j neighbours of
-// all but the edge row are the next row's registers, and the line tables
-// and class bits of j and k are read once per tile.  So a plain cell
-// loads its three G components, its three F components and its
-// material index from DRAM, the two k neighbours from L1, and nothing
-// else.  Cells with CPML or TFSF k-plane bits add their face updates
-// inline; TFSF i/j planes and dispersive cells run the full sequence out
-// of line (hardCell), which reads everything itself.  The arithmetic of
-// every cell is that of stepCell, term for term.
-//
-// Work items are (i chunk, j tile, k tile) triples, k tile fastest, the
-// i chunks in the marching direction; the grid holds one wave of resident
-// blocks and each block takes items blockIdx.x, blockIdx.x + nblocks, ...
-// A fused launch adds one block (the last) that runs the TFSF auxiliary
-// column's half step.
-// ---------------------------------------------------------------------
-#define MARCH_WARPS 4
-#define MARCH_THREADS (32 * MARCH_WARPS)
-#ifndef MARCH_MINB
-#define MARCH_MINB 4
-#endif
-
-struct MarchShape {
-	int nkt, njt, nic;                  // k tiles, j tiles, i chunks
-	int ni;                             // planes per i chunk
-	int nblocks;                        // blocks taking items (the grid, less a fused auxiliary block)
-};
-
-template <int ALT, int RJ>
-__device__ __forceinline__ void marchItem(const HalfStepParams &P, const MarchShape &M, int item, int *tileList, int *nlist)
-{
-	const int kt = item % M.nkt, jt = (item / M.nkt) % M.njt, ic = item / (M.nkt * M.njt);
-	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-	const int k = P.kMIN + kt * 32 + lane;
-	const int j0 = P.jMIN + (jt * MARCH_WARPS + warp) * RJ;
-	// planes of the chunk: chunk 0 is where the march of this field starts
-	const int ni = P.iMAX - P.iMIN + 1;
-	const int lo = ALT == 1 ? max(ni - (ic + 1) * M.ni, 0) : ic * M.ni;
-	const int hi = ALT == 1 ? ni - ic * M.ni - 1 : min((ic + 1) * M.ni, ni) - 1;
-	const int iFirst = ALT == 1 ? P.iMIN + hi : P.iMIN + lo, iLast = ALT == 1 ? P.iMIN + lo : P.iMIN + hi;
-	const bool manyObj = P.nobj > 8;
-	if (manyObj) {
-		// objects whose box meets this item's cells, in list order (warp 0)
-		__syncthreads();
-		if (warp == 0) {
-			const int ti0 = min(iFirst, iLast), ti1 = max(iFirst, iLast);
-			const int tj0 = P.jMIN + jt * MARCH_WARPS * RJ, tj1 = min(tj0 + MARCH_WARPS * RJ - 1, P.jMAX);
-			const int tk0 = P.kMIN + kt * 32, tk1 = min(tk0 + 31, P.kMAX);
-			int cnt = 0;
-			for (int base = 0; base < P.nobj; base += 32) {
-				const int n = base + lane;
-				bool hit = false;
-				if (n < P.nobj) {
-					const DevObj &o = P.obj[n];
-					hit = ti1 >= o.i0 && ti0 <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
-				}
-				const unsigned bal = __ballot_sync(0xffffffffu, hit);
-				if (hit) {
-					const int pos = cnt + __popc(bal & ((1u << lane) - 1));
-					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
-				}
-				cnt += __popc(bal);
-			}
-			if (lane == 0) *nlist = cnt;
-		}
-		__syncthreads();
-	}
-	if (k > P.kMAX || j0 > P.jMAX) return;
-	const int *list = 0;
-	int nIter = P.nobj;
-	if (manyObj && *nlist <= ALIS_TILE_OBJ) list = tileList, nIter = *nlist;
-
-	const int sj = (int)P.L.sj, si = (int)P.L.si;
-	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
-	float *Fx = P.F[0], *Fy = P.F[1], *Fz = P.F[2];
-	const bool hasC = P.C[0] != 0;
-	// per tile: rows in range, their class bits and dt/dy; the lane's k bits and dt/dz
-	const unsigned bk = __ldg(P.cls[2] + (k - P.kMIN));
-	const float dz = __ldg(P.dtd[2] + (k - P.kMIN));
-	unsigned bj[RJ];
-	float dy[RJ];
-	bool row[RJ];
-#pragma unroll
-	for (int r = 0; r < RJ; r++) {
-		row[r] = j0 + r <= P.jMAX;
-		bj[r] = row[r] ? __ldg(P.cls[1] + (j0 + r - P.jMIN)) : 0u;
-		dy[r] = row[r] ? __ldg(P.dtd[1] + (j0 + r - P.jMIN)) : 0.f;
-	}
-	// the i neighbour (z and y components) of the first plane
-	int c = (iFirst - P.L.i0) * si + (j0 - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
-	float nz[RJ], ny[RJ];
-#pragma unroll
-	for (int r = 0; r < RJ; r++) if (row[r]) nz[r] = __ldg(Gz + c + r * sj + ALT * si), ny[r] = __ldg(Gy + c + r * sj + ALT * si);
-	for (int i = iFirst;; i -= ALT, c -= ALT * si) {
-		const unsigned bi = __ldg(P.cls[0] + (i - P.iMIN));
-		const float dx = __ldg(P.dtd[0] + (i - P.iMIN));
-		float gx[RJ], gy[RJ], gz[RJ], gxk[RJ], gyk[RJ], fx[RJ], fy[RJ], fz[RJ], cx[RJ], cy[RJ], cz[RJ];
-#pragma unroll
-		for (int r = 0; r < RJ; r++) {
-			if (!row[r]) continue;
-			const int cr = c + r * sj;
-			gx[r] = __ldg(Gx + cr), gy[r] = __ldg(Gy + cr), gz[r] = __ldg(Gz + cr);
-			gxk[r] = __ldg(Gx + cr + ALT), gyk[r] = __ldg(Gy + cr + ALT);
-			fx[r] = Fx[cr], fy[r] = Fy[cr], fz[r] = Fz[cr];
-			cx[r] = 1, cy[r] = 1, cz[r] = 1;
-			if (hasC) {
-				if (P.matIdx) {
-					const float4 t = __ldg(P.matTab + __ldg(P.matIdx + cr));
-					cx[r] = t.x, cy[r] = t.y, cz[r] = t.z;
-				} else {
-					cx[r] = __ldg(P.C[0] + cr), cy[r] = __ldg(P.C[1] + cr), cz[r] = __ldg(P.C[2] + cr);
-				}
-			}
-		}
-		// j neighbours: the adjacent row's registers, the edge row's from memory
-		float gzj[RJ], gxj[RJ];
-#pragma unroll
-		for (int r = 0; r < RJ; r++) {
-			if (!row[r]) continue;
-			const int q = r + ALT;
-			if (q >= 0 && q < RJ && row[q]) gzj[r] = gz[q], gxj[r] = gx[q];
-			else gzj[r] = __ldg(Gz + c + r * sj + ALT * sj), gxj[r] = __ldg(Gx + c + r * sj + ALT * sj);
-		}
-		unsigned hard = 0;
-#pragma unroll
-		for (int r = 0; r < RJ; r++) {
-			if (!row[r]) continue;
-			const int j = j0 + r, cr = c + r * sj;
-			if (((bi | bj[r]) & CLS_TFSF) || (bi & bj[r] & bk & 0x1FFu)) {
-				hard |= 1u << r;
-			} else {
-				float ex = fx[r], ey = fy[r], ez = fz[r];
-				const float gzi = nz[r], gyi = ny[r];
-				// curl (reference src/update.c:109-118)
-				if (hasC) {
-					ex += (dz * (gy[r] - gyk[r]) + dy[r] * (gzj[r] - gz[r])) * cx[r];
-					ey += (dx * (gz[r] - gzi) + dz * (gxk[r] - gx[r])) * cy[r];
-					ez += (dy[r] * (gx[r] - gxj[r]) + dx * (gyi - gy[r])) * cz[r];
-				} else {
-					ex += (dz * (gy[r] - gyk[r]) + dy[r] * (gzj[r] - gz[r]));
-					ey += (dx * (gz[r] - gzi) + dz * (gxk[r] - gx[r]));
-					ez += (dy[r] * (gx[r] - gxj[r]) + dx * (gyi - gy[r]));
-				}
-				// CPML faces in the reference order xMin, yMin, zMin, xMax, yMax, zMax
-				if ((bi | bj[r] | bk) & (CLS_PML_LO | CLS_PML_HI)) {
-#define PML_ARGS P, i, j, k, ex, ey, ez, gx[r], gy[r], gz[r], gyk[r], gxk[r], gzj[r], gxj[r], gzi, gyi, hasC, cx[r], cy[r], cz[r]
-					if (bi & CLS_PML_LO) pmlFace<0>(PML_ARGS);
-					if (bj[r] & CLS_PML_LO) pmlFace<1>(PML_ARGS);
-					if (bk & CLS_PML_LO) pmlFace<2>(PML_ARGS);
-					if (bi & CLS_PML_HI) pmlFace<3>(PML_ARGS);
-					if (bj[r] & CLS_PML_HI) pmlFace<4>(PML_ARGS);
-					if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
-#undef PML_ARGS
-				}
-				// TFSF k face planes (cells on an i or j face plane are hard)
-				if (bk & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, k, ex, ey, ez, hasC, cx[r], cy[r], cz[r]);
-				Fx[cr] = ex, Fy[cr] = ey, Fz[cr] = ez;
-			}
-			nz[r] = gz[r], ny[r] = gy[r];
-		}
-		// hard cells after the plane's lean ones: only the carried state is
-		// live across the out-of-line calls
-		if (hard) {
-#pragma unroll
-			for (int r = 0; r < RJ; r++) if ((hard >> r) & 1u) hardCell<ALT>(P, i, j0 + r, k, list, nIter);
-		}
-		if (i == iLast) break;
-	}
-}
-
-template <int ALT, int RJ>
-__device__ __forceinline__ void marchBlock(const HalfStepParams &P, const MarchShape &M)
-{
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	const int items = M.nkt * M.njt * M.nic;
-	for (int item = blockIdx.x; item < items; item += M.nblocks) marchItem<ALT, RJ>(P, M, item, tileList, &nlist);
-}
-
-template <int ALT, int RJ>
-__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march(const __grid_constant__ HalfStepParams P, const MarchShape M)
-{
-	marchBlock<ALT, RJ>(P, M);
-}
-
-template <int ALT, int RJ>
-__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march_aux(const __grid_constant__ FusedStepParams F, const MarchShape M)
-{
-	if (blockIdx.x == M.nblocks) {
-		smallStepBlock<ALT>(F.aux, threadIdx.x, blockDim.x);
-		return;
-	}
-	marchBlock<ALT, RJ>(F.P, M);
+	halfStepBlock<ALT, TY>(F.P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z - 1, tileList, &nlist);
 }
 
 // one half-step launch with block height kTyChoice[v] (v a runtime choice)
@@ -1768,10 +1626,13 @@ static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const Fuse
 // ---------------------------------------------------------------------
 // Batched launches over many worlds (batch.cuh)
 // ---------------------------------------------------------------------
-struct BatchEntry {                    // the cells of one world (one m) in a batched march
+// the tiles of a batched entry: nbx x nby tiles of 32 x BATCH_TY cells
+// per i plane, planes in the half step's sweep order
+#define BATCH_TY 4
+struct BatchEntry {                    // the cells of one world (one m) in a batched launch
 	const HalfStepParams *P;           // its device slot
-	MarchShape M;
-	int itemStart;                     // its first item in the launch
+	int nbx, nby, planes;
+	int itemStart;                     // its first tile in the launch
 };
 struct BatchBlock {                    // a half step run by one block (auxiliary column, tiny world)
 	const SmallStepParams *S;          // its device slot
@@ -1785,27 +1646,29 @@ struct BatchGhost {                    // the ghost copies of one world
 	const GhostLevels *G;
 	int start;                         // its first thread in the launch
 };
-struct BatchMarch {
+struct BatchStep {
 	const BatchEntry *E;
-	int nE, nitems, per;               // entries, items, items per block
+	int nE, nitems, per;               // entries, tiles, tiles per block
 	const BatchBlock *blk;
 	int nblk;                          // one-block steps: the first nblk blocks
 	const float *vals;
 };
 
 // One launch over every world of a group: the first blocks run the
-// one-block steps, the others take `per` consecutive items each of the
-// concatenated marches, the world's parameters copied to shared memory
-// whenever an item belongs to another entry than the block's last one.
-template <int ALT, int RJ>
-__global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march_batch(const BatchMarch B)
+// one-block steps, the others take `per` consecutive tiles each of the
+// concatenated worlds, the world's parameters copied to shared memory
+// whenever a tile belongs to another entry than the block's last one.
+// Each tile runs halfStepBlock, the code of the one-world launch.
+template <int ALT>
+__global__ void __launch_bounds__(TX * BATCH_TY, STEP_MINB(BATCH_TY)) k_step_batch(const BatchStep B)
 {
 	__shared__ HalfStepParams sP;
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
+	const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
 	if ((int)blockIdx.x < B.nblk) {
 		const BatchBlock &b = B.blk[blockIdx.x];
-		smallStepBlock<ALT>(*b.S, threadIdx.x, blockDim.x, b.voff >= 0 ? B.vals + b.voff : 0);
+		smallStepBlock<ALT>(*b.S, tid, nth, b.voff >= 0 ? B.vals + b.voff : 0);
 		return;
 	}
 	const int g0 = ((int)blockIdx.x - B.nblk) * B.per, g1 = min(g0 + B.per, B.nitems);
@@ -1816,15 +1679,17 @@ __global__ void __launch_bounds__(MARCH_THREADS, MARCH_MINB) k_march_batch(const
 			const int mid = (lo + hi + 1) >> 1;
 			if (B.E[mid].itemStart <= g) lo = mid; else hi = mid - 1;
 		}
+		const BatchEntry &e = B.E[lo];
 		if (lo != cur) {
 			__syncthreads();
-			const long long *src = reinterpret_cast<const long long *>(B.E[lo].P);
+			const long long *src = reinterpret_cast<const long long *>(e.P);
 			long long *dst = reinterpret_cast<long long *>(&sP);
-			for (int q = threadIdx.x; q < (int)(sizeof(HalfStepParams) / sizeof(long long)); q += blockDim.x) dst[q] = src[q];
+			for (int q = tid; q < (int)(sizeof(HalfStepParams) / sizeof(long long)); q += nth) dst[q] = src[q];
 			__syncthreads();
 			cur = lo;
 		}
-		marchItem<ALT, RJ>(sP, B.E[lo].M, g - B.E[lo].itemStart, tileList, &nlist);
+		const int t = g - e.itemStart;
+		halfStepBlock<ALT, BATCH_TY>(sP, t % e.nbx, (t / e.nbx) % e.nby, t / (e.nbx * e.nby), tileList, &nlist);
 	}
 }
 
@@ -1959,32 +1824,8 @@ extern "C" void alisgpu__slot_free(ParamSlot *s)
 	s->host.clear();
 }
 
-// march rows and shape of a batched entry: chunks of up to 16 planes (the
-// worlds of a group fill the GPU together)
-static int batchRows(void)
-{
-	static int rows = 0;
-	if (!rows) {
-		const char *e = getenv("ALISGPU_BATCH_ROWS");
-		rows = e && atoi(e) == 2 ? 2 : 4;
-	}
-	return rows;
-}
-
-static MarchShape batchShape(const alisgpu_geometry &g, int rows)
-{
-	MarchShape M;
-	const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
-	M.nkt = (nk + 31) / 32;
-	M.njt = (nj + MARCH_WARPS * rows - 1) / (MARCH_WARPS * rows);
-	M.ni = std::min(ni, 16);
-	M.nic = (ni + M.ni - 1) / M.ni;
-	M.nblocks = 0;
-	return M;
-}
-
-template <int ALT, int RJ>
-static int launchMarchBatch(const BatchMarch &B0, cudaStream_t st)
+template <int ALT>
+static int launchStepBatch(const BatchStep &B0, cudaStream_t st)
 {
 	static std::atomic<int> residentAt{0};
 	int resident = residentAt.load();
@@ -1992,19 +1833,19 @@ static int launchMarchBatch(const BatchMarch &B0, cudaStream_t st)
 		int dev = 0, sms = 0, per = 0;
 		ALIS_CUDA(cudaGetDevice(&dev));
 		ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_march_batch<ALT, RJ>, MARCH_THREADS, 0));
+		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_batch<ALT>, TX * BATCH_TY, 0));
 		resident = std::max(1, sms * per);
 		residentAt.store(resident);
 	}
-	BatchMarch B = B0;
+	BatchStep B = B0;
 	B.per = std::max(1, (B.nitems + resident - 1) / resident);
 	const unsigned blocks = (unsigned)B.nblk + (unsigned)((B.nitems + B.per - 1) / B.per);
-	if (blocks) k_march_batch<ALT, RJ><<<blocks, MARCH_THREADS, 0, st>>>(B);
+	if (blocks) k_step_batch<ALT><<<blocks, dim3(TX, BATCH_TY), 0, st>>>(B);
 	return ALISGPU_OK;
 }
 
 // launch the open half-step group: its tables and the changed slots go up
-// in one copy, then the march, the sources and the ghost copies of every
+// in one copy, then the cells, the sources and the ghost copies of every
 // world, each one launch
 static int launchHalfGroup(int field)
 {
@@ -2033,14 +1874,12 @@ static int launchHalfGroup(int field)
 		ALIS_CUDA(cudaMemcpyAsync(u.dst, d + oU + u.off, u.bytes, cudaMemcpyDeviceToDevice, gStream));
 	const float *vals = (const float *)(d + oV);
 	if (!R.entries.empty() || !R.blocks.empty()) {
-		BatchMarch B;
+		BatchStep B;
 		B.E = (const BatchEntry *)(d + oE), B.nE = (int)R.entries.size(), B.nitems = R.nitems, B.per = 1;
 		B.blk = (const BatchBlock *)(d + oB), B.nblk = (int)R.blocks.size();
 		B.vals = vals;
 		int slot = alisgpu__prof_start();
-		const int rows = batchRows();
-		if (field == 0) rc = rows == 2 ? launchMarchBatch<1, 2>(B, gStream) : launchMarchBatch<1, 4>(B, gStream);
-		else rc = rows == 2 ? launchMarchBatch<-1, 2>(B, gStream) : launchMarchBatch<-1, 4>(B, gStream);
+		rc = field == 0 ? launchStepBatch<1>(B, gStream) : launchStepBatch<-1>(B, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 		if (rc) return rc;
@@ -2120,59 +1959,6 @@ extern "C" int alisgpu__batch_flush(void)
 	return batchLaunch();
 }
 
-// Launch shapes of the half step the tuner picks from: k_half_step with
-// blocks of 32 x 2, 32 x 4 or 32 x 8 threads over one plane, or k_march
-// with warps of 2 or 4 rows.
-#define ALIS_SHAPES 5
-#define ALIS_SHAPE_MARCH0 3
-static const int kMarchRows[2] = { 2, 4 };
-
-// Items and blocks of a march over a world: k tiles x j tiles x i chunks
-// of at most 8 planes (fewer when the tiles alone do not fill the
-// resident blocks), and as many blocks as give every block the same
-// number of items, within one wave of resident blocks.
-template <int ALT, int RJ>
-static int marchShape(const alisgpu_geometry &g, MarchShape &M)
-{
-	static std::atomic<int> residentAt{0};
-	int resident = residentAt.load();
-	if (!resident) {
-		int dev = 0, sms = 0, per = 0;
-		ALIS_CUDA(cudaGetDevice(&dev));
-		ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_march<ALT, RJ>, MARCH_THREADS, 0));
-		resident = std::max(1, sms * per);
-		residentAt.store(resident);
-	}
-	const int ni = g.iMAX - g.iMIN + 1, nj = g.jMAX - g.jMIN + 1, nk = g.kMAX - g.kMIN + 1;
-	M.nkt = (nk + 31) / 32;
-	M.njt = (nj + MARCH_WARPS * RJ - 1) / (MARCH_WARPS * RJ);
-	const long long tiles = (long long)M.nkt * M.njt;
-	M.ni = (int)std::max(1LL, std::min(8LL, tiles * ni / (4LL * resident)));
-	M.nic = (ni + M.ni - 1) / M.ni;
-	const long long items = tiles * M.nic;
-	const long long per = (items + resident - 1) / resident;
-	M.nblocks = (int)((items + per - 1) / per);
-	return ALISGPU_OK;
-}
-
-template <int ALT>
-static int launchMarch(int rows, const alisgpu_geometry &g, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
-{
-	MarchShape M;
-	int rc = rows == 2 ? marchShape<ALT, 2>(g, M) : marchShape<ALT, 4>(g, M);
-	if (rc) return rc;
-	const unsigned blocks = (unsigned)M.nblocks + (F ? 1u : 0u);
-	if (rows == 2) {
-		if (F) k_march_aux<ALT, 2><<<blocks, MARCH_THREADS, 0, st>>>(*F, M);
-		else k_march<ALT, 2><<<blocks, MARCH_THREADS, 0, st>>>(P, M);
-	} else {
-		if (F) k_march_aux<ALT, 4><<<blocks, MARCH_THREADS, 0, st>>>(*F, M);
-		else k_march<ALT, 4><<<blocks, MARCH_THREADS, 0, st>>>(P, M);
-	}
-	return ALISGPU_OK;
-}
-
 // ---------------------------------------------------------------------
 // host driver of one half step
 // ---------------------------------------------------------------------
@@ -2200,28 +1986,29 @@ static void fillTfsf(DevTfsf &T, const alisgpu_tfsf &s, int field, const float *
 }
 
 // cached dt/ds face values: the TFSF box is fixed once set up
-struct TfsfCache { const alisgpu_tfsf *key; int field; DevTfsf T; };
-static std::vector<TfsfCache> gTfsfCache;
-static std::mutex gTfsfLock;
+// The device form of a world's TFSF boxes, kept per world (a world has a
+// few); an epoch counter drops every world's entries when a box the host
+// layer frees may have left its address for a new one.
+static std::atomic<unsigned long long> gTfsfEpoch{1};
 
 static DevTfsf tfsfFor(alisgpu_world *w, const alisgpu_tfsf &s, int field)
 {
-	std::lock_guard<std::mutex> lock(gTfsfLock);
-	for (TfsfCache &c : gTfsfCache)
+	const unsigned long long epoch = gTfsfEpoch.load();
+	if (w->tfEpoch != epoch) w->tfCache.clear(), w->tfEpoch = epoch;
+	for (alisgpu_world::TfsfCache &c : w->tfCache)
 		if (c.key == &s && c.field == field && c.T.iMin == s.iMin && c.T.kMax == s.kMax && c.T.L.ni == s.aux->L.ni) return c.T;
-	TfsfCache c;
+	alisgpu_world::TfsfCache c;
 	c.key = &s, c.field = field;
 	const float *dtd[3] = { w->dtd[field][0], w->dtd[field][1], w->dtd[field][2] };
 	fillTfsf(c.T, s, field, dtd, w->g);
-	gTfsfCache.push_back(c);
+	w->tfCache.push_back(c);
 	return c.T;
 }
 
 extern "C" void alisgpu__forget_tfsf(const alisgpu_tfsf *s)
 {
-	std::lock_guard<std::mutex> lock(gTfsfLock);
-	for (size_t q = 0; q < gTfsfCache.size();)
-		if (gTfsfCache[q].key == s) gTfsfCache.erase(gTfsfCache.begin() + q); else q++;
+	(void)s;
+	gTfsfEpoch++;
 }
 
 // ghost copies in list order; consecutive copies of distinct components
@@ -2240,6 +2027,14 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 {
 	const alisgpu_geometry &g = w->g;
 	if (n <= 0) return ALISGPU_OK;
+	if (record && w->ghostChain[field] && w->bG[field].dev && w->ghostSeen[field].size() == (size_t)n &&
+	    !memcmp(w->ghostSeen[field].data(), gl, n * sizeof *gl)) {
+		// the list of the last recorded half step: its one-launch form is in the slot
+		if (gRec.ghostTotal + w->ghostCells[field] >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: ghost copies exceed 32-bit indexing");
+		gRec.ghosts.push_back(BatchGhost{ (const GhostLevels *)w->bG[field].dev, gRec.ghostTotal });
+		gRec.ghostTotal += (int)w->ghostCells[field];
+		return ALISGPU_OK;
+	}
 	if (n <= ALIS_GHOST_MAX) {
 		// dependency levels: written box W, read box R = W shifted
 		int lev[ALIS_GHOST_MAX], nlev = 0;
@@ -2417,8 +2212,9 @@ static int applyPendingGhosts(alisgpu_world *w)
 // half steps of the field cycle through the shapes with events around
 // them; once every one of them has completed, the shape with the least
 // time (each shape's fastest run) stays.  ALISGPU_TUNE=0 keeps 32 x 4.
-#define ALIS_TUNE_STEPS 15
-#define ALIS_SHAPE_DEFAULT 4
+#define ALIS_TUNE_STEPS 9
+#define ALIS_SHAPE_DEFAULT 1
+#define ALIS_SHAPES ALIS_TY_CHOICES
 static int tunedShape(alisgpu_world *w, int field, bool *timed)
 {
 	alisgpu_world::TyTuner &t = w->tune[field];
@@ -2511,13 +2307,14 @@ static int recordGhosts(alisgpu_world *w, int field, const GhostLevels &GL, long
 	const void *dG = 0;
 	int rc = alisgpu__slot_sync(&w->bG[field], &GL, sizeof GL, &dG);
 	if (rc) return rc;
+	w->ghostCells[field] = total;
 	if (gRec.ghostTotal + total >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: ghost copies exceed 32-bit indexing");
 	gRec.ghosts.push_back(BatchGhost{ (const GhostLevels *)dG, gRec.ghostTotal });
 	gRec.ghostTotal += (int)total;
 	return ALISGPU_OK;
 }
 
-// A large world's half step in the open batch group: a march entry per
+// A large world's half step in the open batch group: an entry per
 // field set m, the TFSF auxiliary column's staged step as a one-block
 // entry, the source patches and the ghost copies (H; E's wait for the
 // next host read as usual).  P: the step's parameters with the per-world
@@ -2526,7 +2323,6 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 {
 	const alisgpu_geometry &g = w->g;
 	const int field = s->field;
-	const int rows = batchRows();
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -2537,13 +2333,14 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 		}
 		P.matIdx = field == 0 ? w->matIdx : 0;
 		P.matTab = field == 0 ? w->matTab : 0;
+		P.matWide = w->matWide;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
 		const void *dP = 0;
 		int rc = alisgpu__slot_sync(&w->bP[field][m], &P, sizeof P, &dP);
 		if (rc) return rc;
-		const MarchShape M = batchShape(g, rows);
-		gRec.entries.push_back(BatchEntry{ (const HalfStepParams *)dP, M, gRec.nitems });
-		const long long items = (long long)gRec.nitems + (long long)M.nkt * M.njt * M.nic;
+		const int nbx = (g.kMAX - g.kMIN + TX) / TX, nby = (g.jMAX - g.jMIN + BATCH_TY) / BATCH_TY, planes = g.iMAX - g.iMIN + 1;
+		gRec.entries.push_back(BatchEntry{ (const HalfStepParams *)dP, nbx, nby, planes, gRec.nitems });
+		const long long items = (long long)gRec.nitems + (long long)nbx * nby * planes;
 		if (items >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: too many items");
 		gRec.nitems = (int)items;
 	}
@@ -2612,7 +2409,23 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	P.err = gErrWord;
 
 	// per-axis classification: CPML slabs, TFSF planes, object ranges
-	{
+	// (made again only when one of them changed)
+	static thread_local std::vector<int> key;
+	key.clear();
+	for (int f = 0; f < 6; f++) key.push_back(P.slabOn[f]), key.push_back(P.slabLo[f]), key.push_back(P.slabHi[f]);
+	for (int q = 0; q < P.ntfsf; q++) {
+		const DevTfsf &T = P.tf[q];
+		const int b[6] = { T.iMin, T.iMax, T.jMin, T.jMax, T.kMin, T.kMax };
+		key.insert(key.end(), b, b + 6);
+	}
+	for (const DevObj &o : w->objs) {
+		const int b[6] = { o.i0, o.i1, o.j0, o.j1, o.k0, o.k1 };
+		key.insert(key.end(), b, b + 6);
+	}
+	if (key == w->clsKey[field] && w->cls[field][0] && w->cls[field][1] && w->cls[field][2]) {
+		for (int a = 0; a < 3; a++) P.cls[a] = w->cls[field][a];
+	} else {
+		w->clsKey[field] = key;
 		int n[3] = { g.iMAX - g.iMIN + 1, g.jMAX - g.jMIN + 1, g.kMAX - g.kMIN + 1 };
 		int lo0[3] = { g.iMIN, g.jMIN, g.kMIN }, hi0[3] = { g.iMAX, g.jMAX, g.kMAX };
 		std::vector<unsigned short> t[3];
@@ -2762,9 +2575,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	const int ni = g.iMAX - g.iMIN + 1;
 	bool timed = false, fused = false;
 	const int v = tunedShape(w, field, &timed);
-	const bool march = v >= ALIS_SHAPE_MARCH0;
-	const int ty = march ? 4 : kTyChoice[v], rows = march ? kMarchRows[v - ALIS_SHAPE_MARCH0] : 0;
-	dim3 grid((g.kMAX - g.kMIN + TX * ALIS_KPT) / (TX * ALIS_KPT), (g.jMAX - g.jMIN + ty) / ty, ni);
+	const int ty = kTyChoice[v];
+	dim3 grid((g.kMAX - g.kMIN + TX) / TX, (g.jMAX - g.jMIN + ty) / ty, ni);
 	if (timed) ALIS_CUDA(cudaEventRecord(w->tune[field].a[w->tune[field].seen], gStream));
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
@@ -2776,6 +2588,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		}
 		P.matIdx = field == 0 ? w->matIdx : 0;
 		P.matTab = field == 0 ? w->matTab : 0;
+		P.matWide = w->matWide;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
 		int slot = alisgpu__prof_start();
 		alisgpu_world *aux = s->ntfsf == 1 && m == 0 ? s->tfsf[0].aux : 0;
@@ -2786,14 +2599,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			FP.aux = *aux->staged[field];
 			aux->stagedValid[field] = false;
 			fused = true;
-			if (march) {
-				int rc = field == 0 ? launchMarch<1>(rows, g, P, &FP, gStream) : launchMarch<-1>(rows, g, P, &FP, gStream);
-				if (rc) return rc;
-			} else if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
+			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
 			else launchHalfStep<-1>(v, grid, P, &FP, gStream);
-		} else if (march) {
-			int rc = field == 0 ? launchMarch<1>(rows, g, P, 0, gStream) : launchMarch<-1>(rows, g, P, 0, gStream);
-			if (rc) return rc;
 		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream);
 		else launchHalfStep<-1>(v, grid, P, 0, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);

@@ -102,6 +102,9 @@ void alis_be_vox_end(void *v);
 void alis_be_world_streams(world W);
 /* Flush and sync everything the backend holds (end of a timed loop). */
 void alis_be_sync_all(void);
+/* begin (1) or end (0) recording the steps of many worlds into batched
+ * launches (a backend without batching does nothing) */
+void alis_be_batch(int begin);
 
 /*
  * Near-to-far-field face sums for one phaser and a batch of nA directions.

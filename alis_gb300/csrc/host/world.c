@@ -493,6 +493,16 @@ void alisWorldStreams(world W)
 	alis_be_world_streams(W);
 }
 
+void alisBatchBegin(void)
+{
+	alis_be_batch(1);
+}
+
+void alisBatchEnd(void)
+{
+	alis_be_batch(0);
+}
+
 
 /* --- HDF5 I/O (reference src/world.c:469-537) ---
  * libhdf5 is not part of this build; the two entry points exist so that

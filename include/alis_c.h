@@ -154,6 +154,15 @@ void h5write(int*, float*, char*, ...);
  * worlds driven in turn overlap on the device. */
 void alisSyncHost(world W);
 void alisWorldStreams(world W);
+/* Engine additions (no reference counterpart): between alisBatchBegin and
+ * alisBatchEnd the updateE, updateH and updatePhaser calls of many worlds
+ * (on the shared streams, not alisWorldStreams) are recorded, and the
+ * calls of one kind run as a few launches over all those worlds -- one
+ * launch steps the cells of every world.  Each world's results are those
+ * of the same calls made one world at a time.  Each host thread records
+ * its own calls. */
+void alisBatchBegin(void);
+void alisBatchEnd(void);
 
 
 /* ---- objects and shapes (reference src/alis_c.h:144-176) ---- */

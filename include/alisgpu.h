@@ -193,6 +193,15 @@ typedef struct alisgpu_half_step {
 	                                               (one launch) when both forms allow it */
 } alisgpu_half_step;
 
+/* Batched launches (no counterpart in the reference): between these two
+ * calls the calling thread's alisgpu_half_step_run and
+ * alisgpu_phaser_record calls on worlds of the shared streams are
+ * recorded; consecutive calls of one kind (E half steps, H half steps,
+ * phaser samples) on distinct worlds run as a few launches over all of
+ * them.  Any other call on a world launches what was recorded first. */
+int alisgpu_batch_begin(void);
+int alisgpu_batch_end(void);
+
 /* One half step of a world: conductivity, ADE subtraction, curl with
  * eps^-1, CPML psi (and, for H, the ADE current update driven by E),
  * TFSF face corrections, sources, ghost copies -- bit-identical to the

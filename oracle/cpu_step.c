@@ -741,3 +741,4 @@ void alis_be_nonlinear(world WS, world WP1, world WP2, float Alt)
 }
 
 void alis_be_sync_all(void) {}
+void alis_be_batch(int begin) { (void)begin; }

@@ -128,17 +128,16 @@ def test_attached_auxiliary_column_bit_identical(scene, scale, steps):
     assert not bad, "differs from the oracle: %s" % bad[:10]
 
 
-# the launch shapes of the large-world half step (ALISGPU_STEP_SHAPE):
-# 0-2 one plane per block of 32 x 2, 32 x 4, 32 x 8 threads; 3-4 the
-# marching form with warps of 2 or 4 rows.  Scenes with CPML on every
-# face, TFSF boxes, many dispersive objects, complex fields, a graded
+# the launch shapes of the large-world half step (ALISGPU_STEP_SHAPE): one
+# plane per block of 32 x 2, 32 x 4 or 32 x 8 threads.  Scenes with CPML on
+# every face, TFSF boxes, many dispersive objects, complex fields, a graded
 # grid, PEC walls, rows longer than one warp.
 SHAPE_SCENES = [c for c in scenes.CASES if (c[0], c[1]) in
                 (("c2", 1), ("c2", 2), ("bloch", 1), ("spheres", 1), ("unitcell", 1), ("nug", 1), ("pec", 1), ("multi", 1))]
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("shape", [0, 2, 3, 4])
+@pytest.mark.parametrize("shape", [0, 1, 2])
 @pytest.mark.parametrize("scene,scale,steps", SHAPE_SCENES, ids=["%s-x%d" % (c[0], c[1]) for c in SHAPE_SCENES])
 def test_every_launch_shape_bit_identical(scene, scale, steps, shape):
     gpu = scenes.run("engine", scene, scale, steps, env={"ALISGPU_STEP_SHAPE": str(shape)})

@@ -85,3 +85,21 @@ def test_served_unit_cell_sweep_equals_sequential():
     oracle, _ = _run(_oracle_serve(), ["sequential", 12, 2000, 7, "sweep"], env)
     assert oracle == served
     print("sweep: served %.2f Gcell/s, sequential %.2f Gcell/s" % (s1["gcell_per_s"], s2["gcell_per_s"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mix,n,env", [("small", 24, {}), ("sweep", 12, {"SERVE_STEPS": "400"})], ids=["small", "sweep"])
+def test_batched_results_equal_sequential(mix, n, env):
+    """The batched form (alisBatchBegin/End: every step of a wave of
+    requests as a few launches over all their worlds, recorded by several
+    host threads) gives every request the bytes it gets one request after
+    another."""
+    from alis_gb300 import build
+    build.build_engine()
+    exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                             os.path.join(ROOT, "tests", "drivers", "bin", "serve"), "engine", extra=["-lm"])
+    e = dict(os.environ, **env)
+    batched, s1 = _run(exe, ["batched", n, 2000, 7, mix, 8], e)
+    seq, s2 = _run(exe, ["sequential", n, 2000, 7, mix], e)
+    assert len(batched) == n and batched == seq
+    print("%s: batched %.2f Gcell/s, sequential %.2f Gcell/s" % (mix, s1["gcell_per_s"], s2["gcell_per_s"]))
