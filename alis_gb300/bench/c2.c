@@ -72,6 +72,19 @@ void c2_steps(int n)
 	}
 }
 
+/* the same steps recorded into batched launches (alisBatchBegin/End), the
+ * form that steps many worlds together, here with this world alone */
+void c2_steps_batched(int n)
+{
+	for (int q = 0; q < n; q++) {
+		alisBatchBegin();
+		updateE(W);
+		updateH(W);
+		updatePhaser(W, P);
+		alisBatchEnd();
+	}
+}
+
 /* result of the run so far: total outgoing flux over all frequencies
  * (brings the phaser accumulators to the host) */
 double c2_result(void)

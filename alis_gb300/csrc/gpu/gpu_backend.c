@@ -580,19 +580,44 @@ void alis_be_phaser_deleted(phaser P)
 
 /* phase factors of every frequency of the set, as the reference computes
  * them per call (src/phaser.c:97-98); frequencies before P are skipped */
+/* the phase factors last computed by this thread, with what they were
+ * computed from: worlds of a sweep share their frequencies and times */
+#define PHASE_MEMO 512
+static _Thread_local struct {
+	int nfreq, first;
+	float tE, tH;
+	float f[PHASE_MEMO];
+	float phE[2 * PHASE_MEMO], phH[2 * PHASE_MEMO];
+} phaseMemo;
+
 void updatePhaser(world W, phaser P)
 {
 	devPhaser *d = findPhaser(P);
 	if (!d) { fprintf(stderr, "alis: updatePhaser on an unknown phaser\n"); exit(1); }
 	int first = (int)(P - d->P);
-	for (int n = 0; n < d->nfreq; n++) {
-		float complex pE = 0, pH = 0;
-		if (n >= first) {
-			pE = cexpf(2 * PI * I * d->P[n].f * W->E->t);
-			pH = cexpf(2 * PI * I * d->P[n].f * W->H->t);
+	int same = d->nfreq <= PHASE_MEMO && phaseMemo.nfreq == d->nfreq && phaseMemo.first == first &&
+	           !memcmp(&phaseMemo.tE, &W->E->t, sizeof(float)) && !memcmp(&phaseMemo.tH, &W->H->t, sizeof(float));
+	for (int n = 0; same && n < d->nfreq; n++) same = !memcmp(&phaseMemo.f[n], &d->P[n].f, sizeof(float));
+	if (same) {
+		memcpy(d->phE, phaseMemo.phE, 2 * d->nfreq * sizeof(float));
+		memcpy(d->phH, phaseMemo.phH, 2 * d->nfreq * sizeof(float));
+	} else {
+		for (int n = 0; n < d->nfreq; n++) {
+			float complex pE = 0, pH = 0;
+			if (n >= first) {
+				pE = cexpf(2 * PI * I * d->P[n].f * W->E->t);
+				pH = cexpf(2 * PI * I * d->P[n].f * W->H->t);
+			}
+			d->phE[2*n] = crealf(pE), d->phE[2*n+1] = cimagf(pE);
+			d->phH[2*n] = crealf(pH), d->phH[2*n+1] = cimagf(pH);
 		}
-		d->phE[2*n] = crealf(pE), d->phE[2*n+1] = cimagf(pE);
-		d->phH[2*n] = crealf(pH), d->phH[2*n+1] = cimagf(pH);
+		if (d->nfreq <= PHASE_MEMO) {
+			phaseMemo.nfreq = d->nfreq, phaseMemo.first = first;
+			phaseMemo.tE = W->E->t, phaseMemo.tH = W->H->t;
+			for (int n = 0; n < d->nfreq; n++) phaseMemo.f[n] = d->P[n].f;
+			memcpy(phaseMemo.phE, d->phE, 2 * d->nfreq * sizeof(float));
+			memcpy(phaseMemo.phH, d->phH, 2 * d->nfreq * sizeof(float));
+		}
 	}
 	CHECK("phaser_record", alisgpu_phaser_record(d->dp, d->phE, d->phH));
 	d->hostStale = 1;

@@ -296,7 +296,7 @@ struct alisgpu_world {
 	// and m, of a one-block step, of the source patches and of the ghost
 	// copies; the values of an auxiliary step staged for the parent's
 	// batched launch; the batch group the world last joined
-	ParamSlot bP[2][2], bS[2], bSrc[2], bG[2];
+	ParamSlot bS[2], bSrc[2], bG[2];
 	long long ghostCells[2];                // cells of the ghost copies in bG
 	std::vector<float> stagedVals[2];
 	unsigned long long batchStamp;
@@ -424,6 +424,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 			if (w->psi[grid][m][f][q].p) alisgpu__freeAsync(w->psi[grid][m][f][q].p);
 	}
 	freeObjects(w);
+	for (int f = 0; f < 2; f++) alisgpu__slot_free(&w->bS[f]), alisgpu__slot_free(&w->bSrc[f]), alisgpu__slot_free(&w->bG[f]);
 	for (int f = 0; f < 2; f++) for (int a = 0; a < 3; a++) if (w->cls[f][a]) alisgpu__freeAsync(w->cls[f][a]);
 	if (w->evHCells) cudaEventDestroy(w->evHCells);
 	if (w->vbuf) alisgpu__freeAsync(w->vbuf);
@@ -1629,8 +1630,8 @@ static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const Fuse
 // the tiles of a batched entry: nbx x nby tiles of 32 x BATCH_TY cells
 // per i plane, planes in the half step's sweep order
 #define BATCH_TY 4
+#define BATCH_MINB 12                  // 42 registers: the tile loop's state fits beside halfStepBlock's
 struct BatchEntry {                    // the cells of one world (one m) in a batched launch
-	const HalfStepParams *P;           // its device slot
 	int nbx, nby, planes;
 	int itemStart;                     // its first tile in the launch
 };
@@ -1646,50 +1647,41 @@ struct BatchGhost {                    // the ghost copies of one world
 	const GhostLevels *G;
 	int start;                         // its first thread in the launch
 };
+// The launch parameters of a batched half step: the worlds' parameters
+// travel in the kernel's parameter space, as those of a one-world launch
+// do, so the cell code reads them through the constant cache; at most
+// BATCH_WORLDS entries per launch.
+#define BATCH_WORLDS 16
 struct BatchStep {
-	const BatchEntry *E;
 	int nE, nitems, per;               // entries, tiles, tiles per block
-	const BatchBlock *blk;
 	int nblk;                          // one-block steps: the first nblk blocks
+	const BatchBlock *blk;
 	const float *vals;
+	BatchEntry E[BATCH_WORLDS];
+	HalfStepParams P[BATCH_WORLDS];
 };
+static_assert(sizeof(BatchStep) <= 32000, "batched launch parameters exceed the parameter space");
 
-// One launch over every world of a group: the first blocks run the
+// One launch over the worlds of a group: the first blocks run the
 // one-block steps, the others take `per` consecutive tiles each of the
-// concatenated worlds, the world's parameters copied to shared memory
-// whenever a tile belongs to another entry than the block's last one.
-// Each tile runs halfStepBlock, the code of the one-world launch.
+// concatenated worlds.  Each tile runs halfStepBlock, the code of the
+// one-world launch, with the world's parameters from the launch's.
 template <int ALT>
-__global__ void __launch_bounds__(TX * BATCH_TY, STEP_MINB(BATCH_TY)) k_step_batch(const BatchStep B)
+__global__ void __launch_bounds__(TX * BATCH_TY, BATCH_MINB) k_step_batch(const __grid_constant__ BatchStep B)
 {
-	__shared__ HalfStepParams sP;
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	const int tid = threadIdx.y * blockDim.x + threadIdx.x, nth = blockDim.x * blockDim.y;
 	if ((int)blockIdx.x < B.nblk) {
 		const BatchBlock &b = B.blk[blockIdx.x];
-		smallStepBlock<ALT>(*b.S, tid, nth, b.voff >= 0 ? B.vals + b.voff : 0);
+		smallStepBlock<ALT>(*b.S, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, b.voff >= 0 ? B.vals + b.voff : 0);
 		return;
 	}
 	const int g0 = ((int)blockIdx.x - B.nblk) * B.per, g1 = min(g0 + B.per, B.nitems);
-	int cur = -1;
+	int e = 0;
 	for (int g = g0; g < g1; g++) {
-		int lo = 0, hi = B.nE - 1;
-		while (lo < hi) {
-			const int mid = (lo + hi + 1) >> 1;
-			if (B.E[mid].itemStart <= g) lo = mid; else hi = mid - 1;
-		}
-		const BatchEntry &e = B.E[lo];
-		if (lo != cur) {
-			__syncthreads();
-			const long long *src = reinterpret_cast<const long long *>(e.P);
-			long long *dst = reinterpret_cast<long long *>(&sP);
-			for (int q = tid; q < (int)(sizeof(HalfStepParams) / sizeof(long long)); q += nth) dst[q] = src[q];
-			__syncthreads();
-			cur = lo;
-		}
-		const int t = g - e.itemStart;
-		halfStepBlock<ALT, BATCH_TY>(sP, t % e.nbx, (t / e.nbx) % e.nby, t / (e.nbx * e.nby), tileList, &nlist);
+		while (e + 1 < B.nE && B.E[e + 1].itemStart <= g) e++;
+		const int t = g - B.E[e].itemStart, nbx = B.E[e].nbx, nby = B.E[e].nby;
+		halfStepBlock<ALT, BATCH_TY>(B.P[e], t % nbx, (t / nbx) % nby, t / (nbx * nby), tileList, &nlist);
 	}
 }
 
@@ -1718,9 +1710,12 @@ struct SlotUpdate {
 };
 struct Recorder {
 	bool on = false;
+	StreamGroup *group = nullptr;              // the thread's batch streams
+	cudaEvent_t evBegin = nullptr, evEnd = nullptr;
 	int kind = BATCH_NONE;
 	unsigned long long stamp = 1;
 	std::vector<BatchEntry> entries;
+	std::vector<HalfStepParams> params;        // the entries' parameters
 	std::vector<BatchBlock> blocks;
 	std::vector<BatchSource> sources;
 	std::vector<BatchGhost> ghosts;
@@ -1731,7 +1726,7 @@ struct Recorder {
 	void clear() {
 		kind = BATCH_NONE;
 		stamp++;
-		entries.clear(), blocks.clear(), sources.clear(), ghosts.clear();
+		entries.clear(), params.clear(), blocks.clear(), sources.clear(), ghosts.clear();
 		nitems = 0, ghostTotal = 0;
 		values.clear(), updates.clear(), updateList.clear();
 	}
@@ -1825,7 +1820,7 @@ extern "C" void alisgpu__slot_free(ParamSlot *s)
 }
 
 template <int ALT>
-static int launchStepBatch(const BatchStep &B0, cudaStream_t st)
+static int launchStepBatch(BatchStep &B, cudaStream_t st)
 {
 	static std::atomic<int> residentAt{0};
 	int resident = residentAt.load();
@@ -1837,7 +1832,6 @@ static int launchStepBatch(const BatchStep &B0, cudaStream_t st)
 		resident = std::max(1, sms * per);
 		residentAt.store(resident);
 	}
-	BatchStep B = B0;
 	B.per = std::max(1, (B.nitems + resident - 1) / resident);
 	const unsigned blocks = (unsigned)B.nblk + (unsigned)((B.nitems + B.per - 1) / B.per);
 	if (blocks) k_step_batch<ALT><<<blocks, dim3(TX, BATCH_TY), 0, st>>>(B);
@@ -1851,7 +1845,7 @@ static int launchHalfGroup(int field)
 {
 	Recorder &R = gRec;
 	auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
-	const size_t oE = 0, oB = oE + al(R.entries.size() * sizeof(BatchEntry));
+	const size_t oB = 0;
 	const size_t oS = oB + al(R.blocks.size() * sizeof(BatchBlock));
 	const size_t oG = oS + al(R.sources.size() * sizeof(BatchSource));
 	const size_t oV = oG + al(R.ghosts.size() * sizeof(BatchGhost));
@@ -1863,7 +1857,6 @@ static int launchHalfGroup(int field)
 	if (rc) return rc;
 	unsigned char *h = (unsigned char *)hv;
 	const unsigned char *d = (const unsigned char *)dv;
-	if (!R.entries.empty()) memcpy(h + oE, R.entries.data(), R.entries.size() * sizeof(BatchEntry));
 	if (!R.blocks.empty()) memcpy(h + oB, R.blocks.data(), R.blocks.size() * sizeof(BatchBlock));
 	if (!R.sources.empty()) memcpy(h + oS, R.sources.data(), R.sources.size() * sizeof(BatchSource));
 	if (!R.ghosts.empty()) memcpy(h + oG, R.ghosts.data(), R.ghosts.size() * sizeof(BatchGhost));
@@ -1874,10 +1867,11 @@ static int launchHalfGroup(int field)
 		ALIS_CUDA(cudaMemcpyAsync(u.dst, d + oU + u.off, u.bytes, cudaMemcpyDeviceToDevice, gStream));
 	const float *vals = (const float *)(d + oV);
 	if (!R.entries.empty() || !R.blocks.empty()) {
-		BatchStep B;
-		B.E = (const BatchEntry *)(d + oE), B.nE = (int)R.entries.size(), B.nitems = R.nitems, B.per = 1;
+		static thread_local BatchStep B;
+		B.nE = (int)R.entries.size(), B.nitems = R.nitems, B.per = 1;
 		B.blk = (const BatchBlock *)(d + oB), B.nblk = (int)R.blocks.size();
 		B.vals = vals;
+		for (int q = 0; q < B.nE; q++) B.E[q] = R.entries[q], B.P[q] = R.params[q];
 		int slot = alisgpu__prof_start();
 		rc = field == 0 ? launchStepBatch<1>(B, gStream) : launchStepBatch<-1>(B, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
@@ -1904,24 +1898,40 @@ static int launchHalfGroup(int field)
 }
 
 // launch the open group, whatever its kind
+// launch the open group, whatever its kind, on the thread's batch streams
 static int batchLaunch(void)
 {
 	Recorder &R = gRec;
+	StreamGroup *prev = gGroup;
+	gGroup = R.group;
 	int rc = ALISGPU_OK;
 	const bool updates = !R.updateList.empty();
 	if (R.kind == BATCH_E || R.kind == BATCH_H) rc = launchHalfGroup(R.kind == BATCH_E ? 0 : 1);
 	else if (R.kind == BATCH_PHASER) rc = alisgpu__phaser_batch_launch();
 	else if (updates) rc = launchHalfGroup(0);
 	R.clear();
+	gGroup = prev;
 	return rc;
 }
 
+// the shared streams wait for everything the batch streams were given
+static int batchJoinShared(void)
+{
+	Recorder &R = gRec;
+	ALIS_CUDA(cudaEventRecord(R.evEnd, R.group->main));
+	ALIS_CUDA(cudaStreamWaitEvent(gDefaultGroup.main, R.evEnd, 0));
+	return ALISGPU_OK;
+}
+
+// A recorded call runs the rest of its work (uploads of changed tables,
+// launches of a group it closes) on the thread's batch streams.
 extern "C" int alisgpu__batch_enter(int kind, const void *world)
 {
 	Recorder &R = gRec;
 	if (!R.on) return 0;
 	const alisgpu_world *w = (const alisgpu_world *)world;
 	if (w && w->group) return 0;                      // worlds on streams of their own step as usual
+	gGroup = R.group;
 	if (kind == BATCH_NONE) return 1;
 	if (R.kind != kind || (w && w->batchStamp == R.stamp)) {
 		if (batchLaunch()) return -1;
@@ -1931,32 +1941,50 @@ extern "C" int alisgpu__batch_enter(int kind, const void *world)
 	return 1;
 }
 
+// Each recording thread has streams of its own, so that the groups of
+// several threads overlap on the device; its batch starts after the work
+// given to the shared streams so far, and that work's later calls start
+// after the batch.
 extern "C" int alisgpu_batch_begin(void)
 {
 	int rc = alisgpu_init();
 	if (rc) return rc;
-	if (gRec.on) return alisgpu__fail(ALISGPU_EINVAL, "batch_begin: a batch is open already");
+	Recorder &R = gRec;
+	if (R.on) return alisgpu__fail(ALISGPU_EINVAL, "batch_begin: a batch is open already");
+	if (!R.group) {
+		StreamGroup *g = new StreamGroup();
+		if ((rc = groupCreate(g))) { delete g; return rc; }
+		ALIS_CUDA(cudaEventCreateWithFlags(&R.evBegin, cudaEventDisableTiming));
+		ALIS_CUDA(cudaEventCreateWithFlags(&R.evEnd, cudaEventDisableTiming));
+		R.group = g;
+	}
 	bindWorld(0);
-	fullJoin();
-	gRec.clear();
-	gRec.on = true;
+	ALIS_CUDA(cudaEventRecord(R.evBegin, gDefaultGroup.main));
+	ALIS_CUDA(cudaStreamWaitEvent(R.group->main, R.evBegin, 0));
+	R.clear();
+	R.on = true;
 	return ALISGPU_OK;
 }
 
 extern "C" int alisgpu_batch_end(void)
 {
-	if (!gRec.on) return ALISGPU_OK;
-	bindWorld(0);
-	const int rc = batchLaunch();
-	gRec.on = false;
+	Recorder &R = gRec;
+	if (!R.on) return ALISGPU_OK;
+	int rc = batchLaunch();
+	R.on = false;
 	if (rc) alisgpu__phaser_batch_clear();
-	return rc;
+	const int rj = batchJoinShared();
+	bindWorld(0);
+	return rc ? rc : rj;
 }
 
 extern "C" int alisgpu__batch_flush(void)
 {
-	if (!gRec.on || gRec.kind == BATCH_NONE) return ALISGPU_OK;
-	return batchLaunch();
+	Recorder &R = gRec;
+	if (!R.on || R.kind == BATCH_NONE) return ALISGPU_OK;
+	int rc = batchLaunch();
+	if (rc) return rc;
+	return batchJoinShared();
 }
 
 // ---------------------------------------------------------------------
@@ -2323,6 +2351,14 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 {
 	const alisgpu_geometry &g = w->g;
 	const int field = s->field;
+	if ((int)gRec.entries.size() + 1 + g.complexField > BATCH_WORLDS) {
+		// the group is full: launch it and go on with a new one of the same kind
+		const int kind = gRec.kind;
+		int rc = batchLaunch();
+		if (rc) return rc;
+		gRec.kind = kind;
+		w->batchStamp = gRec.stamp;
+	}
 	for (int m = 0; m <= g.complexField; m++) {
 		P.m = m;
 		for (int c = 0; c < 3; c++) {
@@ -2335,11 +2371,9 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 		P.matTab = field == 0 ? w->matTab : 0;
 		P.matWide = w->matWide;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
-		const void *dP = 0;
-		int rc = alisgpu__slot_sync(&w->bP[field][m], &P, sizeof P, &dP);
-		if (rc) return rc;
 		const int nbx = (g.kMAX - g.kMIN + TX) / TX, nby = (g.jMAX - g.jMIN + BATCH_TY) / BATCH_TY, planes = g.iMAX - g.iMIN + 1;
-		gRec.entries.push_back(BatchEntry{ (const HalfStepParams *)dP, nbx, nby, planes, gRec.nitems });
+		gRec.entries.push_back(BatchEntry{ nbx, nby, planes, gRec.nitems });
+		gRec.params.push_back(P);
 		const long long items = (long long)gRec.nitems + (long long)nbx * nby * planes;
 		if (items >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: too many items");
 		gRec.nitems = (int)items;
@@ -2408,6 +2442,14 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	for (int q = 0; q < s->ntfsf; q++) P.tf[q] = tfsfFor(w, s->tfsf[q], field);
 	P.err = gErrWord;
 
+	// a batch records the call (its uploads then go to the batch streams):
+	// an auxiliary column's step is staged for its parent's entry, any
+	// other step joins the group of its field
+	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
+	const bool smallPath = cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC &&
+	                       s->nghost <= ALIS_SMALL_GHOSTS;
+	const int rec = alisgpu__batch_enter(smallPath && s->concurrent && s->attach ? BATCH_NONE : (field == 0 ? BATCH_E : BATCH_H), w);
+	if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
 	// per-axis classification: CPML slabs, TFSF planes, object ranges
 	// (made again only when one of them changed)
 	static thread_local std::vector<int> key;
@@ -2463,8 +2505,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	// the other field, whose fields its TFSF corrections read
 	const bool side = s->concurrent && !gProfOn;
 	if (!side && gAuxRec[1 - field]) ALIS_CUDA(cudaStreamWaitEvent(gStream, gEvAuxDone[1 - field], 0));
-	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
-	if (cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC && s->nghost <= ALIS_SMALL_GHOSTS) {
+	if (smallPath) {
 		static thread_local SmallStepParams S;
 		S.nm = 1 + g.complexField;
 		for (int m = 0; m < S.nm; m++) {
@@ -2487,8 +2528,6 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		if (s->nsrc) memcpy(S.src, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		if (s->nghost) memcpy(S.ghost, s->ghost, s->nghost * sizeof(alisgpu_ghost_copy));
 		// recorded by a batch: staged for the parent's entry, or an entry of its own
-		const int rec = alisgpu__batch_enter(s->concurrent ? BATCH_NONE : (field == 0 ? BATCH_E : BATCH_H), w);
-		if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
 		if (rec) {
 			S.vdev = 0;
 			memset(S.v, 0, sizeof S.v);
@@ -2567,11 +2606,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		}
 		return ALISGPU_OK;
 	}
-	{
-		const int rec = alisgpu__batch_enter(field == 0 ? BATCH_E : BATCH_H, w);
-		if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
-		if (rec) return recordHalfStep(w, s, P);
-	}
+	if (rec) return recordHalfStep(w, s, P);
 	const int ni = g.iMAX - g.iMIN + 1;
 	bool timed = false, fused = false;
 	const int v = tunedShape(w, field, &timed);

@@ -25,6 +25,12 @@ roofline  the fused half-step kernel: algorithmic bytes per step (84 B per
 cpu_baseline  the oracle restatement of the reference loops on the host
           cores (OpenMP), bounded sample of the same world
 --impl reference  times that CPU implementation alone as the reference arm.
+--sweep   the batched metasurface unit-cell sweep instead: N periodic unit
+          cells (32-96 x 32-96 x 64-256 cells, Lorentz pillar, TFSF pulse,
+          32-wavelength transmission plane, 3000 steps each) stepped
+          together by batched launches, against the same cells one after
+          another; both throughputs, the ratio, and whether every cell's
+          result is byte-identical both ways (alis_gb300/bench/serve.c).
 
 Multi-GPU: replicas only (each rank runs its own world on its own GPU);
 value is the sum of all ranks' cell updates over the slowest rank's time.
@@ -44,6 +50,7 @@ sys.path.insert(0, ROOT)
 
 HALF = 230          # domain half size in nm: 256^3 cells with the CPML
 NFREQ = 64
+TUNE_STEPS = 16     # the engine times its launch shapes over a world's first 10 half steps of each field
 def workload(cells):
     n = round(cells ** (1 / 3))
     return "dispersive scatterer %d^3 (gold Drude+2CP, TFSF, CPML 12, 64-f box phasers)" % n
@@ -240,6 +247,8 @@ def engine_arm(args, rank, world, local):
     cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
 
     cells = lib.c2_build(args.half, NFREQ)
+    # the one-world calls, or the batched form (--batched) of the same steps
+    steps_fn = lib.c2_steps_batched if args.batched else lib.c2_steps
     stream = ctypes.c_void_p(eng.alisgpu_stream())
     K, W = args.steps, args.warmup
     ring = int(os.environ.get("ALISGPU_PHASER_RING", "64"))
@@ -248,7 +257,9 @@ def engine_arm(args, rank, world, local):
     for e in ev:
         cudart.cudaEventCreate(ctypes.byref(e))
 
-    lib.c2_steps(W)
+    # the warm-up covers the launch-shape tuner's first half steps
+    W = max(W, TUNE_STEPS)
+    steps_fn(W)
     eng.alisgpu_synchronize()
     with Clocks(local) as clk:
         # kernel-only throughput: device time of R back-to-back windows of
@@ -258,7 +269,7 @@ def engine_arm(args, rank, world, local):
         l0 = eng.alisgpu_launch_count()
         cudart.cudaEventRecord(ev[0], stream)
         for r in range(R):
-            lib.c2_steps(K)
+            steps_fn(K)
             cudart.cudaEventRecord(ev[r + 1], stream)
         cudart.cudaEventSynchronize(ev[R])
         launches = eng.alisgpu_launch_count() - l0
@@ -274,13 +285,13 @@ def engine_arm(args, rank, world, local):
         eng.alisgpu_synchronize()
         t0 = time.perf_counter()
         for r in range(R):
-            lib.c2_steps(K)
+            steps_fn(K)
             flux = lib.c2_result()
         e2e_s = reduce_max(time.perf_counter() - t0, world)
         # per-kernel device times for the roofline and the shares, over a
         # whole number of ring periods
         eng.alisgpu_profile(1)
-        lib.c2_steps(windows(K, ring, 1) * K)
+        steps_fn(windows(K, ring, 1) * K)
         kinds = {}
         for kind, name in enumerate(["step_E", "step_H", "ghost", "source", "gather", "flush", "farfield", "step_aux"]):
             t, n = ctypes.c_double(), ctypes.c_ulonglong()
@@ -317,6 +328,7 @@ def engine_arm(args, rank, world, local):
                    "phaser": "64 frequencies, %s, time-blocked ring of %s steps" % (
                        "Kahan-compensated" if os.environ.get("ALISGPU_PHASER_KAHAN") == "1" else "plain float sums",
                        os.environ.get("ALISGPU_PHASER_RING", "64")),
+                   "path": "batched launches (alisBatchBegin/End)" if args.batched else "one launch per half step",
                    "timing": "%d back-to-back windows of %d steps (%d steps, a whole number of %d-step phaser "
                              "ring periods, so the DFT flush is charged at its own rate); value from their total "
                              "device time" % (R, K, R * K, ring),
@@ -339,6 +351,43 @@ def engine_arm(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+def sweep_arm(args):
+    """The batched unit-cell sweep against the per-instance path."""
+    from alis_gb300 import build
+    build.build_engine()
+    exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                             os.path.join(ROOT, "alis_gb300", "lib", "serve"), "engine", extra=["-lm"])
+    env = dict(os.environ)
+    if args.sweep_steps:
+        env["SERVE_STEPS"] = str(args.sweep_steps)
+    env.setdefault("SERVE_THREADS", "16")
+
+    def run(mode, extra):
+        r = subprocess.run([exe, mode, str(args.sweep), "2000", "7", "sweep"] + extra, capture_output=True,
+                           text=True, env=env, timeout=3600)
+        if r.returncode:
+            raise RuntimeError("sweep %s failed: %s" % (mode, r.stderr[-2000:]))
+        res = {l.split()[1]: l.split()[6] for l in r.stdout.splitlines() if l.startswith("R ")}
+        return res, json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+
+    batched, b = run("batched", [str(args.sweep), "200"])
+    seq, q = run("sequential", [])
+    line = {
+        "metric": "sweep Gcell-updates/s", "value": b["gcell_per_s"], "unit": "Gcell/s", "n_gpus": 1,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "metasurface unit-cell sweep: %d periodic cells 32-96 x 32-96 x 64-256, TiO2-like "
+                               "Lorentz pillar, TFSF pulse, 32-wavelength transmission plane, %s steps each" %
+                               (args.sweep, env.get("SERVE_STEPS", "3000")),
+                   "batched": "alisBatchBegin/End, %s host threads recording" % env["SERVE_THREADS"],
+                   "per_instance": "the same cells one after another through the same API"},
+        "per_instance": {"value": q["gcell_per_s"], "unit": "Gcell/s", "wall_s": q["wall_s"]},
+        "ratio": b["gcell_per_s"] / q["gcell_per_s"],
+        "wall_s": b["wall_s"], "host_s": b["host_s"],
+        "identical_results": batched == seq and len(batched) == args.sweep,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -349,7 +398,15 @@ def main():
     ap.add_argument("--half", type=int, default=HALF, help="domain half size in nm (230: the 256^3 workload)")
     ap.add_argument("--timed-steps", type=int, default=3000,
                     help="least number of steps over all timed windows (about 1 s on the 256^3 workload)")
+    ap.add_argument("--batched", action="store_true",
+                    help="step the world through the batched launches (alisBatchBegin/End) instead")
+    ap.add_argument("--sweep", type=int, default=0, metavar="N",
+                    help="run the batched unit-cell sweep of N cells instead (512: the full sweep)")
+    ap.add_argument("--sweep-steps", type=int, default=0, help="steps per unit cell (default 3000)")
     args = ap.parse_args()
+    if args.sweep:
+        sweep_arm(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = env_rank()
