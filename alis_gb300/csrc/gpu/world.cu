@@ -1630,10 +1630,28 @@ static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const Fuse
 // the tiles of a batched entry: nbx x nby tiles of 32 x BATCH_TY cells
 // per i plane, planes in the half step's sweep order
 #define BATCH_TY 4
-#define BATCH_MINB 12                  // 42 registers: the tile loop's state fits beside halfStepBlock's
+// n / d for 0 <= n < 2^31 as (n m) >> sh, with m = ceil(2^sh / d) and
+// sh = 31 + ceil(log2 d): the product's error stays below 1/d for every
+// such n (checked exhaustively over the divisors a launch uses)
+struct FastDiv {
+	unsigned m;
+	int sh;
+	__device__ __forceinline__ int div(int n) const { return (int)(((unsigned long long)(unsigned)n * m) >> sh); }
+};
+static FastDiv fastDiv(int d)
+{
+	int s = 0;
+	while ((1LL << s) < d) s++;
+	FastDiv f;
+	f.sh = 31 + s;
+	f.m = (unsigned)(((1ULL << f.sh) + (unsigned long long)d - 1) / (unsigned long long)d);
+	return f;
+}
+
 struct BatchEntry {                    // the cells of one world (one m) in a batched launch
 	int nbx, nby, planes;
 	int itemStart;                     // its first tile in the launch
+	FastDiv byRow, byPlane;            // division by nbx and by nbx nby
 };
 struct BatchBlock {                    // a half step run by one block (auxiliary column, tiny world)
 	const SmallStepParams *S;          // its device slot
@@ -1649,40 +1667,48 @@ struct BatchGhost {                    // the ghost copies of one world
 };
 // The launch parameters of a batched half step: the worlds' parameters
 // travel in the kernel's parameter space, as those of a one-world launch
-// do, so the cell code reads them through the constant cache; at most
-// BATCH_WORLDS entries per launch.
+// do, so the cell code reads them through the constant cache.  Launches
+// come in capacities of 1, 4, 8 and 16 entries, so that a launch carries
+// about as many parameter bytes as it has worlds.
 #define BATCH_WORLDS 16
-struct BatchStep {
-	int nE, nitems, per;               // entries, tiles, tiles per block
+struct BatchHead {
+	int nE, nitems;                    // entries, tiles
 	int nblk;                          // one-block steps: the first nblk blocks
 	const BatchBlock *blk;
 	const float *vals;
-	BatchEntry E[BATCH_WORLDS];
-	HalfStepParams P[BATCH_WORLDS];
 };
-static_assert(sizeof(BatchStep) <= 32000, "batched launch parameters exceed the parameter space");
+template <int CAP>
+struct BatchStep {
+	BatchHead h;
+	BatchEntry E[CAP];
+	HalfStepParams P[CAP];
+};
+static_assert(sizeof(BatchStep<BATCH_WORLDS>) <= 32000, "batched launch parameters exceed the parameter space");
 
 // One launch over the worlds of a group: the first blocks run the
-// one-block steps, the others take `per` consecutive tiles each of the
-// concatenated worlds.  Each tile runs halfStepBlock, the code of the
-// one-world launch, with the world's parameters from the launch's.
-template <int ALT>
-__global__ void __launch_bounds__(TX * BATCH_TY, BATCH_MINB) k_step_batch(const __grid_constant__ BatchStep B)
+// one-block steps, each further block one tile of the concatenated
+// worlds, in the order of a one-world launch (k tiles, then rows, then
+// planes in the sweep direction), so the blocks resident at any time work
+// on neighbouring tiles and planes.  A block finds its world from its
+// index alone, and runs halfStepBlock, the code of the one-world launch,
+// with the world's parameters from the launch's.
+template <int ALT, int CAP>
+__global__ void __launch_bounds__(TX * BATCH_TY, STEP_MINB(BATCH_TY)) k_step_batch(const __grid_constant__ BatchStep<CAP> B)
 {
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	if ((int)blockIdx.x < B.nblk) {
-		const BatchBlock &b = B.blk[blockIdx.x];
-		smallStepBlock<ALT>(*b.S, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, b.voff >= 0 ? B.vals + b.voff : 0);
+	if ((int)blockIdx.x < B.h.nblk) {
+		const BatchBlock &b = B.h.blk[blockIdx.x];
+		smallStepBlock<ALT>(*b.S, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, b.voff >= 0 ? B.h.vals + b.voff : 0);
 		return;
 	}
-	const int g0 = ((int)blockIdx.x - B.nblk) * B.per, g1 = min(g0 + B.per, B.nitems);
+	const int g = (int)blockIdx.x - B.h.nblk;
 	int e = 0;
-	for (int g = g0; g < g1; g++) {
-		while (e + 1 < B.nE && B.E[e + 1].itemStart <= g) e++;
-		const int t = g - B.E[e].itemStart, nbx = B.E[e].nbx, nby = B.E[e].nby;
-		halfStepBlock<ALT, BATCH_TY>(B.P[e], t % nbx, (t / nbx) % nby, t / (nbx * nby), tileList, &nlist);
-	}
+#pragma unroll
+	for (int q = 1; q < CAP; q++) if (q < B.h.nE && B.E[q].itemStart <= g) e = q;
+	const BatchEntry &E = B.E[e];
+	const int t = g - E.itemStart, plane = E.byPlane.div(t), r = t - plane * E.nbx * E.nby, by = E.byRow.div(r);
+	halfStepBlock<ALT, BATCH_TY>(B.P[e], r - by * E.nbx, by, plane, tileList, &nlist);
 }
 
 __global__ void k_sources_batch(const BatchSource *T, const float *vals)
@@ -1819,23 +1845,24 @@ extern "C" void alisgpu__slot_free(ParamSlot *s)
 	s->host.clear();
 }
 
-template <int ALT>
-static int launchStepBatch(BatchStep &B, cudaStream_t st)
+template <int ALT, int CAP>
+static int launchStepBatch(const BatchHead &h, const std::vector<BatchEntry> &E, const std::vector<HalfStepParams> &P, cudaStream_t st)
 {
-	static std::atomic<int> residentAt{0};
-	int resident = residentAt.load();
-	if (!resident) {
-		int dev = 0, sms = 0, per = 0;
-		ALIS_CUDA(cudaGetDevice(&dev));
-		ALIS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		ALIS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_step_batch<ALT>, TX * BATCH_TY, 0));
-		resident = std::max(1, sms * per);
-		residentAt.store(resident);
-	}
-	B.per = std::max(1, (B.nitems + resident - 1) / resident);
-	const unsigned blocks = (unsigned)B.nblk + (unsigned)((B.nitems + B.per - 1) / B.per);
-	if (blocks) k_step_batch<ALT><<<blocks, dim3(TX, BATCH_TY), 0, st>>>(B);
+	static thread_local BatchStep<CAP> B;
+	B.h = h;
+	for (int q = 0; q < h.nE; q++) B.E[q] = E[q], B.P[q] = P[q];
+	const unsigned blocks = (unsigned)h.nblk + (unsigned)h.nitems;
+	if (blocks) k_step_batch<ALT, CAP><<<blocks, dim3(TX, BATCH_TY), 0, st>>>(B);
 	return ALISGPU_OK;
+}
+
+template <int ALT>
+static int launchStepBatch(const BatchHead &h, const std::vector<BatchEntry> &E, const std::vector<HalfStepParams> &P, cudaStream_t st)
+{
+	if (h.nE <= 1) return launchStepBatch<ALT, 1>(h, E, P, st);
+	if (h.nE <= 4) return launchStepBatch<ALT, 4>(h, E, P, st);
+	if (h.nE <= 8) return launchStepBatch<ALT, 8>(h, E, P, st);
+	return launchStepBatch<ALT, BATCH_WORLDS>(h, E, P, st);
 }
 
 // launch the open half-step group: its tables and the changed slots go up
@@ -1867,13 +1894,12 @@ static int launchHalfGroup(int field)
 		ALIS_CUDA(cudaMemcpyAsync(u.dst, d + oU + u.off, u.bytes, cudaMemcpyDeviceToDevice, gStream));
 	const float *vals = (const float *)(d + oV);
 	if (!R.entries.empty() || !R.blocks.empty()) {
-		static thread_local BatchStep B;
-		B.nE = (int)R.entries.size(), B.nitems = R.nitems, B.per = 1;
-		B.blk = (const BatchBlock *)(d + oB), B.nblk = (int)R.blocks.size();
-		B.vals = vals;
-		for (int q = 0; q < B.nE; q++) B.E[q] = R.entries[q], B.P[q] = R.params[q];
+		BatchHead h;
+		h.nE = (int)R.entries.size(), h.nitems = R.nitems;
+		h.blk = (const BatchBlock *)(d + oB), h.nblk = (int)R.blocks.size();
+		h.vals = vals;
 		int slot = alisgpu__prof_start();
-		rc = field == 0 ? launchStepBatch<1>(B, gStream) : launchStepBatch<-1>(B, gStream);
+		rc = field == 0 ? launchStepBatch<1>(h, R.entries, R.params, gStream) : launchStepBatch<-1>(h, R.entries, R.params, gStream);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 		if (rc) return rc;
@@ -2372,7 +2398,7 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 		P.matWide = w->matWide;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
 		const int nbx = (g.kMAX - g.kMIN + TX) / TX, nby = (g.jMAX - g.jMIN + BATCH_TY) / BATCH_TY, planes = g.iMAX - g.iMIN + 1;
-		gRec.entries.push_back(BatchEntry{ nbx, nby, planes, gRec.nitems });
+		gRec.entries.push_back(BatchEntry{ nbx, nby, planes, gRec.nitems, fastDiv(nbx), fastDiv(nbx * nby) });
 		gRec.params.push_back(P);
 		const long long items = (long long)gRec.nitems + (long long)nbx * nby * planes;
 		if (items >= (1ll << 31)) return alisgpu__fail(ALISGPU_ERANGE, "batch: too many items");

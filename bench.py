@@ -25,6 +25,8 @@ roofline  the fused half-step kernel: algorithmic bytes per step (84 B per
 cpu_baseline  the oracle restatement of the reference loops on the host
           cores (OpenMP), bounded sample of the same world
 --impl reference  times that CPU implementation alone as the reference arm.
+forms     the batched unit-cell sweep (64 cells) and the served request
+          stream, each against its per-request path (--forms 0 skips)
 --sweep   the batched metasurface unit-cell sweep instead: N periodic unit
           cells (32-96 x 32-96 x 64-256 cells, Lorentz pillar, TFSF pulse,
           32-wavelength transmission plane, 3000 steps each) stepped
@@ -348,43 +350,70 @@ def engine_arm(args, rank, world, local):
         "clocks": clocks,
         "result_flux": flux,
     }
+    if args.forms:
+        # the batched and served forms, each against its per-request path
+        line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form()}
     print(json.dumps(line), flush=True)
 
 
-def sweep_arm(args):
-    """The batched unit-cell sweep against the per-instance path."""
+def serve_exe():
     from alis_gb300 import build
     build.build_engine()
-    exe = build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
-                             os.path.join(ROOT, "alis_gb300", "lib", "serve"), "engine", extra=["-lm"])
+    return build.link_program(os.path.join(ROOT, "alis_gb300", "bench", "serve.c"),
+                              os.path.join(ROOT, "alis_gb300", "lib", "serve"), "engine", extra=["-lm"])
+
+
+def run_serve(exe, args, env):
+    """One run of the request loop: per-request results and its summary."""
+    r = subprocess.run([exe] + [str(a) for a in args], capture_output=True, text=True, env=env, timeout=3600)
+    if r.returncode:
+        raise RuntimeError("serve %s failed: %s" % (args[0], r.stderr[-2000:]))
+    res = {l.split()[1]: l.split()[6] for l in r.stdout.splitlines() if l.startswith("R ")}
+    return res, json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+
+
+def sweep_form(n, steps=0, threads=8):
+    """The batched metasurface sweep of n unit cells against the same cells
+    one after another, and whether every cell's result is the same bytes."""
+    exe = serve_exe()
+    env = dict(os.environ, SERVE_THREADS=str(threads))
+    if steps:
+        env["SERVE_STEPS"] = str(steps)
+    batched, b = run_serve(exe, ["batched", n, 2000, 7, "sweep", n, 200], env)
+    seq, q = run_serve(exe, ["sequential", n, 2000, 7, "sweep"], env)
+    return {"workload": "metasurface unit-cell sweep: %d periodic cells 32-96 x 32-96 x 64-256, TiO2-like Lorentz "
+                        "pillar, TFSF pulse, 32-wavelength transmission plane, %d steps each" % (n, steps or 3000),
+            "batched": {"value": b["gcell_per_s"], "unit": "Gcell/s", "wall_s": b["wall_s"],
+                        "how": "alisBatchBegin/End, %d host threads recording" % threads},
+            "per_instance": {"value": q["gcell_per_s"], "unit": "Gcell/s", "wall_s": q["wall_s"],
+                             "how": "the same cells one after another through the same API"},
+            "ratio": b["gcell_per_s"] / q["gcell_per_s"],
+            "identical_results": batched == seq and len(batched) == n}
+
+
+def served_form(n=48):
+    """The served request stream in miniature: Poisson arrivals of mixed
+    small requests, admitted by footprint, against the same requests one
+    after another; latency percentiles of the served run."""
+    exe = serve_exe()
     env = dict(os.environ)
-    if args.sweep_steps:
-        env["SERVE_STEPS"] = str(args.sweep_steps)
-    env.setdefault("SERVE_THREADS", "16")
+    served, s = run_serve(exe, ["served", n, 200, 42, "small", 16], env)
+    seq, q = run_serve(exe, ["sequential", n, 200, 42, "small"], env)
+    return {"workload": "%d mixed small requests (vacuum and dielectric, Drude bowtie, photonic-crystal k-point "
+                        "runs; 28^3-48^3 cells, 120-240 steps), Poisson arrivals offered at 200/s" % n,
+            "served": {"value": s["gcell_per_s"], "unit": "Gcell/s", "latency_ms": s["latency_ms"],
+                       "slots": 16, "host_threads": s["threads"]},
+            "sequential": {"value": q["gcell_per_s"], "unit": "Gcell/s"},
+            "ratio": s["gcell_per_s"] / q["gcell_per_s"],
+            "identical_results": served == seq and len(served) == n}
 
-    def run(mode, extra):
-        r = subprocess.run([exe, mode, str(args.sweep), "2000", "7", "sweep"] + extra, capture_output=True,
-                           text=True, env=env, timeout=3600)
-        if r.returncode:
-            raise RuntimeError("sweep %s failed: %s" % (mode, r.stderr[-2000:]))
-        res = {l.split()[1]: l.split()[6] for l in r.stdout.splitlines() if l.startswith("R ")}
-        return res, json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
 
-    batched, b = run("batched", [str(args.sweep), "200"])
-    seq, q = run("sequential", [])
-    line = {
-        "metric": "sweep Gcell-updates/s", "value": b["gcell_per_s"], "unit": "Gcell/s", "n_gpus": 1,
-        "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "metasurface unit-cell sweep: %d periodic cells 32-96 x 32-96 x 64-256, TiO2-like "
-                               "Lorentz pillar, TFSF pulse, 32-wavelength transmission plane, %s steps each" %
-                               (args.sweep, env.get("SERVE_STEPS", "3000")),
-                   "batched": "alisBatchBegin/End, %s host threads recording" % env["SERVE_THREADS"],
-                   "per_instance": "the same cells one after another through the same API"},
-        "per_instance": {"value": q["gcell_per_s"], "unit": "Gcell/s", "wall_s": q["wall_s"]},
-        "ratio": b["gcell_per_s"] / q["gcell_per_s"],
-        "wall_s": b["wall_s"], "host_s": b["host_s"],
-        "identical_results": batched == seq and len(batched) == args.sweep,
-    }
+def sweep_arm(args):
+    """The batched unit-cell sweep against the per-instance path, one line."""
+    f = sweep_form(args.sweep, args.sweep_steps)
+    line = {"metric": "sweep Gcell-updates/s", "value": f["batched"]["value"], "unit": "Gcell/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic", "config": {"workload": f["workload"]},
+            "per_instance": f["per_instance"], "ratio": f["ratio"], "identical_results": f["identical_results"]}
     print(json.dumps(line), flush=True)
 
 
@@ -403,6 +432,9 @@ def main():
     ap.add_argument("--sweep", type=int, default=0, metavar="N",
                     help="run the batched unit-cell sweep of N cells instead (512: the full sweep)")
     ap.add_argument("--sweep-steps", type=int, default=0, help="steps per unit cell (default 3000)")
+    ap.add_argument("--forms", type=int, default=64, metavar="N",
+                    help="after the main line's timing, the batched sweep of N unit cells and the served stream, "
+                         "each against its per-request path, as the line's 'forms' (0: skip)")
     args = ap.parse_args()
     if args.sweep:
         sweep_arm(args)
