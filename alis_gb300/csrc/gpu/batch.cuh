@@ -4,9 +4,9 @@
 // phaser samples of the worlds a host thread steps are recorded instead
 // of launched.  Consecutive records of one kind (E half steps, H half
 // steps, phaser samples) of distinct worlds form a group, and a group
-// runs as a few launches over all its worlds: one march over every
-// world's cells (with the TFSF auxiliary columns and tiny worlds as
-// one-block entries), then every world's source patches, then every
+// runs as a few launches over all its worlds: one launch with a block per
+// tile of every world's cells (the TFSF auxiliary columns and tiny worlds
+// as one-block entries), then every world's source patches, then every
 // world's ghost copies; or every phaser's ring flush, then every
 // phaser's face gather.  A record of another kind, or a second record of
 // a world already in the group, launches the group first, so the order
