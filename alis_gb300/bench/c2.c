@@ -118,6 +118,13 @@ double c2_step_bytes(void)
 	return bytes;
 }
 
+/* the same with E and H stored as half values (ALIS_FIELD_STORAGE=half):
+ * 36 of the 72 field bytes per cell */
+double c2_step_bytes_half(void)
+{
+	return c2_step_bytes() - 36.0 * W->iNUM * W->jNUM * W->kNUM;
+}
+
 /* host bytes moved per step by the public-API path: source increments
  * and phase factors up, nothing down until c2_result */
 double c2_step_h2d_bytes(void)

@@ -9,6 +9,7 @@
 // compact box arrays with their own strides.
 #pragma once
 #include <cuda_runtime.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 #include "alisgpu.h"
 
@@ -65,6 +66,60 @@ struct DevTfsf {
 	float dtdMin[3], dtdMax[3];           // dt/ds at the min face and max face
 };
 
+// FP16 field storage of a world (alisgpu_world_set_storage): each E and H
+// component holds IEEE half values times 2^e, one exponent per component
+// and plane of the layout.  Per field and step parity the world keeps the
+// exponents readers use (ex; ghost copies that move whole planes point a
+// plane at another's), the exponents the step computed (exK) and 2^ex as
+// floats (sc), all indexed [comp * L.ni + (i - L.i0)]; the inverse scales
+// 2^-e of the field's next step (inv); the step's largest magnitudes,
+// spread over HALF_SLOTS words per (component, plane) so that the plane's
+// warps update different ones, at [(comp * L.ni + plane) * HALF_SLOTS +
+// slot]; and the table a half step of the field reads its scales from,
+// HALF_TAB floats per plane: the other field's scales at the plane and at
+// the plane + ALT, its own scales as stored, its inverse scales.  After
+// each half step a small kernel (k_half_next) turns the maxima into the
+// field's next exponents and makes the other field's table.
+#define HALF_SLOTS 32
+#define HALF_TAB 12
+#define HALF_E0 (-11)
+#define HALF_EMIN (-100)
+#define HALF_EMAX 100
+struct HalfPlanes {
+	const float *tab;                     // the step's scale table
+	unsigned *mCur;                       // the step's maxima
+};
+
+// the exponent a half step stores with, from the float bits m of the
+// largest magnitude of the previous step: M = f 2^x, f in [0.5, 1), gives
+// x - 11 (M 2^-e in [2^10, 2^11)); subnormal M gives the minimum
+__host__ __device__ __forceinline__ int halfExponent(unsigned m)
+{
+	if (m == 0) return HALF_E0;
+	if (m >= 0x7f800000u) return HALF_EMAX;
+	if (m < 0x00800000u) return HALF_EMIN;
+	const int e = (int)(m >> 23) - 126 - 11;
+	return e < HALF_EMIN ? HALF_EMIN : e > HALF_EMAX ? HALF_EMAX : e;
+}
+
+// 2^e as a float, e in [-126, 127]
+__device__ __forceinline__ float pow2f(int e) { return __uint_as_float((unsigned)(127 + e) << 23); }
+
+// a half value of p times s (s a power of two: exact)
+__device__ __forceinline__ float halfAt(const void *p, long long c, float s)
+{
+	return __half2float(__ushort_as_half(((const unsigned short *)p)[c])) * s;
+}
+
+// v 2^-e (inv = 2^-e) rounded to the nearest half, values beyond the half
+// range saturated at +-65504 (cvt .satfinite)
+__device__ __forceinline__ unsigned short halfOf(float v, float inv)
+{
+	unsigned short h;
+	asm("cvt.rn.satfinite.f16.f32 %0, %1;" : "=h"(h) : "f"(v * inv));
+	return h;
+}
+
 struct HalfStepParams {
 	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
 	int iMin, iMax, jMin, jMax, kMin, kMax;
@@ -91,6 +146,7 @@ struct HalfStepParams {
 	// n's range, bit 8 any object n >= 8, bit 13/14 CPML slab of the min/max
 	// face, bit 15 TFSF face plane
 	const unsigned short *cls[3];
+	HalfPlanes h;                         // FP16 storage (the HALF instances)
 };
 #define CLS_OBJ8 0x100u
 #define CLS_PML_LO 0x2000u

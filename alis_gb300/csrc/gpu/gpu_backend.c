@@ -33,6 +33,7 @@ typedef struct devWorld {
 	int ntf;
 	alisgpu_tfsf tf[MAX_TFSF];
 	int isAux;                /* the auxiliary world of a TFSF box */
+	int stepped;              /* has taken a half step */
 	struct devWorld *next;
 } devWorld;
 
@@ -429,10 +430,25 @@ void alis_be_world_streams(world W)
 	shareStreams(d);
 }
 
+/* FP16 field storage of the worlds the user steps (ALIS_FIELD_STORAGE=half;
+ * their TFSF auxiliary worlds stay float): set before a world's first
+ * half step, see alisgpu_world_set_storage */
+static int halfStorage(void)
+{
+	static int on = -1;
+	if (on < 0) {
+		const char *e = getenv("ALIS_FIELD_STORAGE");
+		on = e && !strcmp(e, "half");
+	}
+	return on;
+}
+
 static void halfStepAs(world W, int field, int attach)
 {
 	devWorld *d = findWorld(W);
 	if (!d) { fprintf(stderr, "alis: world unknown to the GPU backend\n"); exit(1); }
+	if (!d->stepped && !d->isAux && halfStorage()) CHECK("world_set_storage", alisgpu_world_set_storage(d->dw, ALISGPU_STORAGE_HALF));
+	d->stepped = 1;
 	if (d->ownStreams) shareStreams(d);
 	if (d->objectsDirty) uploadObjects(d);
 	alisgpu_ghost_copy g[MAX_GHOST];

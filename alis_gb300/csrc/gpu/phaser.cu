@@ -54,9 +54,11 @@ struct GatherParams {
 	long long start[7];
 	int box[6][7];                        // axis, i0, i1, j0, j1, k0, k1
 	float *out;                           // ring slot
+	const signed char *exE, *exH;         // half storage: the exponents per (component, plane) (else null)
 };
 
 extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, const float **H, Layout *L);
+extern "C" void alisgpu__world_half(const alisgpu_world *w, const signed char **exE, const signed char **exH);
 extern "C" cudaStream_t alisgpu__gather_begin(alisgpu_world *w, const int (*box)[6], int n);
 extern "C" void alisgpu__bind(alisgpu_world *w);
 extern "C" int alisgpu__gather_end(alisgpu_world *w, cudaStream_t st);
@@ -77,10 +79,19 @@ __device__ __forceinline__ void gatherCell(const GatherParams &P, long long t)
 	long long c = P.L.at(i, j, k);
 	long long n = c + (axis == 0 ? P.L.si : axis == 1 ? P.L.sj : 1);
 	float4 v;
-	v.x = P.E[c1][c];
-	v.y = P.E[c2][c];
-	v.z = P.H[c1][c] + P.H[c1][n];
-	v.w = P.H[c2][c] + P.H[c2][n];
+	if (P.exE) {
+		// a half world: each sample times its plane's power of two
+		const int ni = P.L.ni, pl = i - P.L.i0, pn = pl + (axis == 0);
+		v.x = halfAt(P.E[c1], c, pow2f(P.exE[c1 * ni + pl]));
+		v.y = halfAt(P.E[c2], c, pow2f(P.exE[c2 * ni + pl]));
+		v.z = halfAt(P.H[c1], c, pow2f(P.exH[c1 * ni + pl])) + halfAt(P.H[c1], n, pow2f(P.exH[c1 * ni + pn]));
+		v.w = halfAt(P.H[c2], c, pow2f(P.exH[c2 * ni + pl])) + halfAt(P.H[c2], n, pow2f(P.exH[c2 * ni + pn]));
+	} else {
+		v.x = P.E[c1][c];
+		v.y = P.E[c2][c];
+		v.z = P.H[c1][c] + P.H[c1][n];
+		v.w = P.H[c2][c] + P.H[c2][n];
+	}
 	reinterpret_cast<float4 *>(P.out)[t] = v;
 }
 
@@ -367,6 +378,7 @@ static void gatherParams(alisgpu_phaser *p, GatherParams &G)
 {
 	memset(&G, 0, sizeof G);
 	alisgpu__world_fields(p->w, 0, G.E, G.H, &G.L);
+	alisgpu__world_half(p->w, &G.exE, &G.exH);
 	G.nface = p->nface;
 	for (int f = 0; f <= p->nface; f++) G.start[f] = p->faceStart[f];
 	for (int f = 0; f < p->nface; f++) {
@@ -478,6 +490,7 @@ extern "C" int alisgpu_phaser_record(alisgpu_phaser *p, const float *phaseE, con
 		memset(&G, 0, sizeof G);
 		int rc = alisgpu__world_fields(p->w, 0, G.E, G.H, &G.L);
 		if (rc) return rc;
+		alisgpu__world_half(p->w, &G.exE, &G.exH);
 		G.nface = p->nface;
 		for (int f = 0; f <= p->nface; f++) G.start[f] = p->faceStart[f];
 		for (int f = 0; f < p->nface; f++) {

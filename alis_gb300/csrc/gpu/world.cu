@@ -307,7 +307,30 @@ struct alisgpu_world {
 	// what the cell-class tables of each field were made from: the CPML
 	// slabs, the TFSF boxes and the object boxes
 	std::vector<int> clsKey[2];
+	// FP16 storage (alisgpu_world_set_storage), per field: by the parity
+	// of the step, the exponents as read and as computed and the scales as
+	// read; the next step's inverse scales; the plane maxima of two steps
+	// in turn; the half steps taken.  written: a step or upload wrote the
+	// fields
+	int half;
+	signed char *ex[2][2], *exK[2][2];
+	float *sc[2][2], *inv[2], *tab[2];
+	unsigned *mx[2][2];
+	long long nHalf[2];
+	bool tabFresh[2];                      // tab[f] holds the scales of f's next step
+	bool written;
 };
+
+// the exponents of a half world's field as its readers use them now, and
+// their scales
+static inline const signed char *halfRead(const alisgpu_world *w, int field)
+{
+	return w->ex[field][(w->nHalf[field] + 1) & 1];
+}
+static inline const float *halfScales(const alisgpu_world *w, int field)
+{
+	return w->sc[field][(w->nHalf[field] + 1) & 1];
+}
 
 static inline void bindWorld(const alisgpu_world *w)
 {
@@ -413,6 +436,13 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 		if (w->H[m][c]) alisgpu__freeAsync(w->H[m][c]);
 	}
 	for (int c = 0; c < 3; c++) if (w->C[c]) alisgpu__freeAsync(w->C[c]);
+	for (int f = 0; f < 2; f++) {
+		for (int p = 0; p < 2; p++) {
+			alisgpu__freeAsync(w->ex[f][p]), alisgpu__freeAsync(w->exK[f][p]);
+			alisgpu__freeAsync(w->sc[f][p]), alisgpu__freeAsync(w->mx[f][p]);
+		}
+		alisgpu__freeAsync(w->inv[f]), alisgpu__freeAsync(w->tab[f]);
+	}
 	if (w->planeTab) alisgpu__freeAsync(w->planeTab);
 	if (w->matIdx) alisgpu__freeAsync(w->matIdx);
 	if (w->matTab) alisgpu__freeAsync(w->matTab);
@@ -503,6 +533,105 @@ extern "C" void *alisgpu_world_stream(const alisgpu_world *w)
 	return (void *)(w && w->group ? w->group->main : gDefaultGroup.main);
 }
 
+__global__ void k_fill(float *p, float v, int n)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t < n) p[t] = v;
+}
+
+static int halfTable(alisgpu_world *w, int field);
+
+// exponents and scales back to their start value (the first step finds
+// no maxima), maxima and step counts to zero
+static int halfStateReset(alisgpu_world *w)
+{
+	const int n = 3 * w->L.ni;
+	for (int f = 0; f < 2; f++) {
+		for (int p = 0; p < 2; p++) {
+			ALIS_CUDA(cudaMemsetAsync(w->ex[f][p], (unsigned char)(signed char)HALF_E0, n, gStream));
+			ALIS_CUDA(cudaMemsetAsync(w->exK[f][p], (unsigned char)(signed char)HALF_E0, n, gStream));
+			k_fill<<<(n + 255) / 256, 256, 0, gStream>>>(w->sc[f][p], ldexpf(1.0f, HALF_E0), n);
+			ALIS_CUDA(cudaMemsetAsync(w->mx[f][p], 0, (size_t)n * HALF_SLOTS * sizeof(unsigned), gStream));
+		}
+		k_fill<<<(n + 255) / 256, 256, 0, gStream>>>(w->inv[f], ldexpf(1.0f, -HALF_E0), n);
+		alisgpu__count_launch(), alisgpu__count_launch(), alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+		w->nHalf[f] = 0;
+	}
+	for (int f = 0; f < 2; f++) {
+		int rc = halfTable(w, f);
+		if (rc) return rc;
+	}
+	return ALISGPU_OK;
+}
+
+// device bytes of a half world's exponent, scale and maxima arrays
+static size_t halfPlaneBytes(const alisgpu_world *w)
+{
+	const size_t n = 3 * (size_t)w->L.ni;
+	return 2 * (2 * (2 * n + n * sizeof(float) + n * HALF_SLOTS * sizeof(unsigned)) + n * sizeof(float) +
+	            (size_t)w->L.ni * HALF_TAB * sizeof(float));
+}
+
+extern "C" int alisgpu_world_set_storage(alisgpu_world *w, int storage)
+{
+	ALIS_BATCH_GUARD();
+	bindWorld(w);
+	if (!w || (storage != ALISGPU_STORAGE_FLOAT && storage != ALISGPU_STORAGE_HALF))
+		return alisgpu__fail(ALISGPU_EINVAL, "world_set_storage: bad argument");
+	if (storage == w->half) return ALISGPU_OK;
+	if (w->written || w->nHalf[0] || w->nHalf[1])
+		return alisgpu__fail(ALISGPU_EINVAL, "world_set_storage: the world has been stepped or written");
+	if (storage == ALISGPU_STORAGE_HALF && w->g.complexField)
+		return alisgpu__fail(ALISGPU_ENOTSUP, "world_set_storage: half storage needs real fields");
+	fullJoin();
+	const size_t n = w->L.elems(), esz = storage == ALISGPU_STORAGE_HALF ? 2 : sizeof(float), np = 3 * (size_t)w->L.ni;
+	// the new arrays first: on failure the world keeps its form
+	float *E[3] = {}, *H[3] = {}, *sc[2][2] = {}, *inv[2] = {}, *tab[2] = {};
+	signed char *ex[2][2] = {}, *exK[2][2] = {};
+	unsigned *mx[2][2] = {};
+	auto release = [](float *const (&e)[3], float *const (&h)[3], signed char *const (&x)[2][2], signed char *const (&k)[2][2],
+	                  float *const (&c)[2][2], float *const (&iv)[2], float *const (&tb)[2], unsigned *const (&m)[2][2]) {
+		for (int q = 0; q < 3; q++) alisgpu__freeAsync(e[q]), alisgpu__freeAsync(h[q]);
+		for (int f = 0; f < 2; f++) {
+			for (int p = 0; p < 2; p++)
+				alisgpu__freeAsync(x[f][p]), alisgpu__freeAsync(k[f][p]), alisgpu__freeAsync(c[f][p]), alisgpu__freeAsync(m[f][p]);
+			alisgpu__freeAsync(iv[f]), alisgpu__freeAsync(tb[f]);
+		}
+	};
+	cudaError_t e = cudaSuccess;
+	for (int c = 0; c < 3 && e == cudaSuccess; c++) {
+		if ((e = alisgpu__mallocAsync(&E[c], n * esz)) == cudaSuccess) e = alisgpu__mallocAsync(&H[c], n * esz);
+		if (e == cudaSuccess) e = cudaMemsetAsync(E[c], 0, n * esz, gStream);
+		if (e == cudaSuccess) e = cudaMemsetAsync(H[c], 0, n * esz, gStream);
+	}
+	if (storage == ALISGPU_STORAGE_HALF)
+		for (int f = 0; f < 2 && e == cudaSuccess; f++) {
+			for (int p = 0; p < 2 && e == cudaSuccess; p++) {
+				if ((e = alisgpu__mallocAsync(&ex[f][p], np)) == cudaSuccess) e = alisgpu__mallocAsync(&exK[f][p], np);
+				if (e == cudaSuccess) e = alisgpu__mallocAsync(&sc[f][p], np * sizeof(float));
+				if (e == cudaSuccess) e = alisgpu__mallocAsync(&mx[f][p], np * HALF_SLOTS * sizeof(unsigned));
+			}
+			if (e == cudaSuccess) e = alisgpu__mallocAsync(&inv[f], np * sizeof(float));
+			if (e == cudaSuccess) e = alisgpu__mallocAsync(&tab[f], (size_t)w->L.ni * HALF_TAB * sizeof(float));
+		}
+	if (e != cudaSuccess) {
+		release(E, H, ex, exK, sc, inv, tab, mx);
+		return alisgpu__check(e, "world_set_storage");
+	}
+	// the old arrays go, the new ones take their place
+	float *oE[3], *oH[3];
+	for (int c = 0; c < 3; c++) oE[c] = w->E[0][c], oH[c] = w->H[0][c], w->E[0][c] = E[c], w->H[0][c] = H[c];
+	release(oE, oH, w->ex, w->exK, w->sc, w->inv, w->tab, w->mx);
+	memcpy(w->ex, ex, sizeof ex), memcpy(w->exK, exK, sizeof exK), memcpy(w->sc, sc, sizeof sc);
+	memcpy(w->inv, inv, sizeof inv), memcpy(w->tab, tab, sizeof tab), memcpy(w->mx, mx, sizeof mx);
+	const size_t before = w->half ? 2 : sizeof(float);
+	w->bytes = w->bytes - 6 * n * before + 6 * n * esz;
+	w->bytes = storage == ALISGPU_STORAGE_HALF ? w->bytes + halfPlaneBytes(w) : w->bytes - halfPlaneBytes(w);
+	w->half = storage;
+	return w->half ? halfStateReset(w) : ALISGPU_OK;
+}
+
 extern "C" int alisgpu_world_reset(alisgpu_world *w)
 {
 	ALIS_BATCH_GUARD();
@@ -511,7 +640,12 @@ extern "C" int alisgpu_world_reset(alisgpu_world *w)
 	fullJoin();
 	if (w) w->pendingE.clear();
 	if (!w) return alisgpu__fail(ALISGPU_EINVAL, "world_reset: null world");
-	size_t n = w->L.elems() * sizeof(float);
+	size_t n = w->L.elems() * (w->half ? 2 : sizeof(float));
+	if (w->half) {
+		int rc = halfStateReset(w);
+		if (rc) return rc;
+	}
+	w->written = false;
 	for (int m = 0; m <= w->g.complexField; m++) for (int c = 0; c < 3; c++) {
 		ALIS_CUDA(cudaMemsetAsync(w->E[m][c], 0, n, gStream));
 		ALIS_CUDA(cudaMemsetAsync(w->H[m][c], 0, n, gStream));
@@ -739,6 +873,28 @@ static float *fieldPtr(alisgpu_world *w, int field, int m, int comp)
 	return field ? w->H[m][comp] : w->E[m][comp];
 }
 
+// one component of a half world as floats, rows of nk in the host's order
+__global__ void k_field_decode(const float *src, const signed char *ex, const Layout L, float *out)
+{
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= (long long)L.ni * L.nj * L.nk) return;
+	const long long row = t / L.nk;
+	const int kk = (int)(t - row * L.nk);
+	out[t] = halfAt(src, row * L.sj + ALIS_KOFF + kk, pow2f(ex[row / L.nj]));
+}
+
+// the world's observer scratch, grown to n floats
+static int scratchFloats(alisgpu_world *w, size_t n)
+{
+	if (n <= w->planeTabFloats) return ALISGPU_OK;
+	ALIS_CUDA(cudaStreamSynchronize(gStream));
+	if (w->planeTab) alisgpu__freeAsync(w->planeTab);
+	w->planeTab = 0, w->planeTabFloats = 0;
+	ALIS_CUDA(alisgpu__mallocAsync(&w->planeTab, n * sizeof(float)));
+	w->planeTabFloats = n;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int comp, float *host)
 {
 	ALIS_BATCH_GUARD();
@@ -751,6 +907,17 @@ extern "C" int alisgpu_field_download(alisgpu_world *w, int field, int m, int co
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_download: bad argument");
 	const Layout &L = w->L;
+	if (w->half) {
+		const size_t n = (size_t)L.ni * L.nj * L.nk;
+		int rc = scratchFloats(w, n);
+		if (rc) return rc;
+		k_field_decode<<<(unsigned)((n + 255) / 256), 256, 0, gStream>>>(d, halfRead(w, field) + comp * L.ni, L, w->planeTab);
+		alisgpu__count_launch();
+		ALIS_CUDA(cudaGetLastError());
+		ALIS_CUDA(cudaMemcpyAsync(host, w->planeTab, n * sizeof(float), cudaMemcpyDeviceToHost, gStream));
+		ALIS_CUDA(cudaStreamSynchronize(gStream));
+		return ALISGPU_OK;
+	}
 	ALIS_CUDA(cudaMemcpy2DAsync(host, L.nk * sizeof(float), d + ALIS_KOFF, L.sj * sizeof(float), L.nk * sizeof(float),
 	                            (size_t)L.ni * L.nj, cudaMemcpyDeviceToHost, gStream));
 	ALIS_CUDA(cudaStreamSynchronize(gStream));
@@ -766,6 +933,8 @@ extern "C" int alisgpu_field_upload(alisgpu_world *w, int field, int m, int comp
 	if (w && field == 0) w->pendingE.clear();        // the host's halo wins
 	float *d = w && host ? fieldPtr(w, field, m, comp) : 0;
 	if (!d) return alisgpu__fail(ALISGPU_EINVAL, "field_upload: bad argument");
+	if (w->half) return alisgpu__fail(ALISGPU_ENOTSUP, "field_upload: the world stores half values");
+	w->written = true;
 	const Layout &L = w->L;
 	ALIS_CUDA(cudaMemcpy2DAsync(d + ALIS_KOFF, L.sj * sizeof(float), host, L.nk * sizeof(float), L.nk * sizeof(float),
 	                            (size_t)L.ni * L.nj, cudaMemcpyHostToDevice, gStream));
@@ -1021,13 +1190,74 @@ __device__ __forceinline__ void tfsfCell(const HalfStepParams &P, int i, int j, 
 	}
 }
 
+// Field loads and stores of a half step.  Float storage, or (HALF) IEEE
+// half values times the plane's power of two.  The scales are the same
+// for a warp (one plane): uniform loads from the plane's entry of the
+// step's table, the other field's at plane i (HS_G) and i + ALT (HS_GI),
+// the stepped field's as stored (HS_F) and the inverse scales the step
+// stores with (HS_INV).
+#define HS_T(i) (P.h.tab + (size_t)((i) - P.L.i0) * HALF_TAB)
+#define HS_G(q) (HALF ? __ldg(HS_T(i) + (q)) : 1.0f)
+#define HS_GI(q) (HALF ? __ldg(HS_T(i) + 3 + (q)) : 1.0f)
+#define HS_F(q) (HALF ? __ldg(HS_T(i) + 6 + (q)) : 1.0f)
+#define HS_INV(q) __ldg(HS_T(i) + 9 + (q))
+template <bool HALF>
+__device__ __forceinline__ float ldG(const float *p, int c, float s)
+{
+	if (HALF) return __half2float(__ushort_as_half(__ldg((const unsigned short *)p + c))) * s;
+	return __ldg(p + c);
+}
+template <bool HALF>
+__device__ __forceinline__ float ldF(const float *p, int c, float s)
+{
+	if (HALF) return halfAt(p, c, s);
+	return p[c];
+}
+template <bool HALF>
+__device__ __forceinline__ void stF(float *p, int c, float v, float inv)
+{
+	if (HALF) ((unsigned short *)p)[c] = halfOf(v, inv);
+	else p[c] = v;
+}
+// the step's largest magnitudes per component of plane i (float bits of
+// |v|, NaN above infinity): a maximum over the lanes here, one atomic per
+// component into one of the plane's HALF_SLOTS words, chosen by the
+// warp's position, so that the plane's warps spread over them
+__device__ __forceinline__ void halfMax(const HalfStepParams &P, int i, float fx, float fy, float fz)
+{
+	const unsigned mask = __activemask();
+	const unsigned ax = __reduce_max_sync(mask, __float_as_uint(fabsf(fx)));
+	const unsigned ay = __reduce_max_sync(mask, __float_as_uint(fabsf(fy)));
+	const unsigned az = __reduce_max_sync(mask, __float_as_uint(fabsf(fz)));
+	if ((int)(threadIdx.x & 31) == __ffs(mask) - 1) {
+		const int slot = (int)((blockIdx.x * blockDim.y + blockIdx.y + threadIdx.y) % HALF_SLOTS);
+		unsigned *m = P.h.mCur + (size_t)(i - P.L.i0) * HALF_SLOTS + slot;
+		const size_t comp = (size_t)P.L.ni * HALF_SLOTS;
+		atomicMax(m, ax);
+		atomicMax(m + comp, ay);
+		atomicMax(m + 2 * comp, az);
+	}
+}
+template <bool HALF>
+__device__ __forceinline__ void storeCell(const HalfStepParams &P, int i, int c, float fx, float fy, float fz)
+{
+	if (HALF) {
+		stF<true>(P.F[0], c, fx, HS_INV(0));
+		stF<true>(P.F[1], c, fy, HS_INV(1));
+		stF<true>(P.F[2], c, fz, HS_INV(2));
+		halfMax(P, i, fx, fy, fz);
+	} else {
+		P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+	}
+}
+
 // One cell of a half step, in the reference order: conductivity and -J
 // (E), curl, CPML faces, TFSF corrections, ADE update (H).  Three per-axis
 // bit tables classify the cell by its i, j and k (CPML slab side, TFSF face
 // plane, dispersive object range); a cell with none of these bits takes
 // only the curl.  list/nIter: the objects to visit (a tile's list, or all
 // objects filtered by the class bits when list is null).
-template <int ALT>
+template <int ALT, bool HALF = false>
 __device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, int k, const int *list, int nIter)
 {
 	const int sj = (int)P.L.sj, si = (int)P.L.si;
@@ -1036,11 +1266,12 @@ __device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, 
 	const unsigned any = bi | bj | bk;
 	const unsigned objm = bi & bj & bk & 0x1FFu;
 	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
-	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
-	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
-	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
-	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
-	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const float sx = HS_G(0), sy = HS_G(1), sz = HS_G(2);
+	const float gx0 = ldG<HALF>(Gx, c, sx), gy0 = ldG<HALF>(Gy, c, sy), gz0 = ldG<HALF>(Gz, c, sz);
+	const float gyk = ldG<HALF>(Gy, c + ALT, sy), gxk = ldG<HALF>(Gx, c + ALT, sx);
+	const float gzj = ldG<HALF>(Gz, c + ALT * sj, sz), gxj = ldG<HALF>(Gx, c + ALT * sj, sx);
+	const float gzi = ldG<HALF>(Gz, c + ALT * si, HS_GI(2)), gyi = ldG<HALF>(Gy, c + ALT * si, HS_GI(1));
+	float fx = ldF<HALF>(P.F[0], c, HS_F(0)), fy = ldF<HALF>(P.F[1], c, HS_F(1)), fz = ldF<HALF>(P.F[2], c, HS_F(2));
 	const bool hasC = P.C[0] != 0;
 	float cx = 1, cy = 1, cz = 1;
 	if (hasC) cx = __ldg(P.C[0] + c), cy = __ldg(P.C[1] + c), cz = __ldg(P.C[2] + c);
@@ -1071,16 +1302,16 @@ __device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, 
 	}
 	if (any & CLS_TFSF) tfsfCell<ALT>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
 	if (ALT == -1 && objm) objectsAfterCurl(P, i, j, k, gx0, gy0, gz0, objm, list, nIter);
-	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+	storeCell<HALF>(P, i, c, fx, fy, fz);
 }
 
 // Cells on a TFSF face plane or inside a dispersive object box run the
 // full sequence out of line (their neighbours' lean code stays small);
 // P is the kernel's __grid_constant__ parameter, passed by reference.
-template <int ALT>
+template <int ALT, bool HALF = false>
 __device__ __noinline__ void hardCell(const HalfStepParams &P, int i, int j, int k, const int *list, int nIter)
 {
-	stepCell<ALT>(P, i, j, k, list, nIter);
+	stepCell<ALT, HALF>(P, i, j, k, list, nIter);
 }
 
 #define TX 32
@@ -1094,7 +1325,7 @@ static const int kTyChoice[ALIS_TY_CHOICES] = { 2, 4, 8 };
 // The lean tiers for NC cells k, k + TX, ... of one row, all in range and
 // none of them hard: the loads of every cell first, then the updates, so
 // the cells' memory round trips overlap and share their index arithmetic.
-template <int ALT, int NC>
+template <int ALT, int NC, bool HALF = false>
 __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j, int k, unsigned bi, unsigned bj, const unsigned *bk)
 {
 	const int sj = (int)P.L.sj, si = (int)P.L.si;
@@ -1106,11 +1337,13 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 #pragma unroll
 	for (int q = 0; q < NC; q++) {
 		const int c = c0 + q * TX;
-		gx0[q] = __ldg(Gx + c), gy0[q] = __ldg(Gy + c), gz0[q] = __ldg(Gz + c);
-		gyk[q] = __ldg(Gy + c + ALT), gxk[q] = __ldg(Gx + c + ALT);
-		gzj[q] = __ldg(Gz + c + ALT * sj), gxj[q] = __ldg(Gx + c + ALT * sj);
-		gzi[q] = __ldg(Gz + c + ALT * si), gyi[q] = __ldg(Gy + c + ALT * si);
-		fx[q] = P.F[0][c], fy[q] = P.F[1][c], fz[q] = P.F[2][c];
+		const float sx = HS_G(0), sy = HS_G(1), sz = HS_G(2);
+		gx0[q] = ldG<HALF>(Gx, c, sx), gy0[q] = ldG<HALF>(Gy, c, sy), gz0[q] = ldG<HALF>(Gz, c, sz);
+		gyk[q] = ldG<HALF>(Gy, c + ALT, sy), gxk[q] = ldG<HALF>(Gx, c + ALT, sx);
+		gzj[q] = ldG<HALF>(Gz, c + ALT * sj, sz), gxj[q] = ldG<HALF>(Gx, c + ALT * sj, sx);
+		gzi[q] = ldG<HALF>(Gz, c + ALT * si, HS_GI(2)), gyi[q] = ldG<HALF>(Gy, c + ALT * si, HS_GI(1));
+		fx[q] = ldF<HALF>(P.F[0], c, HS_F(0)), fy[q] = ldF<HALF>(P.F[1], c, HS_F(1));
+		fz[q] = ldF<HALF>(P.F[2], c, HS_F(2));
 		dz[q] = __ldg(P.dtd[2] + (k + q * TX - P.kMIN));
 		cx[q] = 1, cy[q] = 1, cz[q] = 1;
 		if (hasC) {
@@ -1150,23 +1383,24 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 		}
 		// TFSF k face planes (cells on an i or j face plane are hard)
 		if (bk[q] & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, kq, fx[q], fy[q], fz[q], hasC, cx[q], cy[q], cz[q]);
-		P.F[0][c] = fx[q], P.F[1][c] = fy[q], P.F[2][c] = fz[q];
+		storeCell<HALF>(P, i, c, fx[q], fy[q], fz[q]);
 	}
 }
 
 // A cell with no class bits: the curl alone (reference
 // src/update.c:109-118), with the loads and arithmetic of leanCells.
-template <int ALT>
+template <int ALT, bool HALF = false>
 __device__ __forceinline__ void plainCell(const HalfStepParams &P, int i, int j, int k)
 {
 	const int sj = (int)P.L.sj, si = (int)P.L.si;
 	const int c = (i - P.L.i0) * si + (j - P.L.j0) * sj + (k - P.L.k0) + ALIS_KOFF;
 	const float *Gx = P.G[0], *Gy = P.G[1], *Gz = P.G[2];
-	const float gx0 = __ldg(Gx + c), gy0 = __ldg(Gy + c), gz0 = __ldg(Gz + c);
-	const float gyk = __ldg(Gy + c + ALT), gxk = __ldg(Gx + c + ALT);
-	const float gzj = __ldg(Gz + c + ALT * sj), gxj = __ldg(Gx + c + ALT * sj);
-	const float gzi = __ldg(Gz + c + ALT * si), gyi = __ldg(Gy + c + ALT * si);
-	float fx = P.F[0][c], fy = P.F[1][c], fz = P.F[2][c];
+	const float sx = HS_G(0), sy = HS_G(1), sz = HS_G(2);
+	const float gx0 = ldG<HALF>(Gx, c, sx), gy0 = ldG<HALF>(Gy, c, sy), gz0 = ldG<HALF>(Gz, c, sz);
+	const float gyk = ldG<HALF>(Gy, c + ALT, sy), gxk = ldG<HALF>(Gx, c + ALT, sx);
+	const float gzj = ldG<HALF>(Gz, c + ALT * sj, sz), gxj = ldG<HALF>(Gx, c + ALT * sj, sx);
+	const float gzi = ldG<HALF>(Gz, c + ALT * si, HS_GI(2)), gyi = ldG<HALF>(Gy, c + ALT * si, HS_GI(1));
+	float fx = ldF<HALF>(P.F[0], c, HS_F(0)), fy = ldF<HALF>(P.F[1], c, HS_F(1)), fz = ldF<HALF>(P.F[2], c, HS_F(2));
 	const float dx = __ldg(P.dtd[0] + (i - P.iMIN)), dy = __ldg(P.dtd[1] + (j - P.jMIN)), dz = __ldg(P.dtd[2] + (k - P.kMIN));
 	if (P.C[0]) {
 		float cx, cy, cz;
@@ -1184,7 +1418,7 @@ __device__ __forceinline__ void plainCell(const HalfStepParams &P, int i, int j,
 		fy += (dx * (gz0 - gzi) + dz * (gxk - gx0));
 		fz += (dy * (gx0 - gxj) + dx * (gyi - gy0));
 	}
-	P.F[0][c] = fx, P.F[1][c] = fy, P.F[2][c] = fz;
+	storeCell<HALF>(P, i, c, fx, fy, fz);
 }
 
 // Fused half step of a large world over one tile: one thread per cell,
@@ -1197,7 +1431,7 @@ __device__ __forceinline__ void plainCell(const HalfStepParams &P, int i, int j,
 // (at most 2^31 elements per array, checked on the host).  Worlds with
 // more than 8 objects add a per-tile list of the objects that meet it
 // (tileList/nlist in shared memory, one block's).
-template <int ALT, int TY_>
+template <int ALT, int TY_, bool HALF = false>
 __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, int by, int plane, int *tileList, int *nlist)
 {
 	const int k = P.kMIN + bx * TX + threadIdx.x;
@@ -1236,12 +1470,12 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, i
 	if (inRange) bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
 	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI | CLS_TFSF)) && !(bi & bj & bk & 0x1FFu);
 	if (__all_sync(0xffffffffu, plain)) {
-		plainCell<ALT>(P, i, j, k);
+		plainCell<ALT, HALF>(P, i, j, k);
 		return;
 	}
 	if (!inRange) return;
 	if (!((bi | bj) & CLS_TFSF) && !(bi & bj & bk & 0x1FFu)) {
-		leanCells<ALT, 1>(P, i, j, k, bi, bj, &bk);
+		leanCells<ALT, 1, HALF>(P, i, j, k, bi, bj, &bk);
 		return;
 	}
 	// hard cells run the full sequence out of line (object loops: the
@@ -1249,15 +1483,15 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, i
 	const int *list = 0;
 	int nIter = P.nobj;
 	if (manyObj && *nlist <= ALIS_TILE_OBJ) list = tileList, nIter = *nlist;
-	hardCell<ALT>(P, i, j, k, list, nIter);
+	hardCell<ALT, HALF>(P, i, j, k, list, nIter);
 }
 
-template <int ALT, int TY>
+template <int ALT, int TY, bool HALF = false>
 __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	halfStepBlock<ALT, TY>(P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, tileList, &nlist);
+	halfStepBlock<ALT, TY, HALF>(P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, tileList, &nlist);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1274,6 +1508,7 @@ struct SourceParams {
 	alisgpu_source_patch p[ALIS_MAXSRC];
 	const float *vdev;                       // values beyond the inline buffer
 	unsigned int *err;
+	const signed char *ex;                   // half storage: the step's exponents (else null)
 	float v[ALIS_MAXSRCV];
 };
 
@@ -1293,7 +1528,14 @@ __device__ __forceinline__ void sourcesBlock(const SourceParams &P, const float 
 				atomicOr(P.err, 4u);
 				continue;
 			}
-			F[P.L.at(i, j, k)] += v;
+			const long long at = P.L.at(i, j, k);
+			if (P.ex) {
+				// a half world: the sum of the stored value and v, rounded with the plane's exponent
+				const int e = P.ex[s.comp * P.L.ni + (i - P.L.i0)];
+				((unsigned short *)F)[at] = halfOf(halfAt(F, at, pow2f(e)) + v, pow2f(-e));
+			} else {
+				F[at] += v;
+			}
 		}
 		__syncthreads();
 	}
@@ -1359,6 +1601,7 @@ __global__ void k_ghost(const GhostParams P)
 // all blocks of a cooperative launch are resident, so the barrier ends.
 #define ALIS_GHOST_MAX 48
 #define ALIS_GHOST_NEAR 6
+#define ALIS_GHOST_RED 16
 struct GhostLevels {
 	Layout L;
 	float *F[2][3];
@@ -1374,6 +1617,14 @@ struct GhostLevels {
 	// -1: test every copy)
 	signed char nLater[ALIS_GHOST_MAX], nEarlier[ALIS_GHOST_MAX];
 	unsigned char later[ALIS_GHOST_MAX][ALIS_GHOST_NEAR], earlier[ALIS_GHOST_MAX][ALIS_GHOST_NEAR];
+	// half storage: the exponents of the step as computed and as read, the
+	// scales as read, and the (component, plane) whose read exponent the
+	// copies take from another plane's computed one
+	const signed char *exK;
+	signed char *ex;
+	float *sc;
+	int nred;
+	short red[ALIS_GHOST_RED][3];
 };
 
 __global__ void __launch_bounds__(256) k_ghost_levels(const __grid_constant__ GhostLevels P)
@@ -1409,9 +1660,15 @@ __device__ __forceinline__ bool inCopy(const alisgpu_ghost_copy &c, int i, int j
 	return c.i0 <= i && i <= c.i1 && c.j0 <= j && j <= c.j1 && c.k0 <= k && k <= c.k1;
 }
 
-template <bool CHECK>
+template <bool CHECK, bool HALF = false>
 __device__ __forceinline__ void ghostChainCell(const GhostLevels &P, int t, unsigned int *flag)
 {
+	if (HALF && t < P.nred) {
+		const int ni = P.L.ni;
+		const int e = P.exK[P.red[t][0] * ni + P.red[t][2]];
+		P.ex[P.red[t][0] * ni + P.red[t][1]] = (signed char)e;
+		P.sc[P.red[t][0] * ni + P.red[t][1]] = pow2f(e);
+	}
 	if (t >= P.start[P.n]) return;
 	int q = 0;
 	while (t >= P.start[q + 1]) q++;
@@ -1456,6 +1713,16 @@ __device__ __forceinline__ void ghostChainCell(const GhostLevels &P, int t, unsi
 	}
 	const long long s = L.at(ci, cj, ck), d = L.at(i, j, k);
 	float *F = P.F[0][g.comp];
+	if (HALF) {
+		// real fields: the root's value times the chain's factors (+-1, 0:
+		// exact), stored with the exponent of the root's plane -- the plane
+		// the destination plane reads its exponent from after the copies
+		const int e = P.exK[g.comp * L.ni + (ci - L.i0)];
+		float f = halfAt(F, s, pow2f(e));
+		for (int l = depth - 1; l >= 0; l--) f = P.c[chain[l]].cosk * f;
+		((unsigned short *)F)[d] = halfOf(f, pow2f(-e));
+		return;
+	}
 	if (P.complexField) {
 		float *G = P.F[1][g.comp];
 		float f = F[s], gg = G[s];
@@ -1472,10 +1739,10 @@ __device__ __forceinline__ void ghostChainCell(const GhostLevels &P, int t, unsi
 	}
 }
 
-template <bool CHECK>
+template <bool CHECK, bool HALF = false>
 __global__ void __launch_bounds__(256) k_ghost_chain(const __grid_constant__ GhostLevels P, unsigned int *flag)
 {
-	ghostChainCell<CHECK>(P, blockIdx.x * blockDim.x + threadIdx.x, flag);
+	ghostChainCell<CHECK, HALF>(P, blockIdx.x * blockDim.x + threadIdx.x, flag);
 }
 
 // Small worlds (the TFSF auxiliary columns, tiny test worlds): the whole
@@ -1598,7 +1865,7 @@ struct FusedStepParams {
 	SmallStepParams aux;
 };
 
-template <int ALT, int TY>
+template <int ALT, int TY, bool HALF = false>
 __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const __grid_constant__ FusedStepParams F)
 {
 	if (blockIdx.z == 0) {
@@ -1607,21 +1874,27 @@ __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const 
 	}
 	__shared__ int tileList[ALIS_TILE_OBJ];
 	__shared__ int nlist;
-	halfStepBlock<ALT, TY>(F.P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z - 1, tileList, &nlist);
+	halfStepBlock<ALT, TY, HALF>(F.P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z - 1, tileList, &nlist);
 }
 
 // one half-step launch with block height kTyChoice[v] (v a runtime choice)
-template <int ALT>
-static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
+template <int ALT, bool HALF>
+static void launchHalfStepAs(int ty, dim3 g, dim3 block, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st)
 {
-	const int ty = kTyChoice[v];
-	dim3 block(TX, ty, 1);
-	dim3 g(grid.x, grid.y, grid.z + (F ? 1 : 0));
-#define ALIS_LAUNCH(TY) do { if (F) k_half_step_aux<ALT, TY><<<g, block, 0, st>>>(*F); else k_half_step<ALT, TY><<<g, block, 0, st>>>(P); } while (0)
+#define ALIS_LAUNCH(TY) do { if (F) k_half_step_aux<ALT, TY, HALF><<<g, block, 0, st>>>(*F); else k_half_step<ALT, TY, HALF><<<g, block, 0, st>>>(P); } while (0)
 	if (ty == 2) ALIS_LAUNCH(2);
 	else if (ty == 8) ALIS_LAUNCH(8);
 	else ALIS_LAUNCH(4);
 #undef ALIS_LAUNCH
+}
+template <int ALT>
+static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const FusedStepParams *F, cudaStream_t st, bool half = false)
+{
+	const int ty = kTyChoice[v];
+	dim3 block(TX, ty, 1);
+	dim3 g(grid.x, grid.y, grid.z + (F ? 1 : 0));
+	if (half) launchHalfStepAs<ALT, true>(ty, g, block, P, F, st);
+	else launchHalfStepAs<ALT, false>(ty, g, block, P, F, st);
 }
 
 // ---------------------------------------------------------------------
@@ -2077,10 +2350,53 @@ static int recordGhosts(alisgpu_world *w, int field, const GhostLevels &GL, long
 // The ghost copies of a half step.  With record set (a batch records the
 // world's half step) the one-launch form joins the batch group; the other
 // forms launch the group first and then run on their own.
+// Ghost copies of a half world move values exactly: real copies by +-1 or
+// 0, each stored with the exponent of the plane its chain starts in.  A
+// copy between x planes takes its destination plane to the exponent of
+// the plane it reads, so it must write the plane whole: every cell the
+// half step updates there, and every cell an earlier copy of the component
+// wrote there.  Fills the list's plane redirects; false when the list
+// does not qualify.
+static bool halfGhostPlan(const alisgpu_world *w, const alisgpu_ghost_copy *gl, int n, GhostLevels &GL)
+{
+	const Layout &L = w->L;
+	const alisgpu_geometry &g = w->g;
+	std::vector<int> es(3 * (size_t)L.ni);
+	for (int q = 0; q < 3; q++) for (int p = 0; p < L.ni; p++) es[q * L.ni + p] = p;
+	for (int c = 0; c < n; c++) {
+		const alisgpu_ghost_copy &x = gl[c];
+		if (x.i1 < x.i0 || x.j1 < x.j0 || x.k1 < x.k0) continue;
+		if (x.comp < 0 || x.comp > 2 || !(x.cosk == 1.0f || x.cosk == -1.0f || x.cosk == 0.0f)) return false;
+		if (x.di == 0) continue;
+		if (x.i0 + x.di <= x.i1 && x.i1 + x.di >= x.i0) return false;
+		const bool covers = x.j0 <= g.jMIN && x.j1 >= g.jMAX && x.k0 <= g.kMIN && x.k1 >= g.kMAX;
+		for (int p = x.i0; p <= x.i1; p++) {
+			if (p < L.i0 || p >= L.i0 + L.ni || p + x.di < L.i0 || p + x.di >= L.i0 + L.ni) return false;
+			if (p >= g.iMIN && p <= g.iMAX && !covers) return false;
+			for (int b = 0; b < c; b++) {
+				const alisgpu_ghost_copy &y = gl[b];
+				if (y.comp != x.comp || y.i1 < y.i0 || y.j1 < y.j0 || y.k1 < y.k0 || p < y.i0 || p > y.i1) continue;
+				if (y.j0 < x.j0 || y.j1 > x.j1 || y.k0 < x.k0 || y.k1 > x.k1) return false;
+			}
+			es[x.comp * L.ni + (p - L.i0)] = es[x.comp * L.ni + (p + x.di - L.i0)];
+		}
+	}
+	GL.nred = 0;
+	for (int q = 0; q < 3; q++) for (int p = 0; p < L.ni; p++) {
+		if (es[q * L.ni + p] == p) continue;
+		if (GL.nred == ALIS_GHOST_RED) return false;
+		GL.red[GL.nred][0] = (short)q, GL.red[GL.nred][1] = (short)p, GL.red[GL.nred][2] = (short)es[q * L.ni + p];
+		GL.nred++;
+	}
+	return true;
+}
+
 static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, int n, bool record = false)
 {
 	const alisgpu_geometry &g = w->g;
 	if (n <= 0) return ALISGPU_OK;
+	if (w->half && (record || n > ALIS_GHOST_MAX))
+		return alisgpu__fail(ALISGPU_ENOTSUP, "ghost copies: %d copies of a half world", n);
 	if (record && w->ghostChain[field] && w->bG[field].dev && w->ghostSeen[field].size() == (size_t)n &&
 	    !memcmp(w->ghostSeen[field].data(), gl, n * sizeof *gl)) {
 		// the list of the last recorded half step: its one-launch form is in the slot
@@ -2165,6 +2481,21 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 				w->ghostChain[field] = h == 0;
 			}
 			if (w->ghostChain[field] && record) return recordGhosts(w, field, GL, total);
+			if (w->ghostChain[field] && w->half) {
+				if (!halfGhostPlan(w, gl, n, GL))
+					return alisgpu__fail(ALISGPU_ENOTSUP, "ghost copies: the list does not move whole planes of a half world");
+				const int cur = (int)((w->nHalf[field] + 1) & 1);
+				GL.exK = w->exK[field][cur], GL.ex = w->ex[field][cur], GL.sc = w->sc[field][cur];
+				// the redirected scales are read by both fields' next steps
+				if (GL.nred) w->tabFresh[0] = w->tabFresh[1] = false;
+				const unsigned hb = (unsigned)((std::max<long long>(total, GL.nred) + 255) / 256);
+				int slot = alisgpu__prof_start();
+				k_ghost_chain<false, true><<<hb, 256, 0, gStream>>>(GL, nullptr);
+				alisgpu__prof_stop(slot, ALISGPU_K_GHOST);
+				alisgpu__count_launch();
+				ALIS_CUDA(cudaGetLastError());
+				return ALISGPU_OK;
+			}
 			if (w->ghostChain[field]) {
 				int slot = alisgpu__prof_start();
 				k_ghost_chain<false><<<blocks, 256, 0, gStream>>>(GL, nullptr);
@@ -2177,6 +2508,7 @@ static int runGhosts(alisgpu_world *w, int field, const alisgpu_ghost_copy *gl, 
 			memset(GL.start, 0, sizeof GL.start);
 			GL.n = 0;
 		}
+		if (w->half) return alisgpu__fail(ALISGPU_ENOTSUP, "ghost copies: chains that a half world cannot run in one launch");
 		if (record) {
 			int rc = alisgpu__batch_flush();
 			if (rc) return rc;
@@ -2435,6 +2767,100 @@ static int recordHalfStep(alisgpu_world *w, const alisgpu_half_step *s, HalfStep
 	return ALISGPU_OK;
 }
 
+// The scale table of a half world's field X for its next step: per
+// updated plane, the other field's scales at the plane and at the plane +
+// ALT of X (as read now), X's scales as read now, X's inverse scales.
+struct HalfTableParams {
+	const float *scG, *scOld, *inv;
+	float *tab;
+	int ni, p0, p1, alt;
+};
+
+__device__ __forceinline__ void halfTableEntry(const HalfTableParams &T, int t)
+{
+	if (t >= T.ni * HALF_TAB) return;
+	const int pl = t / HALF_TAB, k = t % HALF_TAB, q = k % 3;
+	if (pl < T.p0 || pl > T.p1) return;
+	const int at = q * T.ni + pl;
+	T.tab[t] = k < 3 ? T.scG[at] : k < 6 ? T.scG[at + T.alt] : k < 9 ? T.scOld[at] : T.inv[at];
+}
+
+__global__ void k_half_table(const HalfTableParams T)
+{
+	halfTableEntry(T, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// After a half step of a half world's field F, per (component, plane) of
+// the planes it updated: the largest magnitude over the plane's slots
+// gives F's next exponent, which becomes the next parity's exponent as
+// read and as computed, its scale and the inverse scale F's next step
+// stores with; the slots F's next step fills are zeroed (one warp per
+// (component, plane)).  The threads after those make the other field's
+// scale table from F's scales as read now.
+struct HalfNextParams {
+	const unsigned *m;
+	unsigned *mZero;
+	signed char *ex, *exK;
+	float *sc, *inv;
+	int ni, p0, p1;                            // layout planes the half step updates
+	HalfTableParams other;
+};
+
+__global__ void k_half_next(const HalfNextParams P)
+{
+	const int t = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+	const int w = t / 32, lane = (int)(threadIdx.x & 31);
+	if (w >= 3 * P.ni) {
+		halfTableEntry(P.other, t - 3 * P.ni * 32);
+		return;
+	}
+	const int pl = w % P.ni;
+	P.mZero[(size_t)w * HALF_SLOTS + lane] = 0;
+	if (pl < P.p0 || pl > P.p1) return;
+	const unsigned m = __reduce_max_sync(0xffffffffu, P.m[(size_t)w * HALF_SLOTS + lane]);
+	if (lane == 0) {
+		const int e = halfExponent(m);
+		P.ex[w] = P.exK[w] = (signed char)e;
+		P.sc[w] = pow2f(e);
+		P.inv[w] = pow2f(-e);
+	}
+}
+
+static HalfTableParams halfTableFor(const alisgpu_world *w, int field)
+{
+	HalfTableParams T;
+	T.scG = halfScales(w, 1 - field), T.scOld = halfScales(w, field), T.inv = w->inv[field], T.tab = w->tab[field];
+	T.ni = w->L.ni, T.p0 = w->g.iMIN - w->L.i0, T.p1 = w->g.iMAX - w->L.i0, T.alt = field == 0 ? 1 : -1;
+	return T;
+}
+
+// the scale table of a field whose table is not current
+static int halfTable(alisgpu_world *w, int field)
+{
+	const HalfTableParams T = halfTableFor(w, field);
+	k_half_table<<<(T.ni * HALF_TAB + 255) / 256, 256, 0, gStream>>>(T);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	w->tabFresh[field] = true;
+	return ALISGPU_OK;
+}
+
+static int halfNext(alisgpu_world *w, int field)
+{
+	const int next = (int)(w->nHalf[field] & 1);
+	HalfNextParams P;
+	P.m = w->mx[field][next ^ 1], P.mZero = w->mx[field][next];
+	P.ex = w->ex[field][next], P.exK = w->exK[field][next], P.sc = w->sc[field][next], P.inv = w->inv[field];
+	P.ni = w->L.ni, P.p0 = w->g.iMIN - w->L.i0, P.p1 = w->g.iMAX - w->L.i0;
+	P.other = halfTableFor(w, 1 - field);
+	const int threads = 3 * P.ni * 32 + P.ni * HALF_TAB;
+	k_half_next<<<(threads + 255) / 256, 256, 0, gStream>>>(P);
+	alisgpu__count_launch();
+	ALIS_CUDA(cudaGetLastError());
+	w->tabFresh[1 - field] = true;
+	return ALISGPU_OK;
+}
+
 extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *s)
 {
 	bindWorld(w);
@@ -2472,7 +2898,18 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	// an auxiliary column's step is staged for its parent's entry, any
 	// other step joins the group of its field
 	const long long cells = (long long)(g.iMAX - g.iMIN + 1) * (g.jMAX - g.jMIN + 1) * (g.kMAX - g.kMIN + 1);
-	const bool smallPath = cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC &&
+	// a half world takes the grid launch, unrecorded, with its source
+	// patches inside the cells the step updates
+	if (w->half) {
+		if (batchRecording()) return alisgpu__fail(ALISGPU_ENOTSUP, "half_step: batched recording of a half world");
+		for (int q = 0; q < s->nsrc; q++) {
+			const alisgpu_source_patch &p = s->src[q];
+			if (p.m != 0 || p.comp < 0 || p.comp > 2 || p.i0 < g.iMIN || p.i1 > g.iMAX || p.j0 < g.jMIN || p.j1 > g.jMAX ||
+			    p.k0 < g.kMIN || p.k1 > g.kMAX)
+				return alisgpu__fail(ALISGPU_ENOTSUP, "half_step: a source patch of a half world outside the updated cells");
+		}
+	}
+	const bool smallPath = !w->half && cells <= (s->concurrent ? ALIS_SMALL_CELLS : ALIS_TINY_CELLS) && s->nsrc <= ALIS_MAXSRC &&
 	                       s->nghost <= ALIS_SMALL_GHOSTS;
 	const int rec = alisgpu__batch_enter(smallPath && s->concurrent && s->attach ? BATCH_NONE : (field == 0 ? BATCH_E : BATCH_H), w);
 	if (rec < 0) return alisgpu__fail(ALISGPU_ECUDA, "half_step: batch launch failed: %s", gErr);
@@ -2633,6 +3070,10 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		return ALISGPU_OK;
 	}
 	if (rec) return recordHalfStep(w, s, P);
+	if (w->half && !w->tabFresh[field]) {
+		int rc = halfTable(w, field);
+		if (rc) return rc;
+	}
 	const int ni = g.iMAX - g.iMIN + 1;
 	bool timed = false, fused = false;
 	const int v = tunedShape(w, field, &timed);
@@ -2651,6 +3092,12 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		P.matTab = field == 0 ? w->matTab : 0;
 		P.matWide = w->matWide;
 		for (int f = 0; f < 6; f++) for (int q = 0; q < 2; q++) P.psi[f][q] = w->psi[field][m][f][q];
+		if (w->half) {
+			// step n stores with the inverse scales made from the maxima of
+			// step n - 1 and accumulates its own
+			P.h.tab = w->tab[field];
+			P.h.mCur = w->mx[field][w->nHalf[field] & 1];
+		}
 		int slot = alisgpu__prof_start();
 		alisgpu_world *aux = s->ntfsf == 1 && m == 0 ? s->tfsf[0].aux : 0;
 		if (aux && aux->stagedValid[field]) {
@@ -2660,14 +3107,15 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 			FP.aux = *aux->staged[field];
 			aux->stagedValid[field] = false;
 			fused = true;
-			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream);
-			else launchHalfStep<-1>(v, grid, P, &FP, gStream);
-		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream);
-		else launchHalfStep<-1>(v, grid, P, 0, gStream);
+			if (field == 0) launchHalfStep<1>(v, grid, P, &FP, gStream, w->half);
+			else launchHalfStep<-1>(v, grid, P, &FP, gStream, w->half);
+		} else if (field == 0) launchHalfStep<1>(v, grid, P, 0, gStream, w->half);
+		else launchHalfStep<-1>(v, grid, P, 0, gStream, w->half);
 		alisgpu__prof_stop(slot, field == 0 ? ALISGPU_K_STEP_E : ALISGPU_K_STEP_H);
 		alisgpu__count_launch();
 	}
 	ALIS_CUDA(cudaGetLastError());
+	if (w->half) w->nHalf[field]++, w->tabFresh[field] = false;
 	if (timed) {
 		alisgpu_world::TyTuner &t = w->tune[field];
 		ALIS_CUDA(cudaEventRecord(t.b[t.seen], gStream));
@@ -2691,6 +3139,7 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		memcpy(SP.p, s->src, s->nsrc * sizeof(alisgpu_source_patch));
 		SP.vdev = 0;
 		SP.err = gErrWord;
+		SP.ex = w->half ? halfRead(w, field) : 0;
 		if (s->nvalues <= ALIS_MAXSRCV) {
 			memcpy(SP.v, s->values, s->nvalues * sizeof(float));
 		} else {
@@ -2714,7 +3163,12 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		w->hGhosts.assign(s->ghost, s->ghost + s->nghost);
 		int rc = runGhosts(w, 1, s->ghost, s->nghost);
 		if (rc) return rc;
+		if (w->half && (rc = halfNext(w, 1))) return rc;
 		w->hOps = gOps, w->hRecorded = true;
+	}
+	if (field == 0 && w->half) {
+		int rc = halfNext(w, 0);
+		if (rc) return rc;
 	}
 	// an auxiliary world stepped on the side stream waits for this record;
 	// none is needed when there is no box or its column ran in this launch
@@ -2736,9 +3190,18 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 // terms; H is averaged across the plane.  One block: its threads compute
 // the inner sums, one thread adds the outer loops in order.
 // ---------------------------------------------------------------------
+// an observer's read of element c of a field component: float storage, or
+// (ex: the component's exponents per plane of a half world) a half value
+// times its plane's power of two (plane = c / si, the layout's plane pitch)
+__device__ __forceinline__ float fieldAt(const float *p, const signed char *ex, long long si, long long c)
+{
+	return ex ? halfAt(p, c, pow2f(ex[c / si])) : p[c];
+}
+
 struct PlaneParams {
 	Layout L;
 	const float *E[3], *H[3];
+	const signed char *exE[3], *exH[3];          // half storage (else null)
 	int axis, pos;
 	int lo[2], hi[2];                          // in-plane axes u < v
 	const float *wE[2], *wH[2];                // spacings over [lo, hi], indexed by index
@@ -2769,6 +3232,8 @@ __global__ void __launch_bounds__(32 * PF_WARPS) k_plane_rows(const PlaneParams 
 	const int o = P.lo[oAx] + 1 + t, m0 = P.lo[nAx], m1 = P.hi[nAx];
 	const float *wN = P.wE[nAx];
 	const float *Ec = P.E[ec], *Hc = P.H[hc];
+	const signed char *xE = P.exE[ec], *xH = P.exH[hc];
+	const long long si = P.L.si;
 	const long long dn = a == 0 ? P.L.si : a == 1 ? P.L.sj : 1;  // H across the plane
 	auto cell = [&](int n) -> long long {
 		const int u = oAx == 0 ? o : n, v = oAx == 0 ? n : o;
@@ -2780,7 +3245,7 @@ __global__ void __launch_bounds__(32 * PF_WARPS) k_plane_rows(const PlaneParams 
 		const int n = e ? m1 : m0;
 		const long long c = cell(n);
 		const double hw = 0.5 * (double)wN[n];
-		const double term = __dmul_rn(hw * (double)Ec[c], (double)__fadd_rn(Hc[c], Hc[c + dn]));
+		const double term = __dmul_rn(hw * (double)fieldAt(Ec, xE, si, c), (double)__fadd_rn(fieldAt(Hc, xH, si, c), fieldAt(Hc, xH, si, c + dn)));
 		sum = __double2float_rn(l == 0 ? __dadd_rn((double)sum, term) : __dsub_rn((double)sum, term));
 	}
 	// interior terms in float, a chunk of the row at a time
@@ -2789,8 +3254,8 @@ __global__ void __launch_bounds__(32 * PF_WARPS) k_plane_rows(const PlaneParams 
 		__syncwarp();
 		for (int q = lane; q < cnt; q += 32) {
 			const long long c = cell(base + q);
-			se[warp][q] = __fmul_rn(wN[base + q], Ec[c]);
-			sh[warp][q] = __fadd_rn(Hc[c], Hc[c + dn]);
+			se[warp][q] = __fmul_rn(wN[base + q], fieldAt(Ec, xE, si, c));
+			sh[warp][q] = __fadd_rn(fieldAt(Hc, xH, si, c), fieldAt(Hc, xH, si, c + dn));
 		}
 		__syncwarp();
 		if (lane == 0)
@@ -2855,6 +3320,8 @@ extern "C" int alisgpu_plane_flux(alisgpu_world *w, int axis, int pos, const int
 	memset(&P, 0, sizeof P);
 	P.L = w->L;
 	for (int c = 0; c < 3; c++) P.E[c] = w->E[0][c], P.H[c] = w->H[0][c];
+	if (w->half)
+		for (int c = 0; c < 3; c++) P.exE[c] = halfRead(w, 0) + c * w->L.ni, P.exH[c] = halfRead(w, 1) + c * w->L.ni;
 	P.axis = axis, P.pos = pos;
 	const int axes[2] = { ua, va };
 	for (int q = 0; q < 2; q++) {
@@ -2889,6 +3356,7 @@ struct BoxGatherParams {
 	int nm;
 	int i0, j0, k0, ni, nj, nk;
 	float *out;                                // [E/H][m][comp][ni][nj][nk]
+	const signed char *ex[2];                  // half storage: the fields' exponents (else null)
 };
 
 __global__ void k_box_gather(const BoxGatherParams P)
@@ -2899,7 +3367,8 @@ __global__ void k_box_gather(const BoxGatherParams P)
 	const int r = t % cells, fc = t / cells;           // fc = (field * nm + m) * 3 + comp
 	const int comp = fc % 3, m = (fc / 3) % P.nm, f = fc / (3 * P.nm);
 	const int k = P.k0 + r % P.nk, j = P.j0 + (r / P.nk) % P.nj, i = P.i0 + r / (P.nk * P.nj);
-	P.out[t] = P.F[f][m][comp][P.L.at(i, j, k)];
+	if (P.ex[0]) P.out[t] = halfAt(P.F[f][m][comp], P.L.at(i, j, k), pow2f(P.ex[f][comp * P.L.ni + (i - P.L.i0)]));
+	else P.out[t] = P.F[f][m][comp][P.L.at(i, j, k)];
 }
 
 extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int j0, int j1, int k0, int k1, float *host)
@@ -2921,6 +3390,7 @@ extern "C" int alisgpu_field_box_download(alisgpu_world *w, int i0, int i1, int 
 	P.L = L;
 	P.nm = 1 + g.complexField;
 	for (int m = 0; m < P.nm; m++) for (int c = 0; c < 3; c++) P.F[0][m][c] = w->E[m][c], P.F[1][m][c] = w->H[m][c];
+	if (w->half) P.ex[0] = halfRead(w, 0), P.ex[1] = halfRead(w, 1);
 	P.i0 = i0, P.j0 = j0, P.k0 = k0, P.ni = 1 + i1 - i0, P.nj = 1 + j1 - j0, P.nk = 1 + k1 - k0;
 	const size_t n = (size_t)P.ni * P.nj * P.nk * 6 * P.nm;
 	if (n >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "field_box_download: box of %zu values too large", n);
@@ -2959,6 +3429,7 @@ struct alisgpu_slice_dft {
 struct SliceDftParams {
 	Layout L;
 	const float *F;                            // the sampled component (E or H, m)
+	const signed char *ex;                     // its exponents per plane (half storage; else null)
 	int kind;                                  // 0 raw, 1 E pair, 2 H quad; -1: zero (imaginary part of a real field)
 	int d1, d2;                                // offsets of the second (and third) sample
 	float base;                                // 1, 0.5, 0.25
@@ -2982,9 +3453,11 @@ __global__ void k_slice_dft(const SliceDftParams P)
 		if (P.sym[1] && j < 0) j = -j, p *= P.par[1];
 		if (P.sym[2] && k < 0) k = -k, p *= P.par[2];
 		const long long c = P.L.at(i, j, k);
-		if (P.kind == 0) v = p * P.F[c];
-		else if (P.kind == 1) v = p * (P.F[c] + P.F[c + P.d1]);
-		else v = p * (P.F[c] + P.F[c + P.d1] + P.F[c + P.d2] + P.F[c + P.d1 + P.d2]);
+		const long long si = P.L.si;
+		if (P.kind == 0) v = p * fieldAt(P.F, P.ex, si, c);
+		else if (P.kind == 1) v = p * (fieldAt(P.F, P.ex, si, c) + fieldAt(P.F, P.ex, si, c + P.d1));
+		else v = p * (fieldAt(P.F, P.ex, si, c) + fieldAt(P.F, P.ex, si, c + P.d1) + fieldAt(P.F, P.ex, si, c + P.d2) +
+		              fieldAt(P.F, P.ex, si, c + P.d1 + P.d2));
 	}
 	P.acc[t] += v * P.re;
 	P.acc[t + cells] += v * P.im;
@@ -3040,6 +3513,7 @@ extern "C" int alisgpu_slice_dft_add(alisgpu_slice_dft *d, int field, int m, int
 		P.kind = -1;
 	} else {
 		P.F = field == 0 ? w->E[m][comp] : w->H[m][comp];
+		P.ex = w->half ? halfRead(w, field) + comp * L.ni : 0;
 		const long long st[3] = { L.si, L.sj, 1 };
 		if (!avg) P.kind = 0, P.base = 1.0f;
 		else if (field == 0) P.kind = 1, P.base = 0.5f, P.d1 = (int)st[comp];
@@ -3100,6 +3574,7 @@ extern "C" int alisgpu_slice_dft_destroy(alisgpu_slice_dft *d)
 struct AbsorbParams {
 	Layout L;
 	const float *E[3], *C[3];
+	const signed char *exE[3];                // half storage (else null)
 	DevObj o;
 	int iMIN, iMAX, jMIN, jMAX, kMIN, kMAX;
 	int i0, i1, j0, j1, k0, k1;               // box clipped to the world
@@ -3114,7 +3589,7 @@ __device__ __forceinline__ float objCurrent(const AbsorbParams &P, int a, int i,
 	const DevObj &o = P.o;
 	const int b = (i - o.i0) * (int)o.si + (j - o.j0) * (int)o.sj + (k - o.k0);
 	float f = 0;
-	if (o.a[a]) f = __fadd_rn(f, __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, o.fill[a][b]), P.E[a][c]), __fadd_rn(1.0f, __fdiv_rn(1.0f, o.a[a]))));
+	if (o.a[a]) f = __fadd_rn(f, __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, o.fill[a][b]), fieldAt(P.E[a], P.exE[a], P.L.si, c)), __fadd_rn(1.0f, __fdiv_rn(1.0f, o.a[a]))));
 	for (int p = 0; p < o.NK; p++) f = __fadd_rn(f, o.J[0][p][a][b]);
 	return __fdiv_rn(f, P.C[a][c]);
 }
@@ -3128,9 +3603,9 @@ __global__ void k_absorb_columns(const AbsorbParams P)
 	float xs = 0, ys = 0, zs = 0;
 	for (int k = P.k0; k <= P.k1; k++) {
 		const long long c = P.L.at(i, j, k);
-		if (P.C[0][c] != 0) xs = __fadd_rn(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
-		if (P.C[1][c] != 0) ys = __fadd_rn(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
-		if (P.C[2][c] != 0) zs = __fadd_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], P.E[2][c]), objCurrent(P, 2, i, j, k, c)));
+		if (P.C[0][c] != 0) xs = __fadd_rn(xs, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[0], P.exE[0], P.L.si, c)), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = __fadd_rn(ys, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[1], P.exE[1], P.L.si, c)), objCurrent(P, 1, i, j, k, c)));
+		if (P.C[2][c] != 0) zs = __fadd_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], fieldAt(P.E[2], P.exE[2], P.L.si, c)), objCurrent(P, 2, i, j, k, c)));
 	}
 	// half weights where the box meets the world's k edges; `* 0.5` is a
 	// double product, the difference rounds back to float
@@ -3138,15 +3613,15 @@ __global__ void k_absorb_columns(const AbsorbParams P)
 	if (P.k0 == P.kMIN) {
 		const int k = P.kMIN;
 		const long long c = P.L.at(i, j, k);
-		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
-		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
-		if (P.C[2][c] != 0) zs = __fsub_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], P.E[2][c]), objCurrent(P, 2, i, j, k, c)));
+		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[0], P.exE[0], P.L.si, c)), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[1], P.exE[1], P.L.si, c)), objCurrent(P, 1, i, j, k, c)));
+		if (P.C[2][c] != 0) zs = __fsub_rn(zs, __fmul_rn(__fmul_rn(P.dzH[k], fieldAt(P.E[2], P.exE[2], P.L.si, c)), objCurrent(P, 2, i, j, k, c)));
 	}
 	if (P.k1 == P.kMAX) {
 		const int k = P.kMAX;
 		const long long c = P.L.at(i, j, k);
-		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], P.E[0][c]), objCurrent(P, 0, i, j, k, c)));
-		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], P.E[1][c]), objCurrent(P, 1, i, j, k, c)));
+		if (P.C[0][c] != 0) xs = halfOff(xs, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[0], P.exE[0], P.L.si, c)), objCurrent(P, 0, i, j, k, c)));
+		if (P.C[1][c] != 0) ys = halfOff(ys, __fmul_rn(__fmul_rn(P.dzE[k], fieldAt(P.E[1], P.exE[1], P.L.si, c)), objCurrent(P, 1, i, j, k, c)));
 	}
 	P.cols[3 * t] = xs, P.cols[3 * t + 1] = ys, P.cols[3 * t + 2] = zs;
 }
@@ -3205,6 +3680,8 @@ extern "C" int alisgpu_object_absorption(alisgpu_world *w, int n, float *out)
 	memset(&P, 0, sizeof P);
 	P.L = w->L;
 	for (int c = 0; c < 3; c++) P.E[c] = w->E[0][c], P.C[c] = w->C[c];
+	if (w->half)
+		for (int c = 0; c < 3; c++) P.exE[c] = halfRead(w, 0) + c * w->L.ni;
 	P.o = w->objs[n];
 	P.iMIN = g.iMIN, P.iMAX = g.iMAX, P.jMIN = g.jMIN, P.jMAX = g.jMAX, P.kMIN = g.kMIN, P.kMAX = g.kMAX;
 	P.i0 = std::max(g.iMIN, P.o.i0), P.i1 = std::min(g.iMAX, P.o.i1);
@@ -3339,6 +3816,7 @@ extern "C" int alisgpu_nonlinear_twm(alisgpu_world *ws, const alisgpu_world *wp1
 	if (!ws || !wp1 || !wp2 || !d || n < 0 || n >= (int)ws->objs.size() || m < 0 || m > ws->g.complexField ||
 	    m > wp1->g.complexField || m > wp2->g.complexField)
 		return alisgpu__fail(ALISGPU_EINVAL, "nonlinear_twm: bad argument");
+	if (ws->half || wp1->half || wp2->half) return alisgpu__fail(ALISGPU_ENOTSUP, "nonlinear_twm: a world stores half values");
 	// the pumps' fields are read on the signal world's stream
 	int rc = crossGroup(ws, wp1, true);
 	if (!rc) rc = crossGroup(ws, wp2, true);
@@ -3418,4 +3896,11 @@ extern "C" int alisgpu__world_fields(alisgpu_world *w, int m, const float **E, c
 	for (int c = 0; c < 3; c++) E[c] = w->E[m][c], H[c] = w->H[m][c];
 	*L = w->L;
 	return ALISGPU_OK;
+}
+
+// the exponents E and H are read with now (null for float storage)
+extern "C" void alisgpu__world_half(const alisgpu_world *w, const signed char **exE, const signed char **exH)
+{
+	*exE = w && w->half ? halfRead(w, 0) : 0;
+	*exH = w && w->half ? halfRead(w, 1) : 0;
 }

@@ -26,7 +26,11 @@ cpu_baseline  the oracle restatement of the reference loops on the host
           cores (OpenMP), bounded sample of the same world
 --impl reference  times that CPU implementation alone as the reference arm.
 forms     the batched unit-cell sweep (64 cells) and the served request
-          stream, each against its per-request path (--forms 0 skips)
+          stream, each against its per-request path, and the same workload
+          with half field storage (--forms 0 skips them)
+--storage half  E and H stored as IEEE half values with a power-of-two
+          exponent per component and x plane, float arithmetic; the
+          roofline then counts 2-byte field values (48 B per cell)
 --sweep   the batched metasurface unit-cell sweep instead: N periodic unit
           cells (32-96 x 32-96 x 64-256 cells, Lorentz pillar, TFSF pulse,
           32-wavelength transmission plane, 3000 steps each) stepped
@@ -52,6 +56,8 @@ sys.path.insert(0, ROOT)
 
 HALF = 230          # domain half size in nm: 256^3 cells with the CPML
 NFREQ = 64
+STORAGE = {"float": "float E and H",
+           "half": "E and H as IEEE half values times a power of two per component and x plane, float arithmetic"}
 TUNE_STEPS = 16     # the engine times its launch shapes over a world's first 10 half steps of each field
 def workload(cells):
     n = round(cells ** (1 / 3))
@@ -235,6 +241,9 @@ def engine_arm(args, rank, world, local):
     os.environ.setdefault("ALISGPU_DEVICE", str(local))
     # the workload's phasers accumulate with compensated (Kahan) sums
     os.environ.setdefault("ALISGPU_PHASER_KAHAN", "1")
+    half_storage = args.storage == "half"
+    if half_storage:
+        os.environ["ALIS_FIELD_STORAGE"] = "half"
     so = build_bench_lib()
     import alis_gb300
     eng = alis_gb300.library()
@@ -242,6 +251,7 @@ def engine_arm(args, rank, world, local):
     lib.c2_build.restype = ctypes.c_long
     lib.c2_result.restype = ctypes.c_double
     lib.c2_step_bytes.restype = ctypes.c_double
+    lib.c2_step_bytes_half.restype = ctypes.c_double
     lib.c2_step_h2d_bytes.restype = ctypes.c_double
     lib.c2_result_d2h_bytes.restype = ctypes.c_double
     eng.alisgpu_stream.restype = ctypes.c_void_p
@@ -303,14 +313,14 @@ def engine_arm(args, rank, world, local):
     clocks = clk.summary()
     if rank != 0:
         return
-    step_bytes = lib.c2_step_bytes()
+    step_bytes = lib.c2_step_bytes_half() if half_storage else lib.c2_step_bytes()
     tE, nE = kinds["step_E"]
     tH, nH = kinds["step_H"]
     pair_ms = tE / max(nE, 1) + tH / max(nH, 1)
     achieved = step_bytes / (pair_ms / 1e3) / 1e9
     pk, pk_kind = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
-    traffic = traffic_per_launch_pair()
+    traffic = None if half_storage else traffic_per_launch_pair()
     total_ms = sum(t for t, _ in kinds.values())
     cpu_baseline = None
     if args.cpu_steps > 0:
@@ -326,6 +336,7 @@ def engine_arm(args, rank, world, local):
         "ms_per_step": dev_s * 1e3 / (K * R), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload(cells), "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
+                   "storage": STORAGE[args.storage],
                    "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
                    "phaser": "64 frequencies, %s, time-blocked ring of %s steps" % (
                        "Kahan-compensated" if os.environ.get("ALISGPU_PHASER_KAHAN") == "1" else "plain float sums",
@@ -351,9 +362,29 @@ def engine_arm(args, rank, world, local):
         "result_flux": flux,
     }
     if args.forms:
-        # the batched and served forms, each against its per-request path
-        line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form()}
+        # the batched and served forms, each against its per-request path,
+        # and the same workload with half field storage
+        line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form(),
+                         "half_storage": half_form(args, line)}
     print(json.dumps(line), flush=True)
+
+
+def half_form(args, line):
+    """The workload with E and H stored as half values (--storage half, its
+    own process): throughput, the roofline of its half steps over its own
+    algorithmic bytes, and its speed against the float line."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--storage", "half", "--steps", str(args.steps),
+           "--warmup", str(args.warmup), "--cpu-steps", "0", "--forms", "0", "--half", str(args.half),
+           "--timed-steps", str(args.timed_steps)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
+    if r.returncode:
+        return {"error": (r.stdout + r.stderr)[-500:]}
+    h = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    return {"storage": STORAGE["half"], "value": h["value"], "unit": h["unit"], "ms_per_step": h["ms_per_step"],
+            "e2e": h["e2e"]["value"], "speedup": h["value"] / line["value"],
+            "roofline": {k: h["roofline"][k] for k in ("achieved", "peak", "frac", "frac_nominal",
+                                                        "algorithmic_bytes_per_step", "launch_pair_ms")},
+            "clocks": h["clocks"], "result_flux": h["result_flux"]}
 
 
 def serve_exe():
@@ -432,6 +463,9 @@ def main():
     ap.add_argument("--sweep", type=int, default=0, metavar="N",
                     help="run the batched unit-cell sweep of N cells instead (512: the full sweep)")
     ap.add_argument("--sweep-steps", type=int, default=0, help="steps per unit cell (default 3000)")
+    ap.add_argument("--storage", default="float", choices=sorted(STORAGE),
+                    help="field storage of the world: float, or half values with a power-of-two exponent per "
+                         "component and x plane (alisgpu_world_set_storage)")
     ap.add_argument("--forms", type=int, default=64, metavar="N",
                     help="after the main line's timing, the batched sweep of N unit cells and the served stream, "
                          "each against its per-request path, as the line's 'forms' (0: skip)")

@@ -34,7 +34,8 @@ enum {
 	ALISGPU_ENOMEM = -2,    /* device allocation failed */
 	ALISGPU_ECUDA = -3,     /* CUDA runtime error */
 	ALISGPU_ENODEV = -4,    /* no usable GPU */
-	ALISGPU_ERANGE = -5     /* request beyond a fixed capacity */
+	ALISGPU_ERANGE = -5,    /* request beyond a fixed capacity */
+	ALISGPU_ENOTSUP = -6    /* not available for the world's storage form */
 };
 
 const char *alisgpu_last_error(void);
@@ -89,6 +90,26 @@ int alisgpu_world_destroy(alisgpu_world *w);
 int alisgpu_world_reset(alisgpu_world *w);
 /* Device bytes held by the world (fields, psi, maps, currents). */
 size_t alisgpu_world_bytes(const alisgpu_world *w);
+/* Storage form of the E and H components (no counterpart in the
+ * reference, which stores float).  ALISGPU_STORAGE_HALF holds each
+ * component as IEEE half values times 2^e, one exponent e per component
+ * and x plane: half the field bytes, with the update arithmetic in float.
+ * A half step takes e from the largest magnitude M the plane's cells of
+ * the component reached in the field's previous half step, before
+ * rounding (e = x - 11 for M = f 2^x, f in [0.5, 1); -11 while M = 0;
+ * clamped to [-100, 100]), rounds each updated cell to nearest even
+ * (saturating at +-65504 2^e), and the source patches then add to the
+ * rounded values and round again.  Ghost copies move values unchanged.
+ * ADE currents, CPML psi and TFSF auxiliary worlds stay float.  Only
+ * before the first half step and for real fields (else ALISGPU_EINVAL /
+ * ALISGPU_ENOTSUP).  The observers (field downloads, plane fluxes, slice
+ * DFTs, object absorption, the phaser gather) read the half values.  A
+ * half world refuses with ALISGPU_ENOTSUP: field uploads, batched
+ * recording, ghost lists other than copies, negations and zeros that move
+ * whole planes, source patches outside the updated cells, and nonlinear
+ * coupling. */
+enum { ALISGPU_STORAGE_FLOAT = 0, ALISGPU_STORAGE_HALF = 1 };
+int alisgpu_world_set_storage(alisgpu_world *w, int storage);
 /* Stream groups (no counterpart in the reference, which runs one world at
  * a time on the host cores).  Every world starts in the default group,
  * whose main stream alisgpu_stream() returns.  own_streams moves w to a

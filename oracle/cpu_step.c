@@ -18,6 +18,8 @@
  *
  * Never linked into the product library.
  */
+#include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include "engine.h"
@@ -259,40 +261,137 @@ static void tfsfH(world W, tfsf S)
 
 #define GHOST(W, F, c, ...) (copyBoundary)(W->F[0].c, W->complexField ? W->F[1].c : 0, __VA_ARGS__)
 
-/* FP16 field storage, a study of the storage form (environment
- * ALIS_ORACLE_FP16_STORAGE=1; not built in the engine): after each half
- * step of a user world, every component of the updated field is stored
- * as IEEE half with one power-of-two scale per x plane (the plane's
- * largest magnitude maps into [0.5, 1)) and read back.  TFSF auxiliary
- * columns, ADE currents and CPML psi stay float. */
+/* FP16 field storage (environment ALIS_ORACLE_FP16_STORAGE=1; the
+ * engine's half storage, alisgpu_world_set_storage): the E and H
+ * components of a world stepped by the user (not its TFSF auxiliary
+ * columns) are held as IEEE half values times 2^e, one exponent e per
+ * component and x plane.  A half step takes e from the largest magnitude
+ * M the plane's cells of that component reached in the previous half step
+ * of the field, before rounding: e = x - 11 for M = f 2^x, f in [0.5, 1)
+ * (M 2^-e in [2^10, 2^11): 32 times headroom below the half maximum
+ * 65504), e = -11 while M = 0, e = 100 for M infinite or NaN, clamped to
+ * [-100, 100].  The step rounds every cell it updates (after the curl,
+ * currents, CPML and TFSF corrections) to v = half(v 2^-e) 2^e, with
+ * round-to-nearest-even and values beyond the half range saturated at
+ * +-65504 2^e; the source patches then add to the rounded values and
+ * their cells are rounded again with the same e.  Ghost copies move the
+ * rounded values unchanged.  ADE currents, CPML psi and the auxiliary
+ * columns stay float.  M is taken over the float bits of |v| as unsigned
+ * integers (the order of magnitudes, NaN above infinity). */
+#define HALF_E0 (-11)
+#define HALF_EMIN (-100)
+#define HALF_EMAX 100
 static int fp16Storage = -1, stepDepth;
 
-static void storeHalf(world W, vfield F)
+typedef struct HalfState {
+	world W;
+	int ni;
+	unsigned *M[2][2];                     /* [E/H][previous/current] 3 x ni */
+	struct HalfState *next;
+} HalfState;
+static HalfState *halfStates;
+
+static int halfExponent(unsigned mbits)
 {
-	float ***c[3] = { F.x, F.y, F.z };
-	for (int q = 0; q < 3; q++) {
-		_Pragma("omp parallel for")
-		for (int i = W->iMIN; i <= W->iMAX; i++) {
-			double m = 0;
-			for (int j = W->jMIN; j <= W->jMAX; j++) for (int k = W->kMIN; k <= W->kMAX; k++)
-				if (fabs(c[q][i][j][k]) > m) m = fabs(c[q][i][j][k]);
-			if (m == 0) continue;
-			int e;
-			frexp(m, &e);
-			for (int j = W->jMIN; j <= W->jMAX; j++) for (int k = W->kMIN; k <= W->kMAX; k++)
-				c[q][i][j][k] = ldexp((double)(_Float16)ldexp(c[q][i][j][k], -e), e);
-		}
-	}
+	if (mbits == 0) return HALF_E0;
+	if (mbits >= 0x7f800000u) return HALF_EMAX;
+	float m;
+	memcpy(&m, &mbits, 4);
+	int x;
+	frexpf(m, &x);
+	int e = x - 11;
+	return e < HALF_EMIN ? HALF_EMIN : e > HALF_EMAX ? HALF_EMAX : e;
 }
 
-static void storeFields(world W, vfield *F)
+static float roundHalf(float v, int e)
+{
+	float x = v * ldexpf(1.0f, -e);
+	if (x > 65504.0f) x = 65504.0f;
+	else if (x < -65504.0f) x = -65504.0f;
+	return (float)(_Float16)x * ldexpf(1.0f, e);
+}
+
+static HalfState *halfState(world W)
+{
+	HalfState *h = halfStates;
+	while (h && h->W != W) h = h->next;
+	if (!h) {
+		if (W->complexField) { fprintf(stderr, "oracle: FP16 storage needs real fields\n"); exit(1); }
+		h = calloc(1, sizeof *h);
+		h->W = W, h->ni = W->iMAX - W->iMIN + 1;
+		for (int f = 0; f < 2; f++) for (int q = 0; q < 2; q++) h->M[f][q] = calloc(3 * (size_t)h->ni, sizeof(unsigned));
+		h->next = halfStates, halfStates = h;
+	}
+	return h;
+}
+
+/* a rebooted world starts again from M = 0 */
+static void halfForget(world W)
+{
+	for (HalfState *h = halfStates; h; h = h->next)
+		if (h->W == W)
+			for (int f = 0; f < 2; f++) for (int q = 0; q < 2; q++) memset(h->M[f][q], 0, 3 * (size_t)h->ni * sizeof(unsigned));
+}
+
+static int halfOn(void)
 {
 	if (fp16Storage < 0) {
 		const char *e = getenv("ALIS_ORACLE_FP16_STORAGE");
 		fp16Storage = e && e[0] == '1';
+#ifdef ALIS_ORACLE_FP64_H
+		fp16Storage = 0;                   /* a float storage form: not in the FP64 build */
+#endif
 	}
-	if (fp16Storage && stepDepth == 1)
-		for (int m = 0; m <= W->complexField; m++) storeHalf(W, F[m]);
+	return fp16Storage && stepDepth == 1;
+}
+
+/* the half step's rounding of the cells it updated (field f: 0 E, 1 H) */
+static void storeStep(world W, vfield F, int f)
+{
+	if (!halfOn()) return;
+	HalfState *h = halfState(W);
+	float ***c[3] = { F.x, F.y, F.z };
+	unsigned *prev = h->M[f][0], *cur = h->M[f][1];
+	for (int q = 0; q < 3; q++) {
+		_Pragma("omp parallel for")
+		for (int i = W->iMIN; i <= W->iMAX; i++) {
+			int e = halfExponent(prev[q * h->ni + (i - W->iMIN)]);
+			unsigned m = 0;
+			for (int j = W->jMIN; j <= W->jMAX; j++) for (int k = W->kMIN; k <= W->kMAX; k++) {
+				float a = fabsf(c[q][i][j][k]);
+				unsigned bits;
+				memcpy(&bits, &a, 4);
+				if (bits > m) m = bits;
+				c[q][i][j][k] = roundHalf(c[q][i][j][k], e);
+			}
+			cur[q * h->ni + (i - W->iMIN)] = m;
+		}
+	}
+	h->M[f][0] = cur, h->M[f][1] = prev;
+}
+
+/* the source patches' cells, rounded again with the exponents of the step
+ * (storeStep has made them the previous ones) */
+static void storeSources(world W, vfield F, int f, source S)
+{
+	if (!halfOn()) return;
+	HalfState *h = halfState(W);
+	const unsigned *used = h->M[f][1];
+	float ***c[3] = { F.x, F.y, F.z };
+	for (; S; S = S->S) {
+		if (!(W->n < S->N)) continue;
+		int q = S->F == F.x ? 0 : S->F == F.y ? 1 : S->F == F.z ? 2 : -1;
+		if (q < 0 || S->iMin < W->iMIN || S->iMax > W->iMAX || S->jMin < W->jMIN || S->jMax > W->jMAX ||
+		    S->kMin < W->kMIN || S->kMax > W->kMAX) {
+			fprintf(stderr, "oracle: FP16 storage needs source patches inside the updated cells\n");
+			exit(1);
+		}
+		for (int i = S->iMin; i <= S->iMax; i++) {
+			int e = halfExponent(used[q * h->ni + (i - W->iMIN)]);
+			for (int j = S->jMin; j <= S->jMax; j++) for (int k = S->kMin; k <= S->kMax; k++)
+				c[q][i][j][k] = roundHalf(c[q][i][j][k], e);
+		}
+	}
 }
 
 /* reference src/update.c:275-299 */
@@ -304,8 +403,8 @@ void updateE(world W)
 		currentStep(W, W->H[m], W->CH);
 	}
 	if (W->S) tfsfE(W, W->S);
-	if (W->SE) sourceStep(W, W->SE, W->H->t);
-	storeFields(W, W->E);
+	storeStep(W, W->E[0], 0);
+	if (W->SE) sourceStep(W, W->SE, W->H->t), storeSources(W, W->E[0], 0, W->SE);
 	int iAlt = (W->xMinSur==PBC || W->xMinSur==BBC ? W->iNUM-1 : 1);
 	int jAlt = (W->yMinSur==PBC || W->yMinSur==BBC ? W->jNUM-1 : 1);
 	int kAlt = (W->zMinSur==PBC || W->zMinSur==BBC ? W->kNUM-1 : 1);
@@ -330,8 +429,8 @@ void updateH(world W)
 		currentStep(W, W->E[m], W->CE);
 	}
 	if (W->S) tfsfH(W, W->S);
-	if (W->SH) sourceStep(W, W->SH, W->E->t);
-	storeFields(W, W->H);
+	storeStep(W, W->H[0], 1);
+	if (W->SH) sourceStep(W, W->SH, W->E->t), storeSources(W, W->H[0], 1, W->SH);
 	int iAlt = (W->xMinSur==PBC || W->xMinSur==BBC ? W->iNUM-1 : 1);
 	int jAlt = (W->yMinSur==PBC || W->yMinSur==BBC ? W->jNUM-1 : 1);
 	int kAlt = (W->zMinSur==PBC || W->zMinSur==BBC ? W->kNUM-1 : 1);
@@ -654,10 +753,20 @@ void alis_be_farfield_sums(phaser P, int nA, const tfield *T, const float *kx, c
 /* --- backend hooks: the oracle steps the host arrays themselves --- */
 
 void alis_be_world_created(world W) { (void)W; }
-void alis_be_world_deleted(world W) { (void)W; }
+void alis_be_world_deleted(world W)
+{
+	for (HalfState **pp = &halfStates; *pp; pp = &(*pp)->next)
+		if ((*pp)->W == W) {
+			HalfState *h = *pp;
+			*pp = h->next;
+			for (int f = 0; f < 2; f++) for (int q = 0; q < 2; q++) free(h->M[f][q]);
+			free(h);
+			break;
+		}
+}
 void alis_be_objects_changed(world W) { (void)W; }
 void alis_be_sources_changed(world W) { (void)W; }
-void alis_be_world_reset(world W) { (void)W; }
+void alis_be_world_reset(world W) { halfForget(W); }
 void alis_be_sync_world(world W) { (void)W; }
 void alis_be_phaser_created(phaser P) { (void)P; }
 void alis_be_phaser_deleted(phaser P) { (void)P; }

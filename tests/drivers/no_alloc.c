@@ -14,7 +14,8 @@
  * points instead, each without a launch: an injected allocation failure
  * (ALISGPU_ENOMEM), a frequency outside the phaser's and test fields
  * shorter than the phaser box (ALISGPU_EINVAL); and that a call after
- * them still gives the same sums.
+ * them still gives the same sums.  Then the storage form's refusals:
+ * after a write, a bad kind, complex fields, an upload to a half world.
  */
 #include <alisgpu.h>
 #include <math.h>
@@ -108,10 +109,37 @@ int main(int argc, char **argv)
 		printf("enomem %d einval_f %d %d einval_nk %d %d launched %d same_after %d\n",
 		       oom == ALISGPU_ENOMEM, badF == ALISGPU_EINVAL, badFs == ALISGPU_EINVAL,
 		       shortT == ALISGPU_EINVAL, shortTs == ALISGPU_EINVAL, launched, same);
+		/* the storage form: only before a world's first step or write,
+		 * real fields only; a half world refuses uploads, and switching
+		 * back and forth before a step is allowed */
+		int written = alisgpu_world_set_storage(w, ALISGPU_STORAGE_HALF);
+		int badKind = alisgpu_world_set_storage(w, 7);
+		alisgpu_geometry cg = geo;
+		cg.complexField = 1;
+		alisgpu_world *wc, *wh;
+		CHECK(alisgpu_world_create(&cg, &wc));
+		int cplx = alisgpu_world_set_storage(wc, ALISGPU_STORAGE_HALF);
+		CHECK(alisgpu_world_create(&geo, &wh));
+		size_t b0 = alisgpu_world_bytes(wh);
+		int toHalf = alisgpu_world_set_storage(wh, ALISGPU_STORAGE_HALF);
+		size_t b1 = alisgpu_world_bytes(wh);
+		int upload = alisgpu_field_upload(wh, 0, 0, 1, host);
+		int down = alisgpu_field_download(wh, 1, 0, 2, host);
+		int zero = 1;
+		for (size_t q = 0; q < n3; q++) zero &= host[q] == 0.0f;
+		int back = alisgpu_world_set_storage(wh, ALISGPU_STORAGE_FLOAT);
+		size_t b2 = alisgpu_world_bytes(wh);
+		int again = alisgpu_world_set_storage(wh, ALISGPU_STORAGE_HALF);
+		int storageOk = written == ALISGPU_EINVAL && badKind == ALISGPU_EINVAL && cplx == ALISGPU_ENOTSUP && toHalf == 0 &&
+		                b1 < b0 && upload == ALISGPU_ENOTSUP && down == 0 && zero && back == 0 && b2 == b0 && again == 0;
+		printf("storage %d (written %d kind %d complex %d half %d bytes %zu -> %zu -> %zu upload %d download %d zero %d back %d again %d)\n",
+		       storageOk, written, badKind, cplx, toHalf, b0, b1, b2, upload, down, zero, back, again);
+		alisgpu_world_destroy(wc);
+		alisgpu_world_destroy(wh);
 		alisgpu_phaser_destroy(p);
 		alisgpu_world_destroy(w);
 		return oom == ALISGPU_ENOMEM && badF == ALISGPU_EINVAL && badFs == ALISGPU_EINVAL && shortT == ALISGPU_EINVAL &&
-		       shortTs == ALISGPU_EINVAL && !launched && same ? 0 : 1;
+		       shortTs == ALISGPU_EINVAL && !launched && same && storageOk ? 0 : 1;
 	}
 
 	double ref[2][NA * 12], got[2][NA * 12];

@@ -253,16 +253,31 @@ def test_precise_conduction_acts_where_an_object_conducts(builds):
     assert not scenes.compare_exact(ref, pre)
 
 
-def test_fp16_storage_study(builds):
-    """FP16 field storage with one power-of-two scale per x plane
-    (ALIS_ORACLE_FP16_STORAGE=1; emulated in the oracle, not built in the
-    engine) against the FP64 run: the half's 11-bit mantissa, rounded at
-    every store, puts the sweep's unit cell 7.8e-4 from FP64 in band and
-    its fields 2.7e-2, against 1.8e-5 and 3.8e-6 for FP32 storage -- above
-    the 1e-4 spectral bound, which is why the engine stores FP32."""
-    b = scenes.run("oracle64", "unitcell", 1, 1500)
-    e32 = errors(scenes.run("oracle", "unitcell", 1, 1500), b)
-    e16 = errors(scenes.run("oracle", "unitcell", 1, 1500, env={"ALIS_ORACLE_FP16_STORAGE": "1"}), b)
-    print("unit cell, flux in band: FP32 storage %.2e, FP16 storage %.2e" % (e32["flux"][0], e16["flux"][0]))
-    assert e32["flux"][0] <= BOUND["flux"] < e16["flux"][0] < 1e-2
-    assert 1e-3 < e16["field"][0] < 1e-1
+# FP16 storage cases: the error each scene's half run (the oracle's
+# restatement; the engine's half storage is byte-identical to it,
+# test_gpu_half) carries against FP64, beside the float run's
+HALF_CASES = [("c1", 1, 800), ("c2", 1, 400), ("unitcell", 1, 1500), ("dipole", 1, 400), ("sym", 1, 400),
+              ("spheres", 1, 300)]
+
+
+@pytest.mark.parametrize("case", HALF_CASES, ids=["%s-%d" % (c[0], c[2]) for c in HALF_CASES])
+def test_fp16_storage_error_against_fp64(builds, case):
+    """FP16 field storage (E and H as half values times a power of two per
+    component and x plane, float arithmetic) against the FP64 run, beside
+    float storage.  Rounding every stored value to 11 significant bits
+    puts fields 1.6e-3 (spheres) to 7e-2 (sym) from FP64 and in-band
+    fluxes 3.4e-5 (c2) to 3.3e-3 (unit cell), against 1e-6 to 2.5e-5 for
+    float storage: above the 1e-4 spectral bound except on c2, so the form
+    is opt-in, for memory (2 B per field value) and bandwidth, with its
+    error stated here."""
+    sc, scale, steps = case
+    b = scenes.run("oracle64", sc, scale, steps)
+    e32 = errors(scenes.run("oracle", sc, scale, steps), b)
+    e16 = errors(scenes.run("oracle", sc, scale, steps, env={"ALIS_ORACLE_FP16_STORAGE": "1"}), b)
+    print("%s-%d error vs FP64, float storage / half storage: %s" % (sc, steps, ", ".join(
+        "%s %.2e / %.2e" % (k, e32[k][0], e16[k][0]) for k in ("field", "ade", "face", "far", "flux") if k in e16)))
+    assert e16["field"][0] < 1e-1
+    if "flux" in e16:
+        assert e32["flux"][0] <= BOUND["flux"] and e16["flux"][0] < 2e-2
+    if "far" in e16:
+        assert e16["far"][0] < 2e-2
