@@ -59,6 +59,14 @@ NFREQ = 64
 STORAGE = {"float": "float E and H",
            "half": "E and H as IEEE half values times a power of two per component and x plane, float arithmetic"}
 TUNE_STEPS = 16     # the engine times its launch shapes over a world's first 10 half steps of each field
+C5 = (1024, 1024, 512, 200, 128)   # cells per axis with the CPML, balls, phaser frequencies
+
+
+def workload_c5(cells):
+    return ("large domain %dx%dx%d (%d seeded Drude-Lorentz balls of radius 20-80 cells in an n=1.5 host, CPML 16, "
+            "2 pulsed dipoles, %d-f transmission plane)" % C5)
+
+
 def workload(cells):
     n = round(cells ** (1 / 3))
     return "dispersive scatterer %d^3 (gold Drude+2CP, TFSF, CPML 12, 64-f box phasers)" % n
@@ -249,6 +257,7 @@ def engine_arm(args, rank, world, local):
     eng = alis_gb300.library()
     lib = ctypes.CDLL(so)
     lib.c2_build.restype = ctypes.c_long
+    lib.c5_build.restype = ctypes.c_long
     lib.c2_result.restype = ctypes.c_double
     lib.c2_step_bytes.restype = ctypes.c_double
     lib.c2_step_bytes_half.restype = ctypes.c_double
@@ -258,7 +267,8 @@ def engine_arm(args, rank, world, local):
     eng.alisgpu_launch_count.restype = ctypes.c_ulonglong
     cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
 
-    cells = lib.c2_build(args.half, NFREQ)
+    c5 = args.workload == "c5"
+    cells = lib.c5_build(*C5) if c5 else lib.c2_build(args.half, NFREQ)
     # the one-world calls, or the batched form (--batched) of the same steps
     steps_fn = lib.c2_steps_batched if args.batched else lib.c2_steps
     stream = ctypes.c_void_p(eng.alisgpu_stream())
@@ -323,7 +333,7 @@ def engine_arm(args, rank, world, local):
     traffic = None if half_storage else traffic_per_launch_pair()
     total_ms = sum(t for t, _ in kinds.values())
     cpu_baseline = None
-    if args.cpu_steps > 0:
+    if args.cpu_steps > 0 and not c5:
         cpu = run_cpu(args.half, args.cpu_steps, 1)
         cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
         cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
@@ -335,10 +345,12 @@ def engine_arm(args, rank, world, local):
         "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": dev_s * 1e3 / (K * R), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload(cells), "cells": cells, "parallelism": "replicas" if world > 1 else "single GPU",
+        "config": {"workload": workload_c5(cells) if c5 else workload(cells), "cells": cells,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
                    "storage": STORAGE[args.storage],
                    "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
-                   "phaser": "64 frequencies, %s, time-blocked ring of %s steps" % (
+                   "phaser": "%d frequencies, %s, time-blocked ring of %s steps" % (
+                       C5[4] if c5 else NFREQ,
                        "Kahan-compensated" if os.environ.get("ALISGPU_PHASER_KAHAN") == "1" else "plain float sums",
                        os.environ.get("ALISGPU_PHASER_RING", "64")),
                    "path": "batched launches (alisBatchBegin/End)" if args.batched else "one launch per half step",
@@ -361,7 +373,7 @@ def engine_arm(args, rank, world, local):
         "clocks": clocks,
         "result_flux": flux,
     }
-    if args.forms:
+    if args.forms and not c5:
         # the batched and served forms, each against its per-request path,
         # and the same workload with half field storage
         line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form(),
@@ -463,6 +475,9 @@ def main():
     ap.add_argument("--sweep", type=int, default=0, metavar="N",
                     help="run the batched unit-cell sweep of N cells instead (512: the full sweep)")
     ap.add_argument("--sweep-steps", type=int, default=0, help="steps per unit cell (default 3000)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c5"],
+                    help="c2: the dispersive scatterer (256^3, the headline); c5: the large-domain precision "
+                         "workload (1024 x 1024 x 512, 200 balls), for its float and half storage throughput")
     ap.add_argument("--storage", default="float", choices=sorted(STORAGE),
                     help="field storage of the world: float, or half values with a power-of-two exponent per "
                          "component and x plane (alisgpu_world_set_storage)")

@@ -43,6 +43,10 @@
  *   farmaps the dipole world's far-field maps: farFieldProfile images of
  *           all seven polarisations over two projections (one of them
  *           logarithmic) and the farFieldTheta / farFieldPhi cuts
+ *   c5      the large-domain precision workload in miniature: seeded
+ *           Drude-Lorentz balls in a dielectric host, 16-cell CPML, two
+ *           pulsed dipoles and a transmission phaser plane ((64 scale)^3
+ *           cells)
  */
 #include <alis.h>
 #include "dump.h"
@@ -395,6 +399,50 @@ static void sceneSpheres(int steps)
 	dumpPhasers(P, "P");
 }
 
+/* the large-domain precision workload in miniature (configuration 5):
+ * (64 scale)^3 cells with a 16-cell CPML on all faces, a dielectric host
+ * (n = 1.5) holding 2 + scale^3 / 10 seeded Drude-Lorentz balls of radius
+ * 5 scale to 20 scale cells (20-80 at scale 4, its 256^3 sub-run), two
+ * pulsed dipoles, a transmission phaser plane.  (A plane wave's auxiliary
+ * column takes the world's object list, and the reference stops on an
+ * object that misses the column, as scattered balls do.) */
+static void sceneC5(int steps)
+{
+	const int n = 64 * scale, in = n - 34;          /* cells per axis, interior */
+	const float dx = 5;
+	dom D = {{-(in / 2) * dx, (in - in / 2 - 1) * dx}, {-(in / 2) * dx, (in - in / 2 - 1) * dx},
+	         {-(in / 2) * dx, (in - in / 2 - 1) * dx}};
+	res R = {2.5, {dx}, {1240}};
+	sur S = {{PML}, {PML}, {PML}, {16}};
+	world W = createWorld(D, R, S, "");
+	enum { NBMAX = 64 };
+	const int nb = 2 + scale * scale * scale / 10;
+	object O[NBMAX + 1];
+	matter M[NBMAX + 1];
+	lcgSeed(2024);
+	for (int q = 0; q < nb && q < NBMAX; q++) {
+		/* one draw per statement: the order is fixed */
+		float r = dx * scale * (5 + 15 * lcgUniform());
+		float x = D.x.Min + r + (D.x.Max - D.x.Min - 2 * r) * lcgUniform();
+		float y = D.y.Min + r + (D.y.Max - D.y.Min - 2 * r) * lcgUniform();
+		float z = D.z.Min + r + (D.z.Max - D.z.Min - 2 * r) * lcgUniform();
+		float e = 1.5 + lcgUniform(), wp = 5 + 4 * lcgUniform(), g = 0.05 + 0.2 * lcgUniform();
+		float w0 = 3 + lcgUniform(), f0 = 0.5 + lcgUniform();
+		O[q] = (object){Ball, {{x - r, x + r}, {y - r, y + r}, {z - r, z + r}}};
+		M[q] = (matter){{e}, {{wp, g}, {w0, 0.2, f0}}};
+	}
+	O[nb < NBMAX ? nb : NBMAX] = (object){0};
+	M[nb < NBMAX ? nb : NBMAX] = n(1.5);
+	putObjectArray(W, M, O);
+	pointDipole(W, Ex, 0, 0, D.z.Min / 2, Pulse, 600, 150);
+	pointDipole(W, Ez, D.x.Max / 3, D.y.Min / 3, 0, Pulse, 500, 100);
+	phaser P = createPhasers(W, 400, 800, 400.0 / 15, -INF, INF, -INF, INF, D.z.Max - 4 * dx, D.z.Max - 4 * dx);
+	run(W, P, steps);
+	dumpScalar("S.abs", objectAbsorption(W, O[0]));
+	dumpWorld(W, "W");
+	dumpPhasers(P, "P");
+}
+
 /* a metasurface unit cell of the batched sweep: periodic x/y, CPML z, a
  * TiO2-like Lorentz pillar on a glass substrate, a normal-incidence pulse,
  * a transmission phaser plane */
@@ -710,6 +758,7 @@ int main(int argc, char **argv)
 	else if (!strcmp(s, "aniso")) sceneAniso(steps);
 	else if (!strcmp(s, "lattice")) sceneLattice(steps);
 	else if (!strcmp(s, "farmaps")) sceneFarMaps(steps);
+	else if (!strcmp(s, "c5")) sceneC5(steps);
 	else { fprintf(stderr, "unknown scene %s\n", s); return 2; }
 	dumpClose();
 	return 0;

@@ -54,6 +54,9 @@ CASES = [
     ("aniso", 1, 120),
     ("lattice", 1, 120),
     ("farmaps", 1, 120),
+    # the large-domain precision workload in miniature: seeded Drude-Lorentz
+    # balls in a dielectric host, 16-cell CPML, pulsed dipoles
+    ("c5", 1, 120),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 

@@ -281,3 +281,33 @@ def test_fp16_storage_error_against_fp64(builds, case):
         assert e32["flux"][0] <= BOUND["flux"] and e16["flux"][0] < 2e-2
     if "far" in e16:
         assert e16["far"][0] < 2e-2
+
+
+C5_STEPS = 800
+
+
+@pytest.mark.gpu
+def test_config5_subrun_error_against_fp64(builds):
+    """The large-domain precision study (configuration 5) on its 256^3
+    sub-run: the c5 world at scale 4 (256^3 cells with the 16-cell CPML,
+    8 seeded Drude-Lorentz balls of radius 20-80 cells in an n = 1.5
+    host, two pulsed dipoles, a 16-frequency transmission plane; 800
+    steps, until the pulses have crossed the plane) on the engine with
+    float and with half field storage, against the FP64 run of the same
+    world on the host cores.  Float storage is the FP32 reference's
+    arithmetic (byte-identical to the oracle): fields 1.2e-5 from FP64,
+    phaser faces 3.0e-5, in-band flux 5.9e-5, the balls' ADE currents
+    1.4e-4 (their Drude poles' float recursion over 800 steps).  Half
+    storage carries the 11-bit mantissa's rounding at every store: fields
+    5.4e-3, faces 1.9e-3, flux 6.1e-4, currents 1.7e-4 (measured on the
+    oracle's restatement of both forms, which the engine matches byte for
+    byte)."""
+    b = scenes.run("oracle64", "c5", 4, C5_STEPS)
+    e32 = errors(scenes.run("engine", "c5", 4, C5_STEPS), b)
+    e16 = errors(scenes.run("engine", "c5", 4, C5_STEPS, env={"ALIS_FIELD_STORAGE": "half"}), b)
+    print("c5 256^3 sub-run, %d steps, error vs FP64, float storage / half storage: %s" % (C5_STEPS, ", ".join(
+        "%s %.2e / %.2e" % (k, e32[k][0], e16[k][0]) for k in ("field", "ade", "face", "flux") if k in e16)))
+    for cat, bound in dict(BOUND, ade=5e-4).items():
+        if cat in e32:
+            assert e32[cat][0] <= bound, (cat, e32[cat])
+    assert e16["field"][0] < 3e-2 and e16["face"][0] < 1e-2 and e16["flux"][0] < 5e-3
