@@ -16,7 +16,6 @@
 #define ALIS_KOFF 31
 #define ALIS_MAXPOLES 6
 #define ALIS_MAXTFSF 4
-#define ALIS_TILE_OBJ 48
 
 struct Layout {
 	int i0, j0, k0;          // first stored index (MIN - 1)
@@ -146,8 +145,16 @@ struct HalfStepParams {
 	// n's range, bit 8 any object n >= 8, bit 13/14 CPML slab of the min/max
 	// face, bit 15 TFSF face plane
 	const unsigned short *cls[3];
+	// worlds with more than 8 objects: per tile of ALIS_TILE_K cells along
+	// k x ALIS_TILE_J rows x 1 plane, the objects whose box meets it, in
+	// list order (tileObj[tileStart[t] .. tileStart[t + 1]]); tiles
+	// numbered (plane * tjn + j tile) * tkn + k tile, from MIN
+	const int *tileStart, *tileObj;
+	int tjn, tkn;
 	HalfPlanes h;                         // FP16 storage (the HALF instances)
 };
+#define ALIS_TILE_K 32
+#define ALIS_TILE_J 8
 #define CLS_OBJ8 0x100u
 #define CLS_PML_LO 0x2000u
 #define CLS_PML_HI 0x4000u

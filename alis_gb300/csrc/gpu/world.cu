@@ -307,6 +307,10 @@ struct alisgpu_world {
 	// what the cell-class tables of each field were made from: the CPML
 	// slabs, the TFSF boxes and the object boxes
 	std::vector<int> clsKey[2];
+	// per-tile object lists of a world with more than 8 objects, and the
+	// object boxes they were made from
+	int *tileStart, *tileObj;
+	std::vector<int> tileKey;
 	// FP16 storage (alisgpu_world_set_storage), per field: by the parity
 	// of the step, the exponents as read and as computed and the scales as
 	// read; the next step's inverse scales; the plane maxima of two steps
@@ -444,6 +448,7 @@ extern "C" int alisgpu_world_destroy(alisgpu_world *w)
 		alisgpu__freeAsync(w->inv[f]), alisgpu__freeAsync(w->tab[f]);
 	}
 	if (w->planeTab) alisgpu__freeAsync(w->planeTab);
+	alisgpu__freeAsync(w->tileStart), alisgpu__freeAsync(w->tileObj);
 	if (w->matIdx) alisgpu__freeAsync(w->matIdx);
 	if (w->matTab) alisgpu__freeAsync(w->matTab);
 	for (int grid = 0; grid < 2; grid++) for (int a = 0; a < 3; a++) if (w->sp[grid][a]) alisgpu__freeAsync(w->sp[grid][a]);
@@ -1429,69 +1434,50 @@ __device__ __forceinline__ void plainCell(const HalfStepParams &P, int i, int j,
 // all inline, and cells on TFSF i or j face planes (whole blocks or
 // warps) and dispersive cells go to hardCell.  Index arithmetic is 32-bit
 // (at most 2^31 elements per array, checked on the host).  Worlds with
-// more than 8 objects add a per-tile list of the objects that meet it
-// (tileList/nlist in shared memory, one block's).
+// more than 8 objects read the list of the objects that meet the block's
+// tile (made on the host when the objects change, objectTiles).
 template <int ALT, int TY_, bool HALF = false>
-__device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, int by, int plane, int *tileList, int *nlist)
+__device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, int by, int plane)
 {
 	const int k = P.kMIN + bx * TX + threadIdx.x;
 	const int j = P.jMIN + by * TY_ + threadIdx.y;
 	// E sweeps i downwards, H upwards: each starts on the planes the other
 	// touched last, which are still in L2
 	const int i = ALT == 1 ? P.iMAX - plane : P.iMIN + plane;
-	const bool manyObj = P.nobj > 8;
-	if (manyObj) {
-		// objects whose box meets this tile, in list order (one warp)
-		__syncthreads();
-		if (threadIdx.y == 0) {
-			const int tj0 = P.jMIN + by * TY_, tj1 = min(tj0 + TY_ - 1, P.jMAX);
-			const int tk0 = P.kMIN + bx * TX, tk1 = min(tk0 + TX - 1, P.kMAX);
-			int cnt = 0;
-			for (int base = 0; base < P.nobj; base += 32) {
-				int n = base + threadIdx.x;
-				bool hit = false;
-				if (n < P.nobj) {
-					const DevObj &o = P.obj[n];
-					hit = i >= o.i0 && i <= o.i1 && tj1 >= o.j0 && tj0 <= o.j1 && tk1 >= o.k0 && tk0 <= o.k1;
-				}
-				unsigned bal = __ballot_sync(0xffffffffu, hit);
-				if (hit) {
-					int pos = cnt + __popc(bal & ((1u << threadIdx.x) - 1));
-					if (pos < ALIS_TILE_OBJ) tileList[pos] = n;
-				}
-				cnt += __popc(bal);
-			}
-			if (threadIdx.x == 0) *nlist = cnt;
-		}
-		__syncthreads();
+	// worlds with more than 8 objects: the objects of the block's tile (a
+	// block lies in one tile: TX = ALIS_TILE_K, TY_ divides ALIS_TILE_J);
+	// a tile that meets none has no object cells
+	const int *list = 0;
+	int nIter = P.nobj;
+	bool objTile = true;
+	if (P.tileStart) {
+		const int t = ((i - P.iMIN) * P.tjn + (by * TY_) / ALIS_TILE_J) * P.tkn + bx;
+		const int s0 = __ldg(P.tileStart + t);
+		list = P.tileObj + s0, nIter = __ldg(P.tileStart + t + 1) - s0, objTile = nIter > 0;
 	}
 	const bool inRange = k <= P.kMAX && j <= P.jMAX;
 	unsigned bi = 0, bj = 0, bk = 0;
 	if (inRange) bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
-	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI | CLS_TFSF)) && !(bi & bj & bk & 0x1FFu);
+	const unsigned objm = objTile ? bi & bj & bk & 0x1FFu : 0u;
+	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI | CLS_TFSF)) && !objm;
 	if (__all_sync(0xffffffffu, plain)) {
 		plainCell<ALT, HALF>(P, i, j, k);
 		return;
 	}
 	if (!inRange) return;
-	if (!((bi | bj) & CLS_TFSF) && !(bi & bj & bk & 0x1FFu)) {
+	if (!((bi | bj) & CLS_TFSF) && !objm) {
 		leanCells<ALT, 1, HALF>(P, i, j, k, bi, bj, &bk);
 		return;
 	}
 	// hard cells run the full sequence out of line (object loops: the
 	// tile's list, or all objects filtered by class bits)
-	const int *list = 0;
-	int nIter = P.nobj;
-	if (manyObj && *nlist <= ALIS_TILE_OBJ) list = tileList, nIter = *nlist;
 	hardCell<ALT, HALF>(P, i, j, k, list, nIter);
 }
 
 template <int ALT, int TY, bool HALF = false>
 __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
-	__shared__ int tileList[ALIS_TILE_OBJ];
-	__shared__ int nlist;
-	halfStepBlock<ALT, TY, HALF>(P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, tileList, &nlist);
+	halfStepBlock<ALT, TY, HALF>(P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
 }
 
 // sources, in list order; one block so later patches see earlier ones
@@ -1872,9 +1858,7 @@ __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step_aux(const 
 		if (blockIdx.x == 0 && blockIdx.y == 0) smallStepBlock<ALT>(F.aux, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
 		return;
 	}
-	__shared__ int tileList[ALIS_TILE_OBJ];
-	__shared__ int nlist;
-	halfStepBlock<ALT, TY, HALF>(F.P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z - 1, tileList, &nlist);
+	halfStepBlock<ALT, TY, HALF>(F.P, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z - 1);
 }
 
 // one half-step launch with block height kTyChoice[v] (v a runtime choice)
@@ -1968,8 +1952,6 @@ static_assert(sizeof(BatchStep<BATCH_WORLDS>) <= 32000, "batched launch paramete
 template <int ALT, int CAP>
 __global__ void __launch_bounds__(TX * BATCH_TY, STEP_MINB(BATCH_TY)) k_step_batch(const __grid_constant__ BatchStep<CAP> B)
 {
-	__shared__ int tileList[ALIS_TILE_OBJ];
-	__shared__ int nlist;
 	if ((int)blockIdx.x < B.h.nblk) {
 		const BatchBlock &b = B.h.blk[blockIdx.x];
 		smallStepBlock<ALT>(*b.S, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, b.voff >= 0 ? B.h.vals + b.voff : 0);
@@ -1981,7 +1963,7 @@ __global__ void __launch_bounds__(TX * BATCH_TY, STEP_MINB(BATCH_TY)) k_step_bat
 	for (int q = 1; q < CAP; q++) if (q < B.h.nE && B.E[q].itemStart <= g) e = q;
 	const BatchEntry &E = B.E[e];
 	const int t = g - E.itemStart, plane = E.byPlane.div(t), r = t - plane * E.nbx * E.nby, by = E.byRow.div(r);
-	halfStepBlock<ALT, BATCH_TY>(B.P[e], r - by * E.nbx, by, plane, tileList, &nlist);
+	halfStepBlock<ALT, BATCH_TY>(B.P[e], r - by * E.nbx, by, plane);
 }
 
 __global__ void k_sources_batch(const BatchSource *T, const float *vals)
@@ -2790,6 +2772,58 @@ __global__ void k_half_table(const HalfTableParams T)
 	halfTableEntry(T, blockIdx.x * blockDim.x + threadIdx.x);
 }
 
+// The objects of each tile of ALIS_TILE_K x ALIS_TILE_J x 1 cells that
+// their boxes (clipped to the updated cells, as the per-cell test clips
+// them) meet, in list order: counted per tile, then filled object by
+// object.  Made again only when the object boxes change.
+static int objectTiles(alisgpu_world *w, HalfStepParams &P)
+{
+	const alisgpu_geometry &g = w->g;
+	const int nI = g.iMAX - g.iMIN + 1, nJ = g.jMAX - g.jMIN + 1, nK = g.kMAX - g.kMIN + 1;
+	P.tjn = (nJ + ALIS_TILE_J - 1) / ALIS_TILE_J, P.tkn = (nK + ALIS_TILE_K - 1) / ALIS_TILE_K;
+	static thread_local std::vector<int> key;
+	key.assign({ g.iMIN, g.iMAX, g.jMIN, g.jMAX, g.kMIN, g.kMAX });
+	for (const DevObj &o : w->objs) key.insert(key.end(), { o.i0, o.i1, o.j0, o.j1, o.k0, o.k1 });
+	if (key != w->tileKey || !w->tileStart) {
+		const size_t nt = (size_t)nI * P.tjn * P.tkn;
+		if (nt >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "object tiles: %zu tiles", nt);
+		std::vector<int> start(nt + 1, 0), at;
+		// the tile ranges of each object's clipped box (empty: none)
+		auto span = [&](const DevObj &o, int r[6]) {
+			const int i0 = std::max(o.i0, g.iMIN), i1 = std::min(o.i1, g.iMAX);
+			const int j0 = std::max(o.j0, g.jMIN), j1 = std::min(o.j1, g.jMAX);
+			const int k0 = std::max(o.k0, g.kMIN), k1 = std::min(o.k1, g.kMAX);
+			if (i1 < i0 || j1 < j0 || k1 < k0) return false;
+			r[0] = i0 - g.iMIN, r[1] = i1 - g.iMIN;
+			r[2] = (j0 - g.jMIN) / ALIS_TILE_J, r[3] = (j1 - g.jMIN) / ALIS_TILE_J;
+			r[4] = (k0 - g.kMIN) / ALIS_TILE_K, r[5] = (k1 - g.kMIN) / ALIS_TILE_K;
+			return true;
+		};
+		int r[6];
+		for (const DevObj &o : w->objs)
+			if (span(o, r))
+				for (int a = r[0]; a <= r[1]; a++) for (int b = r[2]; b <= r[3]; b++) for (int c = r[4]; c <= r[5]; c++)
+					start[((size_t)a * P.tjn + b) * P.tkn + c + 1]++;
+		for (size_t t = 0; t < nt; t++) start[t + 1] += start[t];
+		if ((size_t)start[nt] >= (1u << 31)) return alisgpu__fail(ALISGPU_ERANGE, "object tiles: %d entries", start[nt]);
+		std::vector<int> list(std::max(start[nt], 1)), fill(start.begin(), start.end() - 1);
+		for (size_t n = 0; n < w->objs.size(); n++)
+			if (span(w->objs[n], r))
+				for (int a = r[0]; a <= r[1]; a++) for (int b = r[2]; b <= r[3]; b++) for (int c = r[4]; c <= r[5]; c++)
+					list[fill[((size_t)a * P.tjn + b) * P.tkn + c]++] = (int)n;
+		alisgpu__freeAsync(w->tileStart), alisgpu__freeAsync(w->tileObj);
+		w->tileStart = w->tileObj = 0;
+		w->tileKey.clear();
+		ALIS_CUDA(alisgpu__mallocAsync(&w->tileStart, (nt + 1) * sizeof(int)));
+		ALIS_CUDA(alisgpu__mallocAsync(&w->tileObj, list.size() * sizeof(int)));
+		ALIS_CUDA(orderedCopy(w->tileStart, start.data(), (nt + 1) * sizeof(int), cudaMemcpyHostToDevice));
+		ALIS_CUDA(orderedCopy(w->tileObj, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+		w->tileKey = key;
+	}
+	P.tileStart = w->tileStart, P.tileObj = w->tileObj;
+	return ALISGPU_OK;
+}
+
 // After a half step of a half world's field F, per (component, plane) of
 // the planes it updated: the largest magnitude over the plane's slots
 // gives F's next exponent, which becomes the next parity's exponent as
@@ -2890,6 +2924,10 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	}
 	P.nobj = (int)w->objs.size();
 	P.obj = w->dObjs;
+	if (P.nobj > 8) {
+		int rc = objectTiles(w, P);
+		if (rc) return rc;
+	}
 	P.ntfsf = s->ntfsf;
 	for (int q = 0; q < s->ntfsf; q++) P.tf[q] = tfsfFor(w, s->tfsf[q], field);
 	P.err = gErrWord;
