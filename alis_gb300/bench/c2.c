@@ -18,14 +18,14 @@
  * c5_build makes the large-domain precision workload in its place (the
  * stepping, result and byte functions below serve whichever was built):
  * ni x nj x nk cells with a 16-cell CPML on all faces, dx = 5 nm, a
- * dielectric host (n = 1.5) holding `balls` seeded Drude-Lorentz balls of
- * radius 20-80 cells (apart: each drawn again until it meets no earlier
- * one), two pulsed dipoles and an `nfreq`-frequency
- * transmission phaser plane near the top (1024 x 1024 x 512, 200 balls,
- * 128 frequencies: the full configuration).  E and H are stored as float,
- * or as half values with ALIS_FIELD_STORAGE=half.
+ * dielectric host (n = 1.5) holding `balls` Drude-Lorentz balls of radius
+ * 20-80 cells drawn from seed 99 (c5_balls.h), two pulsed dipoles and an
+ * `nfreq`-frequency phaser box 4 cells inside the CPML (1024 x 1024 x
+ * 512, 200 balls, 128 frequencies: the full configuration).  E and H are
+ * stored as float, or as half values with ALIS_FIELD_STORAGE=half.
  */
 #include <alis.h>
+#include "c5_balls.h"
 
 static world W;
 static phaser P;
@@ -76,46 +76,29 @@ long c5_build(int ni, int nj, int nk, int balls, int nfreq)
 {
 	const float dx = 5;
 	const int n[3] = { ni - 34, nj - 34, nk - 34 };     /* interior cells */
-	dom D;
-	float *lim[3][2] = { { &D.x.Min, &D.x.Max }, { &D.y.Min, &D.y.Max }, { &D.z.Min, &D.z.Max } };
-	for (int a = 0; a < 3; a++) *lim[a][0] = -(n[a] / 2) * dx, *lim[a][1] = (n[a] - n[a] / 2 - 1) * dx;
+	c5Real lo[3], hi[3];
+	c5Domain(n, dx, lo, hi);
+	dom D = {{lo[0], hi[0]}, {lo[1], hi[1]}, {lo[2], hi[2]}};
 	res R = {2.5, {dx}, {1240}};
 	sur S = {{PML}, {PML}, {PML}, {16}};
 	W = createWorld(D, R, S, "");
+	c5Ball *B = calloc(balls, sizeof *B);
 	object *O = calloc(balls + 1, sizeof *O);
 	matter *M = calloc(balls + 1, sizeof *M);
-	rngState = 5 * 6364136223846793005ULL + 1442695040888963407ULL;
-	float (*c)[4] = calloc(balls, sizeof *c);
+	c5Balls(99, balls, lo, hi, dx, B);
 	for (int q = 0; q < balls; q++) {
-		/* one draw per statement: the order is fixed.  A ball that meets
-		 * an earlier one is drawn again (an object wholly covered by
-		 * earlier ones has no cells, which stops the setup) */
-		float r, x, y, z;
-		for (int tries = 0;; tries++) {
-			r = dx * (20 + 60 * uniform01());
-			x = D.x.Min + r + (D.x.Max - D.x.Min - 2 * r) * uniform01();
-			y = D.y.Min + r + (D.y.Max - D.y.Min - 2 * r) * uniform01();
-			z = D.z.Min + r + (D.z.Max - D.z.Min - 2 * r) * uniform01();
-			int meets = 0;
-			for (int p = 0; p < q && !meets; p++) {
-				float u = x - c[p][0], v = y - c[p][1], w = z - c[p][2], s = r + c[p][3];
-				meets = u * u + v * v + w * w < s * s;
-			}
-			if (!meets || tries == 10000) break;
-		}
-		c[q][0] = x, c[q][1] = y, c[q][2] = z, c[q][3] = r;
-		float e = 1.5 + uniform01(), wp = 5 + 4 * uniform01(), g = 0.05 + 0.2 * uniform01();
-		float w0 = 3 + uniform01(), f0 = 0.5 + uniform01();
-		O[q] = (object){Ball, {{x - r, x + r}, {y - r, y + r}, {z - r, z + r}}};
-		M[q] = (matter){{e}, {{wp, g}, {w0, 0.2, f0}}};
+		const c5Ball b = B[q];
+		O[q] = (object){Ball, {{b.x - b.r, b.x + b.r}, {b.y - b.r, b.y + b.r}, {b.z - b.r, b.z + b.r}}};
+		M[q] = (matter){{b.e}, {{b.wp, b.g}, {b.w0, 0.2, b.f0}}};
 	}
 	M[balls] = n(1.5);
 	putObjectArray(W, M, O);
-	free(O), free(M), free(c);
+	free(B), free(O), free(M);
 	pointDipole(W, Ex, 0, 0, D.z.Min / 2, Pulse, 600, 150);
 	pointDipole(W, Ez, D.x.Max / 3, D.y.Min / 3, 0, Pulse, 500, 100);
 	int want = nfreq > 1 ? nfreq : 128;
-	P = createPhasers(W, 400, 800, 400.0f/(want-1), -INF, INF, -INF, INF, D.z.Max - 4 * dx, D.z.Max - 4 * dx);
+	const float m = 4 * dx;
+	P = createPhasers(W, 400, 800, 400.0f/(want-1), D.x.Min + m, D.x.Max - m, D.y.Min + m, D.y.Max - m, D.z.Min + m, D.z.Max - m);
 	for (nfreqs = 0; P[nfreqs].f; nfreqs++);
 	return (long)W->iNUM * W->jNUM * W->kNUM;
 }

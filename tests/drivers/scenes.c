@@ -43,13 +43,13 @@
  *   farmaps the dipole world's far-field maps: farFieldProfile images of
  *           all seven polarisations over two projections (one of them
  *           logarithmic) and the farFieldTheta / farFieldPhi cuts
- *   c5      the large-domain precision workload in miniature: seeded
- *           Drude-Lorentz balls in a dielectric host, 16-cell CPML, two
- *           pulsed dipoles and a transmission phaser plane ((64 scale)^3
- *           cells)
+ *   c5      a (64 scale)^3 window of the large-domain precision world:
+ *           its seeded Drude-Lorentz balls clipped to the window in a
+ *           dielectric host, 16-cell CPML, two pulsed dipoles, box phasers
  */
 #include <alis.h>
 #include "dump.h"
+#include "../../alis_gb300/bench/c5_balls.h"
 
 static int scale = 1;
 
@@ -399,46 +399,54 @@ static void sceneSpheres(int steps)
 	dumpPhasers(P, "P");
 }
 
-/* the large-domain precision workload in miniature (configuration 5):
- * (64 scale)^3 cells with a 16-cell CPML on all faces, a dielectric host
- * (n = 1.5) holding 2 + scale^3 / 10 seeded Drude-Lorentz balls of radius
- * 5 scale to 20 scale cells (20-80 at scale 4, its 256^3 sub-run), two
- * pulsed dipoles, a transmission phaser plane.  (A plane wave's auxiliary
- * column takes the world's object list, and the reference stops on an
- * object that misses the column, as scattered balls do.) */
+/* the large-domain precision workload's sub-runs (configuration 5): a
+ * (64 scale)^3-cell window at the centre of the 1024 x 1024 x 512 world,
+ * with a 16-cell CPML of its own: the full world's 200 balls from seed 99
+ * (c5_balls.h, as the bench world draws them), clipped to the window --
+ * those reaching at least 2 cells into it -- in the n = 1.5 host; two
+ * pulsed dipoles and a 16-frequency phaser box 4 cells inside the CPML.
+ * Scale 4 is the 256^3 sub-run of the precision study. */
 static void sceneC5(int steps)
 {
-	const int n = 64 * scale, in = n - 34;          /* cells per axis, interior */
 	const float dx = 5;
-	dom D = {{-(in / 2) * dx, (in - in / 2 - 1) * dx}, {-(in / 2) * dx, (in - in / 2 - 1) * dx},
-	         {-(in / 2) * dx, (in - in / 2 - 1) * dx}};
+	const int full[3] = { 1024 - 34, 1024 - 34, 512 - 34 }, in = 64 * scale - 34;
+	const int sub[3] = { in, in, in };
+	c5Real flo[3], fhi[3], lo[3], hi[3];
+	c5Domain(full, dx, flo, fhi);
+	c5Domain(sub, dx, lo, hi);
+	dom D = {{lo[0], hi[0]}, {lo[1], hi[1]}, {lo[2], hi[2]}};
 	res R = {2.5, {dx}, {1240}};
 	sur S = {{PML}, {PML}, {PML}, {16}};
 	world W = createWorld(D, R, S, "");
-	enum { NBMAX = 64 };
-	const int nb = 2 + scale * scale * scale / 10;
-	object O[NBMAX + 1];
-	matter M[NBMAX + 1];
-	lcgSeed(2024);
-	for (int q = 0; q < nb && q < NBMAX; q++) {
-		/* one draw per statement: the order is fixed */
-		float r = dx * scale * (5 + 15 * lcgUniform());
-		float x = D.x.Min + r + (D.x.Max - D.x.Min - 2 * r) * lcgUniform();
-		float y = D.y.Min + r + (D.y.Max - D.y.Min - 2 * r) * lcgUniform();
-		float z = D.z.Min + r + (D.z.Max - D.z.Min - 2 * r) * lcgUniform();
-		float e = 1.5 + lcgUniform(), wp = 5 + 4 * lcgUniform(), g = 0.05 + 0.2 * lcgUniform();
-		float w0 = 3 + lcgUniform(), f0 = 0.5 + lcgUniform();
-		O[q] = (object){Ball, {{x - r, x + r}, {y - r, y + r}, {z - r, z + r}}};
-		M[q] = (matter){{e}, {{wp, g}, {w0, 0.2, f0}}};
+	enum { NB = 200 };
+	static c5Ball B[NB];
+	c5Balls(99, NB, flo, fhi, dx, B);
+	object O[NB + 1];
+	matter M[NB + 1];
+	int nb = 0;
+	for (int q = 0; q < NB; q++) {
+		const c5Ball b = B[q];
+		const c5Real c[3] = { b.x, b.y, b.z };
+		c5Real d2 = 0;
+		for (int a = 0; a < 3; a++) {
+			const c5Real e = c[a] < lo[a] ? lo[a] - c[a] : c[a] > hi[a] ? c[a] - hi[a] : 0;
+			d2 += e * e;
+		}
+		const c5Real deep = b.r - 2 * dx;
+		if (deep <= 0 || d2 >= deep * deep) continue;
+		O[nb] = (object){Ball, {{b.x - b.r, b.x + b.r}, {b.y - b.r, b.y + b.r}, {b.z - b.r, b.z + b.r}}};
+		M[nb++] = (matter){{b.e}, {{b.wp, b.g}, {b.w0, 0.2, b.f0}}};
 	}
-	O[nb < NBMAX ? nb : NBMAX] = (object){0};
-	M[nb < NBMAX ? nb : NBMAX] = n(1.5);
+	O[nb] = (object){0};
+	M[nb] = n(1.5);
 	putObjectArray(W, M, O);
 	pointDipole(W, Ex, 0, 0, D.z.Min / 2, Pulse, 600, 150);
 	pointDipole(W, Ez, D.x.Max / 3, D.y.Min / 3, 0, Pulse, 500, 100);
-	phaser P = createPhasers(W, 400, 800, 400.0 / 15, -INF, INF, -INF, INF, D.z.Max - 4 * dx, D.z.Max - 4 * dx);
+	const float m = 4 * dx;
+	phaser P = createPhasers(W, 400, 800, 400.0 / 15, D.x.Min + m, D.x.Max - m, D.y.Min + m, D.y.Max - m, D.z.Min + m, D.z.Max - m);
 	run(W, P, steps);
-	dumpScalar("S.abs", objectAbsorption(W, O[0]));
+	dumpScalar("S.balls", nb);
+	if (nb) dumpScalar("S.abs", objectAbsorption(W, O[0]));
 	dumpWorld(W, "W");
 	dumpPhasers(P, "P");
 }

@@ -54,9 +54,9 @@ CASES = [
     ("aniso", 1, 120),
     ("lattice", 1, 120),
     ("farmaps", 1, 120),
-    # the large-domain precision workload in miniature: seeded Drude-Lorentz
-    # balls in a dielectric host, 16-cell CPML, pulsed dipoles
-    ("c5", 1, 120),
+    # a 128^3 window of the large-domain precision world: its seeded
+    # Drude-Lorentz balls clipped to the window, 16-cell CPML, pulsed dipoles
+    ("c5", 2, 80),
 ]
 IDS = ["%s-x%d" % (c[0], c[1]) for c in CASES]
 

@@ -30,7 +30,7 @@ ORACLE = {"ALIS_ORACLE_FP16_STORAGE": "1"}
 HALF_CASES = [
     ("c1", 1, 120), ("c2", 1, 100), ("dipole", 1, 120), ("unitcell", 1, 120), ("sym", 1, 120),
     ("pec", 1, 120), ("spheres", 1, 80), ("nug", 1, 120), ("bowtie", 1, 120), ("multi", 1, 100),
-    ("aniso", 1, 100), ("lattice", 1, 100), ("farmaps", 1, 100), ("beamtf", 1, 100), ("c5", 1, 120),
+    ("aniso", 1, 100), ("lattice", 1, 100), ("farmaps", 1, 100), ("beamtf", 1, 100), ("c5", 2, 80),
 ]
 IDS = ["%s-%d-%d" % c for c in HALF_CASES]
 
