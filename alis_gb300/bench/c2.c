@@ -185,5 +185,17 @@ double c2_result_d2h_bytes(void)
 	return 6.0 * sizeof(float) * nfreqs;
 }
 
+/* face cells of the phaser box: the faces the phaser keeps (reference
+ * src/phaser.c:57-62), one cell thick */
+double c2_phaser_face_cells(void)
+{
+	const double ni = 1 + P->iMax - P->iMin, nj = 1 + P->jMax - P->jMin, nk = 1 + P->kMax - P->kMin;
+	const int on[6] = { P->xMin.Ey != 0, P->xMax.Ey != 0, P->yMin.Ez != 0, P->yMax.Ez != 0, P->zMin.Ex != 0, P->zMax.Ex != 0 };
+	const double face[3] = { nj * nk, ni * nk, ni * nj };
+	double cells = 0;
+	for (int s = 0; s < 6; s++) if (on[s]) cells += face[s / 2];
+	return cells;
+}
+
 long c2_cells(void) { return (long)W->iNUM * W->jNUM * W->kNUM; }
 int c2_nfreq(void) { return nfreqs; }

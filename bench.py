@@ -263,6 +263,8 @@ def engine_arm(args, rank, world, local):
     lib.c2_step_bytes_half.restype = ctypes.c_double
     lib.c2_step_h2d_bytes.restype = ctypes.c_double
     lib.c2_result_d2h_bytes.restype = ctypes.c_double
+    lib.c2_phaser_face_cells.restype = ctypes.c_double
+    lib.c2_nfreq.restype = ctypes.c_int
     eng.alisgpu_stream.restype = ctypes.c_void_p
     eng.alisgpu_launch_count.restype = ctypes.c_ulonglong
     cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
@@ -314,6 +316,7 @@ def engine_arm(args, rank, world, local):
         # whole number of ring periods
         eng.alisgpu_profile(1)
         steps_fn(windows(K, ring, 1) * K)
+        lib.c2_result()                        # the pass's last ring flush (its face fluxes are not a listed kind)
         kinds = {}
         for kind, name in enumerate(["step_E", "step_H", "ghost", "source", "gather", "flush", "farfield", "step_aux"]):
             t, n = ctypes.c_double(), ctypes.c_ulonglong()
@@ -368,6 +371,7 @@ def engine_arm(args, rank, world, local):
                      "kernel": "k_half_step (E + H launches, mean per launch pair)",
                      "algorithmic_bytes_per_step": step_bytes, "launch_pair_ms": pair_ms},
         "kernel_share": {k: round(t / total_ms, 4) for k, (t, n) in kinds.items() if n},
+        "phaser": phaser_rate(lib, kinds, K, windows(K, ring, 1) * K),
         "cpu_baseline": cpu_baseline,
         "gpu_launches": int(launches),
         "clocks": clocks,
@@ -379,6 +383,21 @@ def engine_arm(args, rank, world, local):
         line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form(),
                          "half_storage": half_form(args, line)}
     print(json.dumps(line), flush=True)
+
+
+def phaser_rate(lib, kinds, K, profiled_steps):
+    """The phaser DFT against the reference formulation, reported apart
+    from the half-step roofline: per face cell per step the reference reads
+    24 B of fields and read-modify-writes 4 complex accumulators per
+    frequency, 64 B (128 B with the Kahan compensation terms); effective
+    GB/s = those bytes / the gather and flush kernels' time per step (the
+    engine's time-blocked DFT moves far fewer)."""
+    cells, nf = lib.c2_phaser_face_cells(), lib.c2_nfreq()
+    kahan = os.environ.get("ALISGPU_PHASER_KAHAN") == "1"
+    ref = cells * (24 + (128 if kahan else 64) * nf)
+    ms = (kinds["gather"][0] + kinds["flush"][0]) / max(profiled_steps, 1)
+    return {"face_cells": cells, "frequencies": nf, "reference_bytes_per_step": ref,
+            "ms_per_step": ms, "effective_GBps": ref / (ms / 1e3) / 1e9 if ms > 0 else None}
 
 
 def half_form(args, line):
