@@ -830,8 +830,7 @@ int alis_gpu_farfield(phaser P, int nA, const tfield *T, const float *kx, const 
  * shape is told by its function; a list holding a shape the device does
  * not evaluate (ImportContour, user functions) stays with the host loops.
  * The host supplies every sample coordinate through the world's own
- * itox/jtoy/ktoz and the glibc trigonometric values of rotations.
- * ALISGPU_VOXELIZE=host leaves every list to the host loops. */
+ * itox/jtoy/ktoz and the glibc trigonometric values of rotations. */
 
 #define VOX_MAX_DEPTH 12   /* nesting the device recursion allows */
 
@@ -954,9 +953,8 @@ static float *voxTable(world W, float (*itox)(world, float), int lo, int hi, int
 
 void *alis_be_vox_begin(world W, object *O, int N)
 {
-	const char *e = getenv("ALISGPU_VOXELIZE");
 	/* the supersampling counts hits exactly up to 2^24 samples */
-	if (N <= 0 || W->subN > 256 || (e && !strcmp(e, "host"))) return NULL;
+	if (N <= 0 || W->subN > 256) return NULL;
 	voxList L = { 0 };
 	voxNodes(&L, N);
 	int ok = 1;

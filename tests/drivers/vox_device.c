@@ -1,9 +1,10 @@
 /*
- * vox_device.c -- one object list put into a world by the engine, for the
- * device voxelizer against the engine's own host loops
- * (ALISGPU_VOXELIZE=host, a second process).  Prints the engine's kernel
- * launches during putObjectArray, its wall time and an FNV-1a hash of the
- * eps^-1 maps and of the dispersive objects' fill maps.
+ * vox_device.c -- one object list put into a world, linked against the
+ * engine (the device voxelizer) or against the oracle (the host loops of
+ * the same host layer), for the device voxelizer against those loops.
+ * Prints the engine's kernel launches during putObjectArray (0 in the
+ * oracle build), its wall time and an FNV-1a hash of the eps^-1 maps and
+ * of the dispersive objects' fill maps.
  *
  *   vox_device <half size in nm> <subN> [contour]
  *
@@ -11,9 +12,12 @@
  * device does not evaluate: the whole list stays with the host loops.
  */
 #include <alis.h>
-#include <alisgpu.h>
 #include <stdint.h>
 #include <time.h>
+
+/* the engine's launch counter; absent from the oracle build */
+unsigned long long alisgpu_launch_count(void) __attribute__((weak));
+static unsigned long long launches(void) { return alisgpu_launch_count ? alisgpu_launch_count() : 0; }
 
 static unsigned long long rng;
 static float uniform(void)
@@ -78,12 +82,12 @@ int main(int argc, char **argv)
 	O[NO] = (object){0};
 	M[NO] = Air;
 
-	unsigned long long l0 = alisgpu_launch_count();
+	unsigned long long l0 = launches();
 	struct timespec t0, t1;
 	clock_gettime(CLOCK_MONOTONIC, &t0);
 	putObjectArray(W, M, O);
 	clock_gettime(CLOCK_MONOTONIC, &t1);
-	unsigned long long l1 = alisgpu_launch_count();
+	unsigned long long l1 = launches();
 
 	coeffs *C = W->CE;
 	uint64_t h = 1469598103934665603ULL;
