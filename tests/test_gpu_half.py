@@ -72,3 +72,20 @@ def test_half_storage_is_the_stored_form():
     full = scenes.run("engine", "c2", 1, 60)
     assert any(not np.array_equal(half[k], full[k]) for k in half_fields(half))
     assert_half_values(half)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scene,scale,steps", [("c1", 1, 120), ("c2", 1, 100), ("unitcell", 1, 120)],
+                         ids=["c1", "c2", "unitcell"])
+@pytest.mark.parametrize("shape", [0, 2], ids=["32x2", "32x8"])
+def test_half_storage_fused_column_and_shapes(scene, scale, steps, shape):
+    """Half storage with the TFSF auxiliary column inside the world's own
+    half-step launch (ALISGPU_AUX_ATTACH=2: the k_half_step_aux instances)
+    and with each other block shape (ALISGPU_STEP_SHAPE), byte-identical to
+    the oracle's half storage."""
+    env = dict(ENGINE, ALISGPU_AUX_ATTACH="2", ALISGPU_STEP_SHAPE=str(shape))
+    gpu = scenes.run("engine", scene, scale, steps, env=env)
+    cpu = scenes.run("oracle", scene, scale, steps, env=ORACLE)
+    near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
+    bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith(FAR)})
+    assert not bad, "differs from the oracle's half storage: %s" % bad[:10]
