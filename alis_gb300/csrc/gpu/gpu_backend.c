@@ -431,8 +431,9 @@ void alis_be_world_streams(world W)
 }
 
 /* FP16 field storage of the worlds the user steps (ALIS_FIELD_STORAGE=half;
- * their TFSF auxiliary worlds stay float): set before a world's first
- * half step, see alisgpu_world_set_storage */
+ * their TFSF auxiliary worlds, and worlds with complex fields, stay
+ * float): set before a world's first half step, see
+ * alisgpu_world_set_storage */
 static int halfStorage(void)
 {
 	static int on = -1;
@@ -447,7 +448,8 @@ static void halfStepAs(world W, int field, int attach)
 {
 	devWorld *d = findWorld(W);
 	if (!d) { fprintf(stderr, "alis: world unknown to the GPU backend\n"); exit(1); }
-	if (!d->stepped && !d->isAux && halfStorage()) CHECK("world_set_storage", alisgpu_world_set_storage(d->dw, ALISGPU_STORAGE_HALF));
+	if (!d->stepped && !d->isAux && !W->complexField && halfStorage())
+		CHECK("world_set_storage", alisgpu_world_set_storage(d->dw, ALISGPU_STORAGE_HALF));
 	d->stepped = 1;
 	if (d->ownStreams) shareStreams(d);
 	if (d->objectsDirty) uploadObjects(d);

@@ -263,8 +263,9 @@ static void tfsfH(world W, tfsf S)
 
 /* FP16 field storage (environment ALIS_ORACLE_FP16_STORAGE=1; the
  * engine's half storage, alisgpu_world_set_storage): the E and H
- * components of a world stepped by the user (not its TFSF auxiliary
- * columns) are held as IEEE half values times 2^e, one exponent e per
+ * components of a real world stepped by the user (not its TFSF auxiliary
+ * columns, not worlds with complex fields) are held as IEEE half values
+ * times 2^e, one exponent e per
  * component and x plane.  A half step takes e from the largest magnitude
  * M the plane's cells of that component reached in the previous half step
  * of the field, before rounding: e = x - 11 for M = f 2^x, f in [0.5, 1)
@@ -316,7 +317,6 @@ static HalfState *halfState(world W)
 	HalfState *h = halfStates;
 	while (h && h->W != W) h = h->next;
 	if (!h) {
-		if (W->complexField) { fprintf(stderr, "oracle: FP16 storage needs real fields\n"); exit(1); }
 		h = calloc(1, sizeof *h);
 		h->W = W, h->ni = W->iMAX - W->iMIN + 1;
 		for (int f = 0; f < 2; f++) for (int q = 0; q < 2; q++) h->M[f][q] = calloc(3 * (size_t)h->ni, sizeof(unsigned));
@@ -345,10 +345,11 @@ static int halfOn(void)
 	return fp16Storage && stepDepth == 1;
 }
 
-/* the half step's rounding of the cells it updated (field f: 0 E, 1 H) */
+/* the half step's rounding of the cells it updated (field f: 0 E, 1 H);
+ * worlds with complex fields stay float */
 static void storeStep(world W, vfield F, int f)
 {
-	if (!halfOn()) return;
+	if (!halfOn() || W->complexField) return;
 	HalfState *h = halfState(W);
 	float ***c[3] = { F.x, F.y, F.z };
 	unsigned *prev = h->M[f][0], *cur = h->M[f][1];
@@ -374,7 +375,7 @@ static void storeStep(world W, vfield F, int f)
  * (storeStep has made them the previous ones) */
 static void storeSources(world W, vfield F, int f, source S)
 {
-	if (!halfOn()) return;
+	if (!halfOn() || W->complexField) return;
 	HalfState *h = halfState(W);
 	const unsigned *used = h->M[f][1];
 	float ***c[3] = { F.x, F.y, F.z };

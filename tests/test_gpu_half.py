@@ -89,3 +89,15 @@ def test_half_storage_fused_column_and_shapes(scene, scale, steps, shape):
     near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
     bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith(FAR)})
     assert not bad, "differs from the oracle's half storage: %s" % bad[:10]
+
+
+@pytest.mark.gpu
+def test_complex_world_keeps_float_storage():
+    """With ALIS_FIELD_STORAGE=half a world with complex (Bloch) fields
+    stays in float storage (the device refuses half storage for it): the
+    same bytes as the oracle's float run."""
+    gpu = scenes.run("engine", "bloch", 1, 80, env=ENGINE)
+    cpu = scenes.run("oracle", "bloch", 1, 80)
+    near = {k: v for k, v in gpu.items() if not k.startswith(FAR)}
+    bad = scenes.compare_exact(near, {k: v for k, v in cpu.items() if not k.startswith(FAR)})
+    assert not bad, "differs from the oracle's float run: %s" % bad[:10]
