@@ -1475,11 +1475,12 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, i
 }
 
 // planes a block of the one-world launches steps, one after the other in
-// the sweep direction: the second plane's i neighbours of the other field
-// are the first plane's own cells, still in L1.  Two for half storage
-// (0.427 against 0.444 ms per pair on the 256^3 dispersive world), one
-// for float (two: 0.332 against 0.305, from register pressure)
-#define BLOCK_PLANES(HALF) ((HALF) ? 2 : 1)
+// the sweep direction: each plane's i neighbours of the other field are
+// the previous plane's own cells, still in L1.  Four for half storage
+// (0.415 ms per pair on the 256^3 dispersive world against 0.433 with
+// two, 0.444 with one and 0.433 with eight), one for float (two: 0.332
+// against 0.305, from register pressure)
+#define BLOCK_PLANES(HALF) ((HALF) ? 4 : 1)
 template <int ALT, int TY, bool HALF = false>
 __global__ void __launch_bounds__(TX * TY, STEP_MINB(TY)) k_half_step(const __grid_constant__ HalfStepParams P)
 {
