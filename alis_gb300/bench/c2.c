@@ -15,8 +15,9 @@
  * baseline program (oracle build).  `half` scales the domain (230 = the
  * full configuration).
  *
- * c5_build makes the large-domain precision workload in its place (the
- * stepping, result and byte functions below serve whichever was built):
+ * c1_build makes the vacuum plane-wave workload in its place and c5_build
+ * the large-domain precision workload (the stepping, result and byte
+ * functions below serve whichever was built).  c5_build:
  * ni x nj x nk cells with a 16-cell CPML on all faces, dx = 5 nm, a
  * dielectric host (n = 1.5) holding `balls` Drude-Lorentz balls of radius
  * 20-80 cells drawn from seed 99 (c5_balls.h), two pulsed dipoles and an
@@ -68,6 +69,25 @@ long c2_build(int half, int nfreq)
 	planewave(W, DT, Ppol, 0, 0, Pulse, 600, 200);
 	int want = nfreq > 1 ? nfreq : 64;
 	P = createPhasers(W, 400, 800, 400.0f/(want-1), -Pb, Pb-2, -Pb, Pb-2, -Pb, Pb-2);
+	for (nfreqs = 0; P[nfreqs].f; nfreqs++);
+	return (long)W->iNUM * W->jNUM * W->kNUM;
+}
+
+/* the vacuum plane-wave workload in its place: n x n x n cells with the
+ * CPML, dx = 10 nm, dt = 5 nm/c (Courant 0.5), periodic x and y, a 16-cell
+ * CPML on both z faces, an x-polarized pulse plane wave (600 nm,
+ * supplement 90) from the plane 20 cells above the low z CPML, and a
+ * 16-wavelength (400-800 nm) phaser plane at z = 100 nm */
+long c1_build(int n)
+{
+	const int h = n / 2, nz = n - 34;                /* interior z cells */
+	dom D = {{-10*h, 10*(h-1)}, {-10*h, 10*(h-1)}, {-10*(nz/2), 10*(nz - nz/2 - 1)}};
+	res R = {5, {10}, {1240}};
+	sur S = {{PBC}, {PBC}, {PML, PML}, {16}};
+	W = createWorld(D, R, S, "");
+	dom T = {{D.x.Min, D.x.Max}, {D.y.Min, D.y.Max}, {W->ktoz(W, W->kMIN+20), W->zMax-30}};
+	planewave(W, T, Ppol, 180, 0, Pulse, 600, 90);
+	P = createPhasers(W, 400, 800, 400.0/15, -INF, INF, -INF, INF, 100, 100);
 	for (nfreqs = 0; P[nfreqs].f; nfreqs++);
 	return (long)W->iNUM * W->jNUM * W->kNUM;
 }
@@ -196,6 +216,9 @@ double c2_phaser_face_cells(void)
 	for (int s = 0; s < 6; s++) if (on[s]) cells += face[s / 2];
 	return cells;
 }
+
+/* outgoing flux of phaser frequency f (its accumulators to the host) */
+double c2_flux(int f) { return phaserPoyntingOut(P + f); }
 
 long c2_cells(void) { return (long)W->iNUM * W->jNUM * W->kNUM; }
 int c2_nfreq(void) { return nfreqs; }

@@ -26,8 +26,13 @@ cpu_baseline  the oracle restatement of the reference loops on the host
           cores (OpenMP), bounded sample of the same world
 --impl reference  times that CPU implementation alone as the reference arm.
 forms     the batched unit-cell sweep (64 cells) and the served request
-          stream, each against its per-request path, and the same workload
-          with half field storage (--forms 0 skips them)
+          stream, each against its per-request path; the same workload
+          with half field storage; the vacuum plane-wave job (128^3, 2000
+          steps) timed whole on the device and on the host cores, with its
+          phaser spectrum against theirs; and the large domain (1024 x 1024
+          x 512, 200 balls) with float and half storage (--forms 0 skips
+          them)
+--workload c1 | c5  one of those two worlds as the main line instead
 --storage half  E and H stored as IEEE half values with a power-of-two
           exponent per component and x plane, float arithmetic; the
           roofline then counts 2-byte field values (48 B per cell)
@@ -60,11 +65,19 @@ STORAGE = {"float": "float E and H",
            "half": "E and H as IEEE half values times a power of two per component and x plane, float arithmetic"}
 TUNE_STEPS = 16     # the engine times its launch shapes over a world's first 10 half steps of each field
 C5 = (1024, 1024, 512, 200, 128)   # cells per axis with the CPML, balls, phaser frequencies
+C1 = 128                           # cells per axis with the CPML of the vacuum plane-wave workload
+C1_STEPS = 2000                    # its whole job
+SPECTRUM_TOL = 1e-5                # phaser spectra against the host cores' run, relative to the largest value
 
 
 def workload_c5(cells):
     return ("large domain %dx%dx%d (%d seeded Drude-Lorentz balls of radius 20-80 cells in an n=1.5 host, CPML 16, "
             "2 pulsed dipoles, %d-f transmission plane)" % C5)
+
+
+def workload_c1(cells):
+    return ("vacuum plane wave %d^3 (periodic x/y, CPML 16 on z, x-polarized 600 nm pulse, "
+            "16-wavelength phaser plane)" % C1)
 
 
 def workload(cells):
@@ -104,6 +117,8 @@ def build_cpu_baseline():
 
 
 def run_cpu(half, steps, warmup):
+    """The CPU program on the host cores: `half` the domain half size of the
+    scatterer world, or "c1" for the vacuum plane-wave world."""
     exe = build_cpu_baseline()
     env = dict(os.environ)
     env.setdefault("OMP_PROC_BIND", "close")
@@ -269,14 +284,16 @@ def engine_arm(args, rank, world, local):
     eng.alisgpu_launch_count.restype = ctypes.c_ulonglong
     cudart = ctypes.CDLL("libcudart.so.13" if os.path.exists("/usr/local/cuda/lib64/libcudart.so.13") else "libcudart.so")
 
-    c5 = args.workload == "c5"
-    cells = lib.c5_build(*C5) if c5 else lib.c2_build(args.half, NFREQ)
+    lib.c2_flux.restype = ctypes.c_double
+    c5, c1 = args.workload == "c5", args.workload == "c1"
+    cells = lib.c5_build(*C5) if c5 else lib.c1_build(C1) if c1 else lib.c2_build(args.half, NFREQ)
     # the one-world calls, or the batched form (--batched) of the same steps
     steps_fn = lib.c2_steps_batched if args.batched else lib.c2_steps
     stream = ctypes.c_void_p(eng.alisgpu_stream())
     K, W = args.steps, args.warmup
     ring = int(os.environ.get("ALISGPU_PHASER_RING", "64"))
-    R = windows(K, ring, args.timed_steps)
+    # the vacuum plane-wave job is timed whole: one window of its K steps
+    R = 1 if c1 else windows(K, ring, args.timed_steps)
     ev = [ctypes.c_void_p() for _ in range(R + 1)]
     for e in ev:
         cudart.cudaEventCreate(ctypes.byref(e))
@@ -303,6 +320,8 @@ def engine_arm(args, rank, world, local):
             cudart.cudaEventElapsedTime(ctypes.byref(ms), ev[r], ev[r + 1])
             win_ms.append(ms.value)
         dev_s = reduce_max(sum(win_ms) / 1e3, world)
+        # the job's spectrum after the timed window (W + K steps)
+        spectrum = [lib.c2_flux(f) for f in range(lib.c2_nfreq())] if c1 else None
         # end to end through the public API, host timed: R windows of K
         # steps, each read back as the flux result
         barrier(world)
@@ -333,10 +352,25 @@ def engine_arm(args, rank, world, local):
     achieved = step_bytes / (pair_ms / 1e3) / 1e9
     pk, pk_kind = peaks()
     peak = pk.get("hbm_gbs", 6800.0)
-    traffic = None if half_storage else traffic_per_launch_pair()
+    # ncu traffic of the committed capture, taken on the scatterer world
+    traffic = None if half_storage or c1 or c5 else traffic_per_launch_pair()
     total_ms = sum(t for t, _ in kinds.values())
-    cpu_baseline = None
-    if args.cpu_steps > 0 and not c5:
+    cpu_baseline = spectrum_check = None
+    if c1 and args.cpu_steps > 0:
+        # the same job on the host cores: W warm-up and K timed steps, and
+        # its spectrum against the engine's at the same step
+        cpu = run_cpu("c1", K, W)
+        cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
+        cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
+                        "cpu_model": cpu_model(),
+                        "sample": "the whole %d-step job after %d warm-up steps (oracle restatement, OpenMP)" % (K, W)}
+        top = max(abs(v) for v in cpu["flux"]) or 1.0
+        diff = max(abs(a - b) for a, b in zip(spectrum, cpu["flux"])) / top
+        spectrum_check = {"frequencies": len(spectrum), "steps": W + K, "max_rel_diff": diff,
+                          "tolerance": SPECTRUM_TOL, "within": diff <= SPECTRUM_TOL and len(spectrum) == len(cpu["flux"]),
+                          "how": "max |engine - host cores| over the phaser frequencies' outgoing flux, over the "
+                                 "largest |flux|"}
+    elif args.cpu_steps > 0 and not c5:
         cpu = run_cpu(args.half, args.cpu_steps, 1)
         cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
         cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
@@ -348,16 +382,18 @@ def engine_arm(args, rank, world, local):
         "metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": dev_s * 1e3 / (K * R), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": workload_c5(cells) if c5 else workload(cells), "cells": cells,
+        "config": {"workload": workload_c5(cells) if c5 else workload_c1(cells) if c1 else workload(cells), "cells": cells,
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "storage": STORAGE[args.storage],
                    "l2": "inputs larger than L2 (%.0f MB of fields per step)" % (step_bytes / 1e6),
                    "phaser": "%d frequencies, %s, time-blocked ring of %s steps" % (
-                       C5[4] if c5 else NFREQ,
+                       lib.c2_nfreq(),
                        "Kahan-compensated" if os.environ.get("ALISGPU_PHASER_KAHAN") == "1" else "plain float sums",
                        os.environ.get("ALISGPU_PHASER_RING", "64")),
                    "path": "batched launches (alisBatchBegin/End)" if args.batched else "one launch per half step",
-                   "timing": "%d back-to-back windows of %d steps (%d steps, a whole number of %d-step phaser "
+                   "timing": ("the whole %d-step job as one window after %d warm-up steps; value from its device "
+                              "time" % (K, W)) if c1 else
+                             "%d back-to-back windows of %d steps (%d steps, a whole number of %d-step phaser "
                              "ring periods, so the DFT flush is charged at its own rate); value from their total "
                              "device time" % (R, K, R * K, ring),
                    "window_ms": {"median": win_sorted[len(win_sorted) // 2], "min": win_sorted[0],
@@ -377,11 +413,15 @@ def engine_arm(args, rank, world, local):
         "clocks": clocks,
         "result_flux": flux,
     }
-    if args.forms and not c5:
+    if spectrum_check:
+        line["spectrum_vs_cpu"] = spectrum_check
+    if args.forms and not c5 and not c1:
         # the batched and served forms, each against its per-request path,
-        # and the same workload with half field storage
+        # the same workload with half field storage, the vacuum plane-wave
+        # job and the large domain
         line["forms"] = {"sweep": sweep_form(args.forms, threads=8), "served": served_form(),
-                         "half_storage": half_form(args, line)}
+                         "half_storage": half_form(args, line), "plane_wave": plane_wave_form(),
+                         "large_domain": large_domain_form()}
     print(json.dumps(line), flush=True)
 
 
@@ -404,18 +444,58 @@ def half_form(args, line):
     """The workload with E and H stored as half values (--storage half, its
     own process): throughput, the roofline of its half steps over its own
     algorithmic bytes, and its speed against the float line."""
-    cmd = [sys.executable, os.path.abspath(__file__), "--storage", "half", "--steps", str(args.steps),
-           "--warmup", str(args.warmup), "--cpu-steps", "0", "--forms", "0", "--half", str(args.half),
-           "--timed-steps", str(args.timed_steps)]
-    r = subprocess.run(cmd, capture_output=True, text=True, timeout=1800)
-    if r.returncode:
-        return {"error": (r.stdout + r.stderr)[-500:]}
-    h = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    h, err = bench_line(["--storage", "half", "--steps", str(args.steps), "--warmup", str(args.warmup),
+                         "--cpu-steps", "0", "--forms", "0", "--half", str(args.half),
+                         "--timed-steps", str(args.timed_steps)])
+    if err:
+        return err
     return {"storage": STORAGE["half"], "value": h["value"], "unit": h["unit"], "ms_per_step": h["ms_per_step"],
             "e2e": h["e2e"]["value"], "speedup": h["value"] / line["value"],
             "roofline": {k: h["roofline"][k] for k in ("achieved", "peak", "frac", "frac_nominal",
                                                         "algorithmic_bytes_per_step", "launch_pair_ms")},
             "clocks": h["clocks"], "result_flux": h["result_flux"]}
+
+
+def bench_line(extra):
+    """One run of this bench in its own process (its own world and
+    device memory): its JSON line, or the error."""
+    r = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True,
+                       timeout=1800)
+    if r.returncode:
+        return None, {"error": (r.stdout + r.stderr)[-500:]}
+    return json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1]), None
+
+
+def plane_wave_form():
+    """The vacuum plane-wave job (128^3, 2000 steps) timed whole on the
+    device and on the host cores, and its phaser spectrum against the host
+    cores' at the same step."""
+    h, err = bench_line(["--workload", "c1", "--steps", str(C1_STEPS), "--warmup", str(TUNE_STEPS),
+                         "--cpu-steps", str(C1_STEPS), "--forms", "0"])
+    if err:
+        return err
+    return {"workload": h["config"]["workload"], "steps": h["steps"], "value": h["value"], "unit": h["unit"],
+            "job_ms": h["ms_per_step"] * h["steps"], "e2e": h["e2e"]["value"],
+            "roofline": {k: h["roofline"][k] for k in ("achieved", "peak", "frac", "algorithmic_bytes_per_step",
+                                                        "launch_pair_ms")},
+            "cpu_baseline": h["cpu_baseline"], "spectrum_vs_cpu": h.get("spectrum_vs_cpu"), "clocks": h["clocks"]}
+
+
+def large_domain_form():
+    """The large domain (1024 x 1024 x 512, 200 balls) with float and with
+    half field storage: 256 timed steps each (four 64-step windows)."""
+    out = {}
+    for storage in ("float", "half"):
+        h, err = bench_line(["--workload", "c5", "--storage", storage, "--steps", "64", "--warmup", str(TUNE_STEPS),
+                             "--timed-steps", "256", "--cpu-steps", "0", "--forms", "0"])
+        out[storage] = err or {
+            "value": h["value"], "unit": h["unit"], "ms_per_step": h["ms_per_step"], "e2e": h["e2e"]["value"],
+            "roofline": {k: h["roofline"][k] for k in ("achieved", "peak", "frac", "algorithmic_bytes_per_step",
+                                                        "launch_pair_ms")},
+            "clocks": h["clocks"]}
+        if not err:
+            out["workload"] = h["config"]["workload"]
+    return out
 
 
 def serve_exe():
@@ -494,15 +574,18 @@ def main():
     ap.add_argument("--sweep", type=int, default=0, metavar="N",
                     help="run the batched unit-cell sweep of N cells instead (512: the full sweep)")
     ap.add_argument("--sweep-steps", type=int, default=0, help="steps per unit cell (default 3000)")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c5"],
-                    help="c2: the dispersive scatterer (256^3, the headline); c5: the large-domain precision "
-                         "workload (1024 x 1024 x 512, 200 balls), for its float and half storage throughput")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c5"],
+                    help="c2: the dispersive scatterer (256^3, the headline); c1: the vacuum plane wave (128^3, "
+                         "timed as one window of --steps, its spectrum against the host cores' run); c5: the "
+                         "large-domain precision workload (1024 x 1024 x 512, 200 balls), for its float and half "
+                         "storage throughput")
     ap.add_argument("--storage", default="float", choices=sorted(STORAGE),
                     help="field storage of the world: float, or half values with a power-of-two exponent per "
                          "component and x plane (alisgpu_world_set_storage)")
     ap.add_argument("--forms", type=int, default=64, metavar="N",
                     help="after the main line's timing, the batched sweep of N unit cells and the served stream, "
-                         "each against its per-request path, as the line's 'forms' (0: skip)")
+                         "each against its per-request path, the half-storage run, the vacuum plane-wave job and "
+                         "the large domain, as the line's 'forms' (0: skip)")
     args = ap.parse_args()
     if args.sweep:
         sweep_arm(args)

@@ -3,9 +3,12 @@
  * dispersive-scatterer benchmark.  The benchmark world of
  * alis_gb300/bench/c2.c is built through the public API and stepped by the
  * oracle restatement of the reference loops (cpu_step.c) on all host
- * cores with OpenMP, as the reference build runs.  Prints one JSON object.
+ * cores with OpenMP, as the reference build runs.  Prints one JSON object
+ * with the timing and the outgoing flux of every phaser frequency after
+ * the last step.  With `c1` in place of the half size the vacuum
+ * plane-wave world of c1_build (128^3 cells) is built instead.
  *
- *   c2_cpu <half-size nm> <timed steps> <warm-up steps>
+ *   c2_cpu <half-size nm | c1> <timed steps> <warm-up steps>
  */
 #include <omp.h>
 #include <sys/time.h>
@@ -20,17 +23,19 @@ static double now(void)
 
 int main(int argc, char **argv)
 {
-	int half = argc > 1 ? atoi(argv[1]) : 230;
+	const char *what = argc > 1 ? argv[1] : "230";
 	int steps = argc > 2 ? atoi(argv[2]) : 5;
 	int warm = argc > 3 ? atoi(argv[3]) : 1;
 	double t0 = now();
-	long cells = c2_build(half, 64);
+	long cells = strcmp(what, "c1") ? c2_build(atoi(what), 64) : c1_build(128);
 	double t1 = now();
 	c2_steps(warm);
 	double t2 = now();
 	c2_steps(steps);
 	double t3 = now();
-	printf("{\"cells\": %ld, \"steps\": %d, \"seconds\": %.6f, \"setup_seconds\": %.3f, \"warmup_seconds\": %.3f, \"threads\": %d}\n",
+	printf("{\"cells\": %ld, \"steps\": %d, \"seconds\": %.6f, \"setup_seconds\": %.3f, \"warmup_seconds\": %.3f, \"threads\": %d, \"flux\": [",
 	       cells, steps, t3 - t2, t1 - t0, t2 - t1, omp_get_max_threads());
+	for (int f = 0; f < c2_nfreq(); f++) printf("%s%.9g", f ? ", " : "", c2_flux(f));
+	printf("]}\n");
 	return 0;
 }
