@@ -142,8 +142,10 @@ struct HalfStepParams {
 	float *Fother[3];                     // E of set m during the H step (ADE drive)
 	unsigned int *err;                    // device error word
 	// per-axis classification of cells (indexed from MIN): bits 0-7 object
-	// n's range, bit 8 any object n >= 8, bit 13/14 CPML slab of the min/max
-	// face, bit 15 TFSF face plane
+	// n's range, bit 8 any object n >= 8, bit 12 within a TFSF box's index
+	// range (one cell of margin), bit 13/14 CPML slab of the min/max face,
+	// bit 15 TFSF face plane.  A cell takes TFSF corrections only where all
+	// three axes have bit 12 and one has bit 15 (tfsfBits).
 	const unsigned short *cls[3];
 	// worlds with more than 8 objects: per tile of ALIS_TILE_K cells along
 	// k x ALIS_TILE_J rows x 1 plane, the objects whose box meets it, in
@@ -156,9 +158,17 @@ struct HalfStepParams {
 #define ALIS_TILE_K 32
 #define ALIS_TILE_J 8
 #define CLS_OBJ8 0x100u
+#define CLS_TFSF_IN 0x1000u
 #define CLS_PML_LO 0x2000u
 #define CLS_PML_HI 0x4000u
 #define CLS_TFSF 0x8000u
+
+// CLS_TFSF where the cell may lie on a TFSF box face (a face plane in
+// one axis, the box's range in the others), else 0
+__device__ __forceinline__ unsigned tfsfBits(unsigned bi, unsigned bj, unsigned bk)
+{
+	return (bi & bj & bk & CLS_TFSF_IN) ? (bi | bj | bk) & CLS_TFSF : 0u;
+}
 
 // the eps^-1 triple of cell c from the material index
 __device__ __forceinline__ float4 matTriple(const HalfStepParams &P, int c)

@@ -1305,7 +1305,7 @@ __device__ __forceinline__ void stepCell(const HalfStepParams &P, int i, int j, 
 		if (bk & CLS_PML_HI) pmlFace<5>(PML_ARGS);
 #undef PML_ARGS
 	}
-	if (any & CLS_TFSF) tfsfCell<ALT>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
+	if (tfsfBits(bi, bj, bk)) tfsfCell<ALT>(P, i, j, k, fx, fy, fz, hasC, cx, cy, cz);
 	if (ALT == -1 && objm) objectsAfterCurl(P, i, j, k, gx0, gy0, gz0, objm, list, nIter);
 	storeCell<HALF>(P, i, c, fx, fy, fz);
 }
@@ -1387,7 +1387,7 @@ __device__ __forceinline__ void leanCells(const HalfStepParams &P, int i, int j,
 #undef PML_ARGS
 		}
 		// TFSF k face planes (cells on an i or j face plane are hard)
-		if (bk[q] & CLS_TFSF) tfsfCell<ALT, true>(P, i, j, kq, fx[q], fy[q], fz[q], hasC, cx[q], cy[q], cz[q]);
+		if (tfsfBits(bi, bj, bk[q])) tfsfCell<ALT, true>(P, i, j, kq, fx[q], fy[q], fz[q], hasC, cx[q], cy[q], cz[q]);
 		storeCell<HALF>(P, i, c, fx[q], fy[q], fz[q]);
 	}
 }
@@ -1459,13 +1459,14 @@ __device__ __forceinline__ void halfStepBlock(const HalfStepParams &P, int bx, i
 	unsigned bi = 0, bj = 0, bk = 0;
 	if (inRange) bi = __ldg(P.cls[0] + (i - P.iMIN)), bj = __ldg(P.cls[1] + (j - P.jMIN)), bk = __ldg(P.cls[2] + (k - P.kMIN));
 	const unsigned objm = objTile ? bi & bj & bk & 0x1FFu : 0u;
-	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI | CLS_TFSF)) && !objm;
+	const unsigned tf = tfsfBits(bi, bj, bk);
+	const bool plain = inRange && !((bi | bj | bk) & (CLS_PML_LO | CLS_PML_HI)) && !tf && !objm;
 	if (__all_sync(0xffffffffu, plain)) {
 		plainCell<ALT, HALF>(P, i, j, k);
 		return;
 	}
 	if (!inRange) return;
-	if (!((bi | bj) & CLS_TFSF) && !objm) {
+	if (!(tf && ((bi | bj) & CLS_TFSF)) && !objm) {
 		leanCells<ALT, 1, HALF>(P, i, j, k, bi, bj, &bk);
 		return;
 	}
@@ -2983,8 +2984,8 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 	for (int f = 0; f < 6; f++) key.push_back(P.slabOn[f]), key.push_back(P.slabLo[f]), key.push_back(P.slabHi[f]);
 	for (int q = 0; q < P.ntfsf; q++) {
 		const DevTfsf &T = P.tf[q];
-		const int b[6] = { T.iMin, T.iMax, T.jMin, T.jMax, T.kMin, T.kMax };
-		key.insert(key.end(), b, b + 6);
+		const int b[12] = { T.iMin, T.iMax, T.jMin, T.jMax, T.kMin, T.kMax, T.iMIN, T.iMAX, T.jMIN, T.jMAX, T.kMIN, T.kMAX };
+		key.insert(key.end(), b, b + 12);
 	}
 	for (const DevObj &o : w->objs) {
 		const int b[6] = { o.i0, o.i1, o.j0, o.j1, o.k0, o.k1 };
@@ -3005,9 +3006,13 @@ extern "C" int alisgpu_half_step_run(alisgpu_world *w, const alisgpu_half_step *
 		for (int q = 0; q < P.ntfsf; q++) {
 			const DevTfsf &T = P.tf[q];
 			int mn[3] = { T.iMin, T.jMin, T.kMin }, mx[3] = { T.iMax, T.jMax, T.kMax };
+			int MN[3] = { T.iMIN, T.jMIN, T.kMIN }, MX[3] = { T.iMAX, T.jMAX, T.kMAX };
 			for (int a = 0; a < 3; a++) {
 				if (mn[a] > lo0[a]) mark(a, mn[a], mn[a], CLS_TFSF);
 				if (mx[a] < hi0[a]) mark(a, mx[a] + field, mx[a] + field, CLS_TFSF);
+				// the index range of the faces' corrections: every face
+				// plane and every range tfsfCell tests along this axis
+				mark(a, min(mn[a], MN[a]) - 1, max(mx[a], MX[a]) + 1, CLS_TFSF_IN);
 			}
 		}
 		for (size_t q = 0; q < w->objs.size(); q++) {
