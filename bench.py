@@ -131,6 +131,11 @@ def run_cpu(half, steps, warmup):
     return json.loads(line)
 
 
+def cpu_split(cpu):
+    """Seconds of the timed steps in updateE + updateH and in updatePhaser."""
+    return {"update": cpu.get("update_seconds"), "phaser": cpu.get("phaser_seconds")}
+
+
 class Clocks:
     """nvidia-smi samples of SM clock and throttle reasons while running."""
 
@@ -254,7 +259,7 @@ def reference_arm(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": workload(cpu["cells"]), "cells": cpu["cells"], "parallelism": "host cores (OpenMP)"},
         "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
-                         "cpu_model": model, "sample": sample},
+                         "cpu_model": model, "split_s": cpu_split(cpu), "sample": sample},
         "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -362,7 +367,7 @@ def engine_arm(args, rank, world, local):
         cpu = run_cpu("c1", K, W)
         cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
         cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
-                        "cpu_model": cpu_model(),
+                        "cpu_model": cpu_model(), "split_s": cpu_split(cpu),
                         "sample": "the whole %d-step job after %d warm-up steps (oracle restatement, OpenMP)" % (K, W)}
         top = max(abs(v) for v in cpu["flux"]) or 1.0
         diff = max(abs(a - b) for a, b in zip(spectrum, cpu["flux"])) / top
@@ -374,7 +379,7 @@ def engine_arm(args, rank, world, local):
         cpu = run_cpu(args.half, args.cpu_steps, 1)
         cpu_rate = cpu["cells"] * cpu["steps"] / cpu["seconds"] / 1e9
         cpu_baseline = {"value": cpu_rate, "unit": "Gcell/s", "cores": cpu["threads"], "kind": "port",
-                        "cpu_model": cpu_model(),
+                        "cpu_model": cpu_model(), "split_s": cpu_split(cpu),
                         "sample": "%d steps of the full world after 1 warm-up step (oracle restatement, OpenMP)" % cpu["steps"]}
     value = cells * K * R * world / dev_s / 1e9
     win_sorted = sorted(win_ms)

@@ -4,8 +4,8 @@
  * alis_gb300/bench/c2.c is built through the public API and stepped by the
  * oracle restatement of the reference loops (cpu_step.c) on all host
  * cores with OpenMP, as the reference build runs.  Prints one JSON object
- * with the timing and the outgoing flux of every phaser frequency after
- * the last step.  With `c1` in place of the half size the vacuum
+ * with the timing (also updateE + updateH and updatePhaser apart) and the
+ * outgoing flux of every phaser frequency after the last step.  With `c1` in place of the half size the vacuum
  * plane-wave world of c1_build (128^3 cells) is built instead.
  *
  *   c2_cpu <half-size nm | c1> <timed steps> <warm-up steps>
@@ -31,10 +31,20 @@ int main(int argc, char **argv)
 	double t1 = now();
 	c2_steps(warm);
 	double t2 = now();
-	c2_steps(steps);
+	/* the steps of c2_steps, with updateE + updateH and updatePhaser timed apart */
+	double tUpdate = 0, tPhaser = 0;
+	for (int q = 0; q < steps; q++) {
+		const double a = omp_get_wtime();
+		updateE(W);
+		updateH(W);
+		const double b = omp_get_wtime();
+		updatePhaser(W, P);
+		tUpdate += b - a, tPhaser += omp_get_wtime() - b;
+	}
 	double t3 = now();
-	printf("{\"cells\": %ld, \"steps\": %d, \"seconds\": %.6f, \"setup_seconds\": %.3f, \"warmup_seconds\": %.3f, \"threads\": %d, \"flux\": [",
-	       cells, steps, t3 - t2, t1 - t0, t2 - t1, omp_get_max_threads());
+	printf("{\"cells\": %ld, \"steps\": %d, \"seconds\": %.6f, \"update_seconds\": %.6f, \"phaser_seconds\": %.6f, "
+	       "\"setup_seconds\": %.3f, \"warmup_seconds\": %.3f, \"threads\": %d, \"flux\": [",
+	       cells, steps, t3 - t2, tUpdate, tPhaser, t1 - t0, t2 - t1, omp_get_max_threads());
 	for (int f = 0; f < c2_nfreq(); f++) printf("%s%.9g", f ? ", " : "", c2_flux(f));
 	printf("]}\n");
 	return 0;
