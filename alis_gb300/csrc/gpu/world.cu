@@ -1911,8 +1911,12 @@ static void launchHalfStep(int v, dim3 grid, const HalfStepParams &P, const Fuse
 // Batched launches over many worlds (batch.cuh)
 // ---------------------------------------------------------------------
 // the tiles of a batched entry: nbx x nby tiles of 32 x BATCH_TY cells
-// per i plane, planes in the half step's sweep order
+// per i plane, planes in the half step's sweep order (2, 4 or 8; 4 unless
+// the build defines it)
+#ifndef BATCH_TY
 #define BATCH_TY 4
+#endif
+static_assert(BATCH_TY == 2 || BATCH_TY == 4 || BATCH_TY == 8, "BATCH_TY divides the object tiles' 8 rows");
 // n / d for 0 <= n < 2^31 as (n m) >> sh, with m = ceil(2^sh / d) and
 // sh = 31 + ceil(log2 d): the product's error stays below 1/d for every
 // such n (checked exhaustively over the divisors a launch uses)
