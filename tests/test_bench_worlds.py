@@ -1,16 +1,20 @@
 """The CPU program behind bench.py's host-core baseline builds the vacuum
 plane-wave world at 128^3 cells (periodic x/y, the 16-cell z CPML counted
 in) with its 16 phaser wavelengths, and reports the outgoing flux of each;
-two runs of the same steps report the same spectrum."""
+two runs of the same steps report the same spectrum.  On the GPU, the
+whole 2000-step job of that world through the engine reproduces the host
+cores' spectrum within 1e-5 of the largest flux."""
 import json
 import os
 import subprocess
+import sys
+
+import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def run(steps, warm):
-    import sys
     sys.path.insert(0, ROOT)
     import bench
     exe = bench.build_cpu_baseline()
@@ -28,3 +32,16 @@ def test_plane_wave_world_and_spectrum():
     assert any(v != 0 for v in a["flux"])
     b = run(300, 3)
     assert a["flux"] == b["flux"]
+
+
+@pytest.mark.gpu
+def test_plane_wave_job_spectrum_matches_host_cores():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--workload", "c1", "--steps", "2000",
+                        "--warmup", "16", "--cpu-steps", "2000", "--forms", "0"],
+                       capture_output=True, text=True, timeout=900, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1])
+    assert line["config"]["cells"] == 128 ** 3
+    check = line["spectrum_vs_cpu"]
+    assert check["frequencies"] == 16 and check["steps"] == line["warmup"] + 2000
+    assert check["within"] and check["max_rel_diff"] <= 1e-5, check
