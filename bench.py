@@ -466,9 +466,12 @@ def half_form(args, line):
 
 def bench_line(extra):
     """One run of this bench in its own process (its own world and
-    device memory): its JSON line, or the error."""
+    device memory, on this rank's device, as a single process outside any
+    torchrun group): its JSON line, or the error."""
+    env = {k: v for k, v in os.environ.items()
+           if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "LOCAL_WORLD_SIZE", "GROUP_RANK", "MASTER_ADDR", "MASTER_PORT")}
     r = subprocess.run([sys.executable, os.path.abspath(__file__)] + extra, capture_output=True, text=True,
-                       timeout=1800)
+                       timeout=1800, env=env)
     if r.returncode:
         return None, {"error": (r.stdout + r.stderr)[-500:]}
     return json.loads([l for l in r.stdout.splitlines() if l.startswith("{")][-1]), None

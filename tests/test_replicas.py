@@ -54,3 +54,27 @@ def test_reduce_max_two_ranks(tmp_path):
     r = _torchrun([str(script)])
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     assert "max 1.0" in r.stdout
+
+
+def test_form_processes_leave_the_torchrun_group(monkeypatch):
+    """The forms that run bench.py again in a process of their own do so
+    as a single process on the rank's device: without the torchrun
+    group's variables, with ALISGPU_DEVICE."""
+    import bench
+    seen = {}
+
+    class Failed:
+        returncode, stdout, stderr = 1, "", "not run"
+
+    def fake_run(cmd, **kw):
+        seen.update(kw.get("env") or {})
+        return Failed()
+
+    for k, v in (("RANK", "1"), ("WORLD_SIZE", "2"), ("LOCAL_RANK", "1"), ("MASTER_ADDR", "127.0.0.1"),
+                 ("MASTER_PORT", "29500"), ("ALISGPU_DEVICE", "1")):
+        monkeypatch.setenv(k, v)
+    monkeypatch.setattr(bench.subprocess, "run", fake_run)
+    line, err = bench.bench_line(["--workload", "c1"])
+    assert line is None and err
+    assert not {"RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"} & set(seen)
+    assert seen.get("ALISGPU_DEVICE") == "1"
