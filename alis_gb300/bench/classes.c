@@ -14,6 +14,9 @@
  *   4  as 0 with a TFSF plane-wave box [-160, 158]^3 nm instead of the
  *      dipole
  *   5  the dispersive-scatterer benchmark world (c2.c)
+ *   6  the large-domain world of c5_build at 512 x 512 x 256 cells with 25
+ *      balls (about the same ball density), a 16-frequency phaser box
+ *   7  as 6 without the balls (the n = 1.5 host only)
  *
  * Prints the cells, the mean E and H launch times, their sum and the
  * algorithmic bytes per step (c2_step_bytes) over it.
@@ -27,6 +30,8 @@ int main(int argc, char **argv)
 	const int steps = argc > 2 ? atoi(argv[2]) : 64;
 	if (kind == 5) {
 		c2_build(230, 64);
+	} else if (kind == 6 || kind == 7) {
+		c5_build(512, 512, 256, kind == 6 ? 25 : 0, 16);
 	} else {
 		const float L = 256;
 		dom D = {{-L, L-2}, {-L, L-2}, {-L, L-2}};

@@ -1080,20 +1080,26 @@ __device__ __forceinline__ void objectsBeforeCurl(const HalfStepParams &P, int i
 __device__ __forceinline__ void objectsAfterCurl(const HalfStepParams &P, int i, int j, int k,
 	float gx0, float gy0, float gz0, unsigned objm, const int *list, int nIter)
 {
+	// poles outer, the three axes inner: the axes' updates of a pole are
+	// independent, and each current sees the same operations as in the
+	// reference's loop order
 	FOR_CELL_OBJECTS(
 		const float e[3] = { gx0, gy0, gz0 };
+		const float fe[3] = { o.fill[0][b], o.fill[1][b], o.fill[2][b] };
+		for (int p = 0; p < o.NJ; p++) {
 #pragma unroll
-		for (int a = 0; a < 3; a++) {
-			const float fe = o.fill[a][b];
-			for (int p = 0; p < o.NJ; p++) {
+			for (int a = 0; a < 3; a++) {
 				float *J = o.J[P.m][p][a];
-				J[b] = o.JJ[p][a] * J[b] + o.JE[p][a] * fe * e[a];
+				J[b] = o.JJ[p][a] * J[b] + o.JE[p][a] * fe[a] * e[a];
 			}
-			for (int p = o.NJ; p < o.NK; p++) {
+		}
+		for (int p = o.NJ; p < o.NK; p++) {
+#pragma unroll
+			for (int a = 0; a < 3; a++) {
 				float *J = o.J[P.m][p][a], *K = o.K[P.m][p][a];
-				float jn = o.JJ[p][a] * J[b] + o.JK[p][a] * K[b] + o.JE[p][a] * fe * e[a];
+				float jn = o.JJ[p][a] * J[b] + o.JK[p][a] * K[b] + o.JE[p][a] * fe[a] * e[a];
 				J[b] = jn;
-				K[b] = o.KJ[p][a] * jn + o.KK[p][a] * K[b] + o.KE[p][a] * fe * e[a];
+				K[b] = o.KJ[p][a] * jn + o.KK[p][a] * K[b] + o.KE[p][a] * fe[a] * e[a];
 			}
 		})
 }
