@@ -3,7 +3,9 @@ plane-wave world at 128^3 cells (periodic x/y, the 16-cell z CPML counted
 in) with its 16 phaser wavelengths, and reports the outgoing flux of each;
 two runs of the same steps report the same spectrum.  On the GPU, the
 whole 2000-step job of that world through the engine reproduces the host
-cores' spectrum within 1e-5 of the largest flux."""
+cores' spectrum within 1e-5 of the largest flux.  The large-domain
+workload's 200 seeded balls lie inside the domain, meet no other ball and
+come out the same on every draw."""
 import json
 import os
 import subprocess
@@ -45,3 +47,24 @@ def test_plane_wave_job_spectrum_matches_host_cores():
     check = line["spectrum_vs_cpu"]
     assert check["frequencies"] == 16 and check["steps"] == line["warmup"] + 2000
     assert check["within"] and check["max_rel_diff"] <= 1e-5, check
+
+
+def test_large_domain_balls_inside_and_apart(tmp_path):
+    import numpy as np
+    exe = str(tmp_path / "c5_balls_check")
+    src = os.path.join(ROOT, "tests", "drivers", "c5_balls_check.c")
+    subprocess.run(["gcc", "-std=gnu99", "-O2", src, "-o", exe], check=True)
+    args = [exe, "99", "200", "1024", "1024", "512", "5"]
+    out = subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    assert out == subprocess.run(args, capture_output=True, text=True, check=True).stdout
+    lines = out.strip().splitlines()
+    dom = [float(v) for v in lines[-1].split()[1:]]
+    B = np.array([[float(v) for v in l.split()] for l in lines[:-1]])
+    assert B.shape == (200, 4)
+    x, r = B[:, :3], B[:, 3]
+    assert ((r >= 5 * 20) & (r <= 5 * 80)).all()
+    for a in range(3):
+        assert (x[:, a] - r >= dom[2 * a] - 1e-3).all() and (x[:, a] + r <= dom[2 * a + 1] + 1e-3).all()
+    d = np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+    np.fill_diagonal(d, np.inf)
+    assert (d >= r[:, None] + r[None, :] - 1e-3).all()
