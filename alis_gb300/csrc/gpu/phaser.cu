@@ -114,10 +114,9 @@ __device__ __forceinline__ float addHalf(float a, float p)
 #define FLUSH_FREQ 8
 #define FLUSH_SUB 8                              // ring steps per compensated add
 
-// thread = one (face cell, component); loops over a chunk of frequencies
-template <bool KAHAN>
-__device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
-                                           long long n4, int nfreq, int steps, long long bx, int by, float2 *sph)
+// the phase factors of frequency group by (FLUSH_FREQ frequencies) for
+// every ring step, into shared memory: [steps][FLUSH_FREQ][E, H]
+__device__ __forceinline__ void flushPhases(const float2 *phase, int nfreq, int steps, int by, float2 *sph)
 {
 	const int f0 = by * FLUSH_FREQ;
 	const int nf = min(FLUSH_FREQ, nfreq - f0);
@@ -125,9 +124,16 @@ __device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2
 		int s = q / (FLUSH_FREQ * 2), r = q % (FLUSH_FREQ * 2), ff = r / 2, h = r % 2;
 		sph[q] = ff < nf ? phase[((long long)s * nfreq + f0 + ff) * 2 + h] : make_float2(0, 0);
 	}
-	__syncthreads();
-	long long t = bx * blockDim.x + threadIdx.x;
-	if (t >= n4) return;
+}
+
+// one (face cell, component) t over frequency group by: ring step s of
+// the cell is buf[s * xs]
+template <bool KAHAN>
+__device__ __forceinline__ void flushCell(const float *buf, long long xs, float2 *acc, float2 *comp, long long n4,
+                                          int nfreq, int steps, long long t, int by, const float2 *sph)
+{
+	const int f0 = by * FLUSH_FREQ;
+	const int nf = min(FLUSH_FREQ, nfreq - f0);
 	const bool isH = (t & 3) >= 2;
 	float2 a[FLUSH_FREQ], cc[FLUSH_FREQ];
 #pragma unroll
@@ -141,7 +147,7 @@ __device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2
 	if (!KAHAN) {
 		// the reference's sums, term by term in its rounding
 		for (int s = 0; s < steps; s++) {
-			const float x = buf[(long long)s * n4 + t];
+			const float x = buf[(long long)s * xs];
 #pragma unroll
 			for (int ff = 0; ff < FLUSH_FREQ; ff++) {
 				if (ff >= nf) break;
@@ -161,7 +167,7 @@ __device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2
 			for (int ff = 0; ff < FLUSH_FREQ; ff++) part[ff] = make_float2(0, 0);
 			const int s1 = min(s0 + FLUSH_SUB, steps);
 			for (int s = s0; s < s1; s++) {
-				const float x = isH ? 0.5f * buf[(long long)s * n4 + t] : buf[(long long)s * n4 + t];
+				const float x = isH ? 0.5f * buf[(long long)s * xs] : buf[(long long)s * xs];
 #pragma unroll
 				for (int ff = 0; ff < FLUSH_FREQ; ff++) {
 					const float2 p = sph[(s * FLUSH_FREQ + ff) * 2 + (isH ? 1 : 0)];
@@ -186,12 +192,45 @@ __device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2
 	}
 }
 
+// thread = one (face cell, component) of cell block bx; frequency group by
+template <bool KAHAN>
+__device__ __forceinline__ void flushBlock(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
+                                           long long n4, int nfreq, int steps, long long bx, int by, float2 *sph)
+{
+	flushPhases(phase, nfreq, steps, by, sph);
+	__syncthreads();
+	const long long t = bx * blockDim.x + threadIdx.x;
+	if (t < n4) flushCell<KAHAN>(buf + t, n4, acc, comp, n4, nfreq, steps, t, by, sph);
+}
+
 template <bool KAHAN>
 __global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush(const float *buf, float2 *acc, float2 *comp, const float2 *phase,
                                                                 long long n4, int nfreq, int steps)
 {
 	extern __shared__ float2 sph[];                 // [steps][FLUSH_FREQ][2]
 	flushBlock<KAHAN>(buf, acc, comp, phase, n4, nfreq, steps, blockIdx.x, blockIdx.y, sph);
+}
+
+// The flush with the block's ring entries staged once: each block reads
+// the ring steps of its FLUSH_THREADS (cell, component) pairs into shared
+// memory and runs every frequency group from there, so the ring is read
+// from memory once instead of once per group.  Each accumulator sums the
+// same terms in the same order as k_phaser_flush.
+template <bool KAHAN>
+__global__ void __launch_bounds__(FLUSH_THREADS) k_phaser_flush_staged(const float *buf, float2 *acc, float2 *comp,
+                                                                       const float2 *phase, long long n4, int nfreq, int steps)
+{
+	extern __shared__ float2 sph[];                 // [steps][FLUSH_FREQ][2], then the ring [steps][FLUSH_THREADS]
+	float *ring = (float *)(sph + steps * FLUSH_FREQ * 2);
+	const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+	for (int st = 0; st < steps; st++) ring[st * blockDim.x + threadIdx.x] = t < n4 ? buf[(long long)st * n4 + t] : 0.0f;
+	const int groups = (nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ;
+	for (int by = 0; by < groups; by++) {
+		__syncthreads();                            // the previous group's phases are no longer read
+		flushPhases(phase, nfreq, steps, by, sph);
+		__syncthreads();
+		if (t < n4) flushCell<KAHAN>(ring + threadIdx.x, blockDim.x, acc, comp, n4, nfreq, steps, t, by, sph);
+	}
 }
 
 // ---- batched phaser work (batch.cuh): every recorded phaser's flush in
@@ -354,7 +393,13 @@ extern "C" int alisgpu_phaser_flush(alisgpu_phaser *p)
 	dim3 grid((unsigned)((n4 + FLUSH_THREADS - 1) / FLUSH_THREADS), (p->nfreq + FLUSH_FREQ - 1) / FLUSH_FREQ);
 	size_t smem = (size_t)p->used * FLUSH_FREQ * 2 * sizeof(float2);
 	int slot = alisgpu__prof_start();
-	if (p->kahan) k_phaser_flush<true><<<grid, FLUSH_THREADS, smem, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
+	// the ring staged per block where phases and ring fit 48 KB (a ring of
+	// up to 64 steps), else one block per cell block and frequency group
+	const size_t staged = smem + (size_t)p->used * FLUSH_THREADS * sizeof(float);
+	if (staged <= 48 * 1024) {
+		if (p->kahan) k_phaser_flush_staged<true><<<grid.x, FLUSH_THREADS, staged, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
+		else k_phaser_flush_staged<false><<<grid.x, FLUSH_THREADS, staged, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
+	} else if (p->kahan) k_phaser_flush<true><<<grid, FLUSH_THREADS, smem, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
 	else k_phaser_flush<false><<<grid, FLUSH_THREADS, smem, st>>>(p->buf, p->acc, p->comp, p->phase, n4, p->nfreq, p->used);
 	alisgpu__prof_stop(slot, ALISGPU_K_FLUSH);
 	alisgpu__count_launch();
